@@ -1,0 +1,133 @@
+/*
+ * ptycho_gb300.h -- C ABI of the GB300 ptychography engine (libptycho_gb300.so).
+ *
+ * The reference (andyofmelbourne/Ptychography) is a Python/NumPy package with
+ * no native interface; each entry point below replaces the reference function
+ * it cites (file:line within that project), and takes plain device pointers,
+ * sizes and a cudaStream_t passed as void*.  The Python drop-in
+ * (ptychography_gb300.ERA / DM) binds these through ctypes.
+ *
+ * Conventions
+ *   - complex arrays are interleaved complex64 (NumPy/torch complex64 layout);
+ *   - detector-plane arrays (amp, mask, background, Pamp) are in unshifted FFT
+ *     order, i.e. already ifftshift-ed as the reference's preamble does
+ *     (ptychography/era.py:497-499, 543);
+ *   - scan offsets R are int64 [n][2], every entry <= 0 (the preamble's shift,
+ *     era.py:504-505), and each probe window must lie inside the object;
+ *   - all buffers belong to the caller; the library never frees them.  A plan
+ *     owns its own device scratch (tile lists, partial sums);
+ *   - every call is stream-ordered; none synchronises the host;
+ *   - return value: PTY_OK (0) or an error code; pty_last_error() describes
+ *     the most recent error on the calling thread.
+ * Calls on one plan are not thread-safe; distinct plans are independent.
+ */
+#ifndef PTYCHO_GB300_H
+#define PTYCHO_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PTY_OK 0
+#define PTY_ERR_ARG 1         /* null pointer, bad method or option */
+#define PTY_ERR_SHAPE 2       /* frame shape has no kernel */
+#define PTY_ERR_RANGE 3       /* a scan window falls outside the object */
+#define PTY_ERR_CUDA 4        /* a CUDA runtime call failed */
+#define PTY_ERR_NOMEM 5       /* device scratch allocation failed */
+#define PTY_ERR_UNSUPPORTED 6 /* valid request the engine does not implement */
+
+typedef struct pty_plan pty_plan;
+
+/* n frames of N0 x N1 detector pixels; object U x V. */
+typedef struct {
+  int32_t n_frames, N0, N1, U, V;
+} pty_geometry;
+
+/* Device buffers of one reconstruction (all device pointers). */
+typedef struct {
+  void* O;                  /* complex64 [U][V] object, in/out */
+  void* P;                  /* complex64 [N0][N1] probe, in/out */
+  void* psi;                /* complex64 [n][N0][N1] exit waves: DM state, ERA scratch */
+  const float* amp;         /* float32 [n][N0][N1] sqrt(I) */
+  const uint8_t* mask;      /* uint8 [N0][N1], 1 = valid pixel; NULL = all valid */
+  float* background;        /* float32 [n][N0][N1] sqrt-background state (methods 4-6) */
+  const float* Pamp;        /* float32 [N0][N1] |FFT(P0)| for Pmod_probe; NULL if unused */
+  float* background_mean;   /* float32 [N0][N1] out: final frame-mean sqrt-background */
+  double* heatmap;          /* float64 [U][V] out: P_heatmap, or NULL */
+  float* intensities;       /* float32 [n][N0][N1] out: fftshift |FFT psi|^2, or NULL */
+  double* eMod;             /* float64 [iters] out: modulus error history */
+  double* eCon;             /* float64 [iters] out: convergence error history */
+} pty_buffers;
+
+typedef struct {
+  int32_t method;           /* 1..6, ptychography/era.py:61-78 */
+  int32_t OP_iters0;        /* OP rounds per update, era.py:49-55 */
+  int32_t OP_iters1;        /* update the probe every OP_iters1 iterations */
+  int64_t Pmod_probe;       /* apply Pmod_P while iteration < Pmod_probe */
+  int32_t probe_centering;  /* era.py:171-186 */
+  int32_t use_graph;        /* capture the whole loop in one CUDA graph */
+  double alpha;             /* regulariser, era.py:90-91 */
+  double I_norm;            /* sum(mask * I), era.py:495 */
+} pty_options;
+
+/* Plan for one scan geometry: uploads R, builds the per-tile frame lists of
+ * the overlap gathers and the FFT twiddles.  Replaces the set-up half of
+ * preamble(), ptychography/era.py:435-548 (R must already be shifted). */
+int pty_plan_create(const pty_geometry* geom, const int64_t* R_host, pty_plan** plan_out);
+int pty_plan_destroy(pty_plan* plan);
+
+/* Whole reconstructions.  pty_era replaces ERA, ptychography/era.py:13-332;
+ * pty_dm replaces DM, ptychography/dm.py:13-333.  *heatmap_valid (host) is
+ * set to 0 when the reference would report info['heatmap'] = None. */
+int pty_era(pty_plan* plan, const pty_buffers* buf, const pty_options* opt, int32_t iters,
+            int32_t* heatmap_valid, void* stream);
+int pty_dm(pty_plan* plan, const pty_buffers* buf, const pty_options* opt, int32_t iters,
+           int32_t* heatmap_valid, void* stream);
+
+/* Single operators (each replaces the reference function it names). */
+/* make_exits, era.py:426-433 */
+int pty_make_exits(pty_plan* plan, const void* O, const void* P, void* psi, void* stream);
+/* pmod_1 + Pmod_1, era.py:550-572: psi in place; *eMod_dev = sum mask (|F|+a - amp)^2 */
+int pty_pmod_1(pty_plan* plan, const float* amp, void* psi, const uint8_t* mask, double alpha,
+               double* eMod_dev, void* stream);
+/* pmod_7 + Pmod_7, era.py:574-595: psi and background (per frame) in place */
+int pty_pmod_7(pty_plan* plan, const float* amp, float* background, void* psi,
+               const uint8_t* mask, double alpha, double* eMod_dev, void* stream);
+/* Pmod_P, era.py:597-610: P in place */
+int pty_Pmod_P(pty_plan* plan, const float* Pamp, void* P, const uint8_t* mask, double alpha,
+               void* stream);
+/* psup_O, era.py:336-369; P_heatmap recomputed when recompute_heatmap != 0 */
+int pty_psup_O(pty_plan* plan, const void* psi, const void* P, double* P_heatmap,
+               int32_t recompute_heatmap, double alpha, void* O_out, void* stream);
+/* psup_P, era.py:371-400; O_heatmap recomputed when recompute_heatmap != 0 */
+int pty_psup_P(pty_plan* plan, const void* psi, const void* O, double* O_heatmap,
+               int32_t recompute_heatmap, double alpha, void* P_out, void* stream);
+/* make_P_heatmap, era.py:402-410 */
+int pty_make_P_heatmap(pty_plan* plan, const void* P, double* heat, void* stream);
+/* make_O_heatmap, era.py:412-417 */
+int pty_make_O_heatmap(pty_plan* plan, const void* O, double* heat, void* stream);
+/* model_error_1, dm.py:337-341.  background: NULL (= 0), one [N0][N1] pattern,
+ * or [n][N0][N1] when background_per_frame != 0. */
+int pty_model_error_1(pty_plan* plan, const float* amp, const void* psi, const uint8_t* mask,
+                      const float* background, int32_t background_per_frame, double* err_dev,
+                      void* stream);
+/* info['I'] = fftshift |FFT(P * O[R])|^2, era.py:295 */
+int pty_intensities(pty_plan* plan, const void* O, const void* P, float* I_out, void* stream);
+/* Per-frame mean of a background stack, era.py:265-270 */
+int pty_background_mean(pty_plan* plan, const float* background, float* mean_out, void* stream);
+
+/* amp = ifftshift(sqrt(I)) per frame, the preamble's era.py:497-498.
+ * I is float32 (is_double = 0) or float64 (is_double = 1), centred order. */
+int pty_amp_from_intensity(pty_plan* plan, const void* I, int32_t is_double, float* amp,
+                           void* stream);
+/* 1 if the frame shape N0 x N1 has a fused FFT kernel. */
+int pty_shape_supported(int32_t N0, int32_t N1);
+const char* pty_last_error(void);
+int pty_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PTYCHO_GB300_H */

@@ -1,0 +1,17 @@
+"""GB300-native ptychographic reconstruction, a drop-in for the ERA / DM /
+forward_sim API of andyofmelbourne/Ptychography.
+
+    import ptychography_gb300 as pty
+    I, R, M, P, O, B = pty.forward_sim(...)
+    O, info = pty.ERA(I, R, P, None, 100, mask=M, method=1)
+
+The reconstruction loops run in libptycho_gb300.so (hand-written sm_103a CUDA,
+C ABI in include/ptycho_gb300.h); Python prepares inputs and returns outputs.
+"""
+from . import dm, era, forward_models  # noqa: F401
+from .dm import DM
+from .era import ERA
+from .forward_models import forward_sim
+
+__all__ = ["ERA", "DM", "forward_sim", "era", "dm", "forward_models"]
+__version__ = "0.1.0"

@@ -1,0 +1,92 @@
+// Internal declarations shared by the CUDA translation units of libptycho_gb300.
+#pragma once
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "pty_common.cuh"
+
+namespace pty {
+
+// operations of the fused frame kernel
+enum FrameOp {
+  OP_EXIT1 = 0,  // P*O[R] -> FFT -> Pmod_1 (+eMod) -> IFFT -> psi          (ERA m1-3)
+  OP_EXIT7 = 1,  // P*O[R] -> FFT -> Pmod_7 (+eMod, bg*f out) -> IFFT -> psi (ERA m4-6)
+  OP_PSI1 = 2,   // psi -> FFT -> Pmod_1 -> IFFT -> psi                     (pmod_1, Pmod_P)
+  OP_PSI7 = 3,   // psi -> FFT -> Pmod_7 (bg in/out) -> IFFT -> psi          (pmod_7, DM m4-6)
+  OP_DM1 = 4,    // psi <- psi - ex0 + Pmod_1(2 ex0 - psi)                    (DM m1-3)
+  OP_DM7 = 5,    // same with the background recursion                        (DM m4-6)
+  OP_MERR = 6,   // P*O[R] -> FFT -> model error (no alpha)                    (model_error_1)
+  OP_INTENS = 7, // P*O[R] -> FFT -> fftshift |F|^2                            (info['I'])
+  OP_MERR_PSI = 8, // psi -> FFT -> model error                                (model_error_1)
+};
+
+struct FrameArgs {
+  int U, V;                  // object shape
+  const int* R;              // [n][2] scan offsets (<= 0), int32
+  const float2* O;           // [U][V]
+  const float2* P;           // [N0][N1]
+  float2* psi;               // [n][N0][N1] exit waves, in/out
+  const float* amp;          // [n][N0][N1] sqrt(I), unshifted order
+  long long amp_stride;      // elements between frames of amp (0: shared)
+  const uint8_t* mask;       // [N0][N1] 1 = valid, or nullptr
+  const float* bg_in;        // background read by Pmod_7
+  long long bg_stride;       // 0: shared pattern, N0*N1: per frame
+  float* bg_out;             // [n][N0][N1] per-frame background written (or DM state)
+  const float* b0;           // [N0][N1] mean background (DM m4-6, model error)
+  float* out_real;           // [n][N0][N1] intensities (OP_INTENS)
+  double* err_part;          // [n] per-frame error partials, or nullptr
+  float alpha;
+  const float2* tw0;         // twiddles of the column transform (length N0)
+  const float2* tw1;         // twiddles of the row transform (length N1)
+};
+
+bool frame_shape_supported(int N0, int N1);
+int prepare_frame_kernels(int N0, int N1);
+int launch_frame_op(int op, int N0, int N1, const FrameArgs& a, int nframes, cudaStream_t st);
+bool cluster_frame_supported();
+int launch_cluster_frame_op(int op, const FrameArgs& a, int nframes, cudaStream_t st);
+int prepare_cluster_frame_kernels();
+
+// error reporting (engine.cu)
+int set_error(int code, const char* msg);
+int set_cuda_error(cudaError_t e, const char* where);
+int check_launch(const char* where);
+
+// ------------------------------------------------------------ overlap kernels
+struct TileLists {
+  int TU, TV, ntu, ntv;      // object tiles
+  const int* ptr;            // [ntu*ntv + 1]
+  const int* frames;         // concatenated frame indices, ascending per tile
+};
+
+// O = sum conj(P) psi / (heat + alpha)   (era.py:336-369); heat in double
+int launch_psup_O(const TileLists& tl, int n, int N0, int N1, int U, int V, const int* R,
+                  const float2* psi, const float2* P, const double* heat, float alpha, float2* O,
+                  cudaStream_t st);
+// heat = sum |P|^2 over windows (era.py:402-410)
+int launch_heat_P(const TileLists& tl, int n, int N0, int N1, int U, int V, const int* R,
+                  const float2* P, double* heat, cudaStream_t st);
+// P = sum conj(O_i) psi_i / (sum |O_i|^2 + alpha) (era.py:371-400, 412-417)
+int launch_psup_P(int n, int N0, int N1, int U, int V, const int* R, const float2* psi,
+                  const float2* O, float2* part_num, float2* part_den, int K, double* heatO,
+                  bool recompute_heat, float alpha, float2* P, cudaStream_t st);
+// mean over frames of a per-frame real pattern (era.py:265-270)
+int launch_frame_mean(int n, int npix, const float* x, float2* part, int K, float* mean,
+                      cudaStream_t st);
+// partial sums of |a-b|^2 and |b|^2 (eCon, era.py:206-208)
+int launch_diffnorm(const float2* a, const float2* b, long long count, double* part, int nblocks,
+                    cudaStream_t st);
+// final per-iteration metrics
+int launch_finalize(const double* err_part, int n, const double* dn_part, int ndn, double I_norm,
+                    double* hist_emod, double* hist_econ, int it, cudaStream_t st);
+// probe centring (era.py:172-186)
+int launch_probe_shift(const float2* P, int N0, int N1, int* shift, cudaStream_t st);
+int launch_roll(const float2* src, float2* dst, int nimg, int H, int W, const int* shift,
+                cudaStream_t st);
+int launch_make_exits(int n, int N0, int N1, int U, int V, const int* R, const float2* O,
+                      const float2* P, float2* psi, cudaStream_t st);
+int launch_heat_O(int n, int N0, int N1, int U, int V, const int* R, const float2* O,
+                  float2* part, int K, double* heatO, cudaStream_t st);
+
+}  // namespace pty

@@ -1,0 +1,304 @@
+// Fused per-frame kernels: exit-wave formation -> 2-D FFT -> modulus constraint
+// -> inverse 2-D FFT, one CTA per frame, the whole frame resident in shared memory.
+//
+// Replaces, per frame and in one launch over all frames:
+//   make_exits        ptychography/era.py:426-433   psi_i = P * O[window_i]
+//   pmod_1 / Pmod_1   ptychography/era.py:550-572   amplitude replacement, eMod
+//   pmod_7 / Pmod_7   ptychography/era.py:574-595   same with incoherent background
+//   Pmod_P            ptychography/era.py:597-610   (one "frame" = the probe)
+//   DM update         ptychography/dm.py:91-97, 216-224
+//   model_error_1     ptychography/dm.py:337-341
+//   info['I']         ptychography/era.py:295, dm.py:299
+//
+// Shared-memory frame layout: row a, column c at a * RP + c + c / A1 (one pad
+// slot every A1 columns), which makes the row exchanges and the column passes
+// free of bank conflicts.  Frequencies are in NumPy's unshifted FFT order,
+// matching the reference's ifftshift-ed amp / mask.
+#include "engine.h"
+#include "fft_line.cuh"
+
+namespace pty {
+
+template <int N0, int N1>
+struct FrameCfg {
+  static constexpr int A0 = LineGeom<N0>::A, B0 = LineGeom<N0>::B;  // column transform
+  static constexpr int A1 = LineGeom<N1>::A, B1 = LineGeom<N1>::B;  // row transform
+  static constexpr int ROWLEN = B1 * (A1 + 1);                      // padded row length
+  // row pitch: half-warps covering several rows must hit disjoint banks in the
+  // stage-2 row exchange (A1 < 16 puts 16/A1 rows in a half-warp)
+  static constexpr int RP = (A1 >= 16) ? ROWLEN
+                          : (A1 == 8)  ? ROWLEN + ((8 - ROWLEN % 16) + 16) % 16
+                                       : ROWLEN + ((4 - ROWLEN % 16) + 16) % 16;
+  static constexpr int T_ROW = N0 * A1, T_COL = N1 * A0;
+  static constexpr int NT0 = T_ROW < T_COL ? T_ROW : T_COL;
+  static constexpr int NT = NT0 < 512 ? NT0 : 512;
+  static constexpr size_t SMEM = (size_t)N0 * RP * sizeof(float2) + (size_t)(N0 + N1) * sizeof(float2) +
+                                 32 * sizeof(double);
+  static_assert(T_ROW % NT == 0 && T_COL % NT == 0 && NT % 32 == 0, "task split");
+};
+
+PTY_DEV int padpos(int c, int A) { return c + c / A; }
+
+template <int N0, int N1, int OP>
+__global__ void __launch_bounds__(FrameCfg<N0, N1>::NT, 1) frame_kernel(FrameArgs g) {
+  using C = FrameCfg<N0, N1>;
+  constexpr int A0 = C::A0, B0 = C::B0, A1 = C::A1, B1 = C::B1, RP = C::RP, NT = C::NT;
+  constexpr bool IN_EXIT = (OP == OP_EXIT1 || OP == OP_EXIT7 || OP == OP_MERR || OP == OP_INTENS);
+  constexpr bool IN_DM = (OP == OP_DM1 || OP == OP_DM7);
+  constexpr bool INVERSE = !(OP == OP_MERR || OP == OP_MERR_PSI || OP == OP_INTENS);
+  constexpr float kInv = 1.0f / (float)(N0 * N1);
+
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float2* fr = reinterpret_cast<float2*>(smem_raw);
+  float2* tw0 = fr + N0 * RP;
+  float2* tw1 = tw0 + N0;
+  double* red = reinterpret_cast<double*>(tw1 + N1);
+
+  const int f = blockIdx.x;
+  const int tid = threadIdx.x;
+  for (int i = tid; i < N0; i += NT) tw0[i] = g.tw0[i];
+  for (int i = tid; i < N1; i += NT) tw1[i] = g.tw1[i];
+
+  int r0 = 0, r1 = 0;
+  if (IN_EXIT || IN_DM) {
+    r0 = g.R[2 * f];
+    r1 = g.R[2 * f + 1];
+  }
+  const size_t fbase = (size_t)f * N0 * N1;
+  float2* psi = g.psi + fbase;
+  __syncthreads();
+
+  // exit wave P * O[window] at frame pixel (a, b)
+  auto exitw = [&](int a, int b) -> float2 {
+    int u = a - r0, v = b - r1;
+    if (u >= g.U) u -= g.U;
+    if (v >= g.V) v -= g.V;
+    return cmul(__ldg(&g.O[(size_t)u * g.V + v]), __ldg(&g.P[a * N1 + b]));
+  };
+
+  // ---------------- forward row pass
+  for (int id = tid; id < N0 * A1; id += NT) {
+    const int t = id % A1, a = id / A1;
+    float2 v[B1];
+#pragma unroll
+    for (int j = 0; j < B1; ++j) {
+      const int b = t + A1 * j;
+      float2 x;
+      if constexpr (IN_EXIT) {
+        x = exitw(a, b);
+      } else if constexpr (IN_DM) {
+        // dm.py:94-95: e1 = psi - ex0 ; x = ex0 - e1
+        float2 ex0 = exitw(a, b);
+        float2 e1 = csub(psi[a * N1 + b], ex0);
+        x = csub(ex0, e1);
+      } else {
+        x = psi[a * N1 + b];
+      }
+      v[j] = x;
+    }
+    line_stage1<N1, -1>(v, t, tw1);
+    float2* row = fr + a * RP;
+#pragma unroll
+    for (int k1 = 0; k1 < B1; ++k1) row[k1 * (A1 + 1) + t] = v[k1];
+    __syncwarp();
+    line_stage2<N1, -1>(v, t, [&](int tt, int k1) { return row[k1 * (A1 + 1) + tt]; });
+    __syncwarp();
+#pragma unroll
+    for (int j = 0; j < B1; ++j) row[t + j * (A1 + 1)] = v[j];
+  }
+  __syncthreads();
+
+  // ---------------- column pass: forward FFT, modulus constraint, inverse FFT
+  // each pass takes CW whole columns (all A0 line-threads of a column in the
+  // same pass, as the exchange needs); lanes of a warp run along a row
+  ff err = ff_zero();
+  constexpr int CW = NT / A0;
+  static_assert(NT % A0 == 0 && N1 % CW == 0 && CW >= 32, "column pass split");
+  for (int c0 = 0; c0 < N1; c0 += CW) {
+    const int c = c0 + tid % CW, t = tid / CW;
+    const int cp = padpos(c, A1);
+    float2 v[B0];
+#pragma unroll
+    for (int j = 0; j < B0; ++j) v[j] = fr[(t + A0 * j) * RP + cp];
+    line_stage1<N0, -1>(v, t, tw0);
+    __syncthreads();
+#pragma unroll
+    for (int k1 = 0; k1 < B0; ++k1) fr[(k1 * A0 + t) * RP + cp] = v[k1];
+    __syncthreads();
+    line_stage2<N0, -1>(v, t, [&](int tt, int k1) { return fr[(k1 * A0 + tt) * RP + cp]; });
+
+    // v[j] = F[kr][c], kr = t + A0 j
+#pragma unroll
+    for (int j = 0; j < B0; ++j) {
+      const int kr = t + A0 * j;
+      const int pix = kr * N1 + c;
+      const float2 F = v[j];
+      const float msk = g.mask ? (float)g.mask[pix] : 1.0f;
+      if constexpr (OP == OP_INTENS) {
+        const int sr = (kr + N0 / 2) % N0, sc = (c + N1 / 2) % N1;
+        g.out_real[fbase + (size_t)sr * N1 + sc] = cabs2(F);
+      } else {
+        const float am = g.amp[(size_t)g.amp_stride * f + pix];
+        if constexpr (OP == OP_EXIT1 || OP == OP_PSI1 || OP == OP_DM1) {
+          // era.py:561-571
+          const float mag = sqrtf(cabs2(F)) + g.alpha;
+          if (g.err_part) {
+            const float d = mag - am;
+            err = ff_add(err, d * d * msk);
+          }
+          const float fac = (msk != 0.f) ? am / mag : 1.0f;
+          v[j] = cscale(F, fac);
+        } else if constexpr (OP == OP_EXIT7 || OP == OP_PSI7) {
+          // era.py:584-594
+          const float b = g.bg_in[(size_t)g.bg_stride * f + pix];
+          const float mag = sqrtf(cabs2(F) + b * b + g.alpha);
+          if (g.err_part) {
+            const float d = mag - am;
+            err = ff_add(err, d * d * msk);
+          }
+          const float fac = msk * am / mag;
+          v[j] = cscale(F, fac);
+          g.bg_out[fbase + pix] = b * fac;
+        } else if constexpr (OP == OP_DM7) {
+          // dm.py:219-224 on the background: g1 = g - b0 ; tb = b0 - g1 ; g = g1 + Pmod7(tb)
+          const float gs = g.bg_out[fbase + pix];
+          const float b0 = g.b0[pix];
+          const float g1 = gs - b0;
+          const float tb = b0 - g1;
+          const float mag = sqrtf(cabs2(F) + tb * tb + g.alpha);
+          const float fac = msk * am / mag;
+          v[j] = cscale(F, fac);
+          g.bg_out[fbase + pix] = g1 + tb * fac;
+        } else if constexpr (OP == OP_MERR || OP == OP_MERR_PSI) {
+          // dm.py:338-340, no alpha
+          const float b = g.bg_in ? g.bg_in[(size_t)g.bg_stride * f + pix] : 0.0f;
+          const float mag = sqrtf(cabs2(F) + b * b);
+          const float d = mag - am;
+          err = ff_add(err, msk * (d * d));
+        }
+      }
+    }
+
+    if constexpr (INVERSE) {
+      line_stage1<N0, +1>(v, t, tw0);
+      __syncthreads();
+#pragma unroll
+      for (int k1 = 0; k1 < B0; ++k1) fr[(k1 * A0 + t) * RP + cp] = v[k1];
+      __syncthreads();
+      line_stage2<N0, +1>(v, t, [&](int tt, int k1) { return fr[(k1 * A0 + tt) * RP + cp]; });
+      __syncthreads();
+#pragma unroll
+      for (int j = 0; j < B0; ++j) fr[(t + A0 * j) * RP + cp] = v[j];
+    }
+  }
+
+  if constexpr (INVERSE) {
+    __syncthreads();
+    // ---------------- inverse row pass, write the result
+    for (int id = tid; id < N0 * A1; id += NT) {
+      const int t = id % A1, a = id / A1;
+      float2* row = fr + a * RP;
+      float2 v[B1];
+#pragma unroll
+      for (int j = 0; j < B1; ++j) v[j] = row[t + j * (A1 + 1)];
+      line_stage1<N1, +1>(v, t, tw1);
+      __syncwarp();
+#pragma unroll
+      for (int k1 = 0; k1 < B1; ++k1) row[k1 * (A1 + 1) + t] = v[k1];
+      __syncwarp();
+      line_stage2<N1, +1>(v, t, [&](int tt, int k1) { return row[k1 * (A1 + 1) + tt]; });
+#pragma unroll
+      for (int j = 0; j < B1; ++j) {
+        const int b = t + A1 * j;
+        const float2 r = cscale(v[j], kInv);
+        if constexpr (IN_DM) {
+          // dm.py:94-97: psi_new = (psi - ex0) + Pmod(2 ex0 - psi)
+          float2 ex0 = exitw(a, b);
+          float2 e1 = csub(psi[a * N1 + b], ex0);
+          psi[a * N1 + b] = cadd(e1, r);
+        } else {
+          psi[a * N1 + b] = r;
+        }
+      }
+    }
+  }
+
+  if (g.err_part) {
+    const double s = block_sum_d(ff_to_double(err), red);
+    if (tid == 0) g.err_part[f] = s;
+  }
+}
+
+template <int N0, int N1, int OP>
+static int set_attr() {
+  using C = FrameCfg<N0, N1>;
+  cudaError_t e = cudaFuncSetAttribute(frame_kernel<N0, N1, OP>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)C::SMEM);
+  if (e != cudaSuccess) return set_cuda_error(e, "frame_kernel smem attribute");
+  return PTY_OK;
+}
+
+template <int N0, int N1, int OP>
+static int launch_one(const FrameArgs& a, int nframes, cudaStream_t st) {
+  using C = FrameCfg<N0, N1>;
+  frame_kernel<N0, N1, OP><<<nframes, C::NT, C::SMEM, st>>>(a);
+  return check_launch("frame_kernel");
+}
+
+template <int N0, int N1>
+static int launch_op(int op, const FrameArgs& a, int nframes, cudaStream_t st) {
+  switch (op) {
+    case OP_EXIT1: return launch_one<N0, N1, OP_EXIT1>(a, nframes, st);
+    case OP_EXIT7: return launch_one<N0, N1, OP_EXIT7>(a, nframes, st);
+    case OP_PSI1: return launch_one<N0, N1, OP_PSI1>(a, nframes, st);
+    case OP_PSI7: return launch_one<N0, N1, OP_PSI7>(a, nframes, st);
+    case OP_DM1: return launch_one<N0, N1, OP_DM1>(a, nframes, st);
+    case OP_DM7: return launch_one<N0, N1, OP_DM7>(a, nframes, st);
+    case OP_MERR: return launch_one<N0, N1, OP_MERR>(a, nframes, st);
+    case OP_INTENS: return launch_one<N0, N1, OP_INTENS>(a, nframes, st);
+    case OP_MERR_PSI: return launch_one<N0, N1, OP_MERR_PSI>(a, nframes, st);
+  }
+  return set_error(PTY_ERR_ARG, "unknown frame op");
+}
+
+template <int N0, int N1>
+static int prepare_shape() {
+  int rc = PTY_OK;
+  if (!rc) rc = set_attr<N0, N1, OP_EXIT1>();
+  if (!rc) rc = set_attr<N0, N1, OP_EXIT7>();
+  if (!rc) rc = set_attr<N0, N1, OP_PSI1>();
+  if (!rc) rc = set_attr<N0, N1, OP_PSI7>();
+  if (!rc) rc = set_attr<N0, N1, OP_DM1>();
+  if (!rc) rc = set_attr<N0, N1, OP_DM7>();
+  if (!rc) rc = set_attr<N0, N1, OP_MERR>();
+  if (!rc) rc = set_attr<N0, N1, OP_INTENS>();
+  if (!rc) rc = set_attr<N0, N1, OP_MERR_PSI>();
+  return rc;
+}
+
+int prepare_frame_kernels(int N0, int N1) {
+  if (N0 == 32 && N1 == 32) return prepare_shape<32, 32>();
+  if (N0 == 64 && N1 == 64) return prepare_shape<64, 64>();
+  if (N0 == 128 && N1 == 128) return prepare_shape<128, 128>();
+  if (N0 == 32 && N1 == 64) return prepare_shape<32, 64>();
+  if (N0 == 256 && N1 == 256) return prepare_cluster_frame_kernels();
+  return set_error(PTY_ERR_SHAPE, "frame shape not supported by the fused FFT kernels");
+}
+
+bool frame_shape_supported(int N0, int N1) {
+  auto ok = [](int n) { return n == 32 || n == 64 || n == 128; };
+  if (N0 == 256 && N1 == 256) return cluster_frame_supported();
+  return ok(N0) && ok(N1) && (N0 == N1 || (N0 == 32 && N1 == 64));
+}
+
+int launch_frame_op(int op, int N0, int N1, const FrameArgs& a, int nframes, cudaStream_t st) {
+  if (nframes <= 0) return PTY_OK;
+  if (N0 == 32 && N1 == 32) return launch_op<32, 32>(op, a, nframes, st);
+  if (N0 == 64 && N1 == 64) return launch_op<64, 64>(op, a, nframes, st);
+  if (N0 == 128 && N1 == 128) return launch_op<128, 128>(op, a, nframes, st);
+  if (N0 == 32 && N1 == 64) return launch_op<32, 64>(op, a, nframes, st);
+  if (N0 == 256 && N1 == 256) return launch_cluster_frame_op(op, a, nframes, st);
+  return set_error(PTY_ERR_UNSUPPORTED, "frame shape not supported by the fused FFT kernels");
+}
+
+}  // namespace pty

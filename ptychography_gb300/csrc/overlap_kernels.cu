@@ -1,0 +1,403 @@
+// Overlap (consistency) projections and small reductions.
+//
+// Every cross-frame sum is a gather in a fixed order, never a float atomic:
+// an object tile walks its own ascending list of overlapping frames, and the
+// probe / background reductions split the frames into K fixed chunks whose
+// partials are combined in chunk order.  Two runs on the same inputs therefore
+// produce identical bits.
+#include "engine.h"
+
+namespace pty {
+
+constexpr int kTile = 32;      // object / probe tile edge
+constexpr int kGatherNT = 256; // threads per tile (4 pixels each)
+
+// ------------------------------------------------------------------ psup_O
+// era.py:336-369: O = sum_i psi_i * conj(P) placed at window i, / (heat + alpha)
+__global__ void __launch_bounds__(kGatherNT) psup_O_kernel(
+    TileLists tl, int N0, int N1, int U, int V, const int* __restrict__ R,
+    const float2* __restrict__ psi, const float2* __restrict__ P, const double* __restrict__ heat,
+    float alpha, float2* __restrict__ O) {
+  const int tile = blockIdx.x;
+  const int tu = tile / tl.ntv, tv = tile % tl.ntv;
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  const int v = tv * kTile + tx;
+  int u[4];
+  float2 acc[4];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    u[k] = tu * kTile + ty + 8 * k;
+    acc[k] = make_float2(0.f, 0.f);
+  }
+  const int beg = tl.ptr[tile], end = tl.ptr[tile + 1];
+  for (int e = beg; e < end; ++e) {
+    const int f = tl.frames[e];
+    const int r0 = R[2 * f], r1 = R[2 * f + 1];
+    const int b = v + r1;
+    if (b < 0 || b >= N1) continue;
+    const float2* pf = psi + (size_t)f * N0 * N1;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const int a = u[k] + r0;
+      if (a >= 0 && a < N0) {
+        const float2 x = pf[a * N1 + b];
+        const float2 p = __ldg(&P[a * N1 + b]);
+        acc[k] = cadd(acc[k], cmulc(x, p));
+      }
+    }
+  }
+  if (v < V) {
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      if (u[k] < U) {
+        const size_t o = (size_t)u[k] * V + v;
+        const float den = (float)(heat[o] + (double)alpha);
+        O[o] = make_float2(acc[k].x / den, acc[k].y / den);
+      }
+    }
+  }
+}
+
+// era.py:402-410: heat = sum_i |P|^2 at window i (float-float, written as double)
+__global__ void __launch_bounds__(kGatherNT) heat_P_kernel(
+    TileLists tl, int N0, int N1, int U, int V, const int* __restrict__ R,
+    const float2* __restrict__ P, double* __restrict__ heat) {
+  const int tile = blockIdx.x;
+  const int tu = tile / tl.ntv, tv = tile % tl.ntv;
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  const int v = tv * kTile + tx;
+  ff acc[4];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) acc[k] = ff_zero();
+  const int beg = tl.ptr[tile], end = tl.ptr[tile + 1];
+  for (int e = beg; e < end; ++e) {
+    const int f = tl.frames[e];
+    const int r0 = R[2 * f], r1 = R[2 * f + 1];
+    const int b = v + r1;
+    if (b < 0 || b >= N1) continue;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const int a = tu * kTile + ty + 8 * k + r0;
+      if (a >= 0 && a < N0) acc[k] = ff_add(acc[k], cabs2(__ldg(&P[a * N1 + b])));
+    }
+  }
+  if (v < V) {
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const int uu = tu * kTile + ty + 8 * k;
+      if (uu < U) heat[(size_t)uu * V + v] = ff_to_double(acc[k]);
+    }
+  }
+}
+
+int launch_psup_O(const TileLists& tl, int n, int N0, int N1, int U, int V, const int* R,
+                  const float2* psi, const float2* P, const double* heat, float alpha, float2* O,
+                  cudaStream_t st) {
+  (void)n;
+  psup_O_kernel<<<tl.ntu * tl.ntv, kGatherNT, 0, st>>>(tl, N0, N1, U, V, R, psi, P, heat, alpha, O);
+  return check_launch("psup_O_kernel");
+}
+
+int launch_heat_P(const TileLists& tl, int n, int N0, int N1, int U, int V, const int* R,
+                  const float2* P, double* heat, cudaStream_t st) {
+  (void)n;
+  heat_P_kernel<<<tl.ntu * tl.ntv, kGatherNT, 0, st>>>(tl, N0, N1, U, V, R, P, heat);
+  return check_launch("heat_P_kernel");
+}
+
+// ------------------------------------------------------------------ psup_P
+// era.py:371-400 (+ make_O_heatmap era.py:412-417): per probe pixel, sum over
+// frames of psi_i * conj(O_i) and |O_i|^2.  Grid: probe tiles x K frame chunks.
+__global__ void __launch_bounds__(kGatherNT) psup_P_partial_kernel(
+    int n, int N0, int N1, int U, int V, const int* __restrict__ R, const float2* __restrict__ psi,
+    const float2* __restrict__ O, int K, bool want_den, float2* __restrict__ part_num,
+    float2* __restrict__ part_den) {
+  const int ntv = (N1 + kTile - 1) / kTile;
+  const int tile = blockIdx.x, k = blockIdx.y;
+  const int tu = tile / ntv, tv = tile % ntv;
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  const int b = tv * kTile + tx;
+  const int f0 = (int)(((long long)n * k) / K), f1 = (int)(((long long)n * (k + 1)) / K);
+  float2 num[4];
+  ff den[4];
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    num[q] = make_float2(0.f, 0.f);
+    den[q] = ff_zero();
+  }
+  if (b < N1) {
+    for (int f = f0; f < f1; ++f) {
+      const int r0 = R[2 * f], r1 = R[2 * f + 1];
+      const float2* pf = psi + (size_t)f * N0 * N1;
+      int vv = b - r1;
+      if (vv >= V) vv -= V;
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int a = tu * kTile + ty + 8 * q;
+        if (a < N0) {
+          int uu = a - r0;
+          if (uu >= U) uu -= U;
+          const float2 o = __ldg(&O[(size_t)uu * V + vv]);
+          num[q] = cadd(num[q], cmulc(pf[a * N1 + b], o));
+          if (want_den) den[q] = ff_add(den[q], cabs2(o));
+        }
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int a = tu * kTile + ty + 8 * q;
+      if (a < N0) {
+        const size_t o = (size_t)k * N0 * N1 + (size_t)a * N1 + b;
+        part_num[o] = num[q];
+        if (want_den) part_den[o] = make_float2(den[q].hi, den[q].lo);
+      }
+    }
+  }
+}
+
+__global__ void psup_P_reduce_kernel(int npix, int K, const float2* __restrict__ part_num,
+                                     const float2* __restrict__ part_den, bool recompute,
+                                     double* __restrict__ heatO, float alpha, float2* __restrict__ P) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= npix) return;
+  ff nr = ff_zero(), ni = ff_zero();
+  for (int k = 0; k < K; ++k) {
+    const float2 x = part_num[(size_t)k * npix + i];
+    nr = ff_add(nr, x.x);
+    ni = ff_add(ni, x.y);
+  }
+  double h;
+  if (recompute) {
+    ff d = ff_zero();
+    for (int k = 0; k < K; ++k) {
+      const float2 x = part_den[(size_t)k * npix + i];
+      d = ff_add(d, ff{x.x, x.y});
+    }
+    h = ff_to_double(d);
+    heatO[i] = h;
+  } else {
+    h = heatO[i];
+  }
+  const float den = (float)(h + (double)alpha);
+  P[i] = make_float2(nr.hi / den, ni.hi / den);
+}
+
+int launch_psup_P(int n, int N0, int N1, int U, int V, const int* R, const float2* psi,
+                  const float2* O, float2* part_num, float2* part_den, int K, double* heatO,
+                  bool recompute_heat, float alpha, float2* P, cudaStream_t st) {
+  const int ntiles = ((N0 + kTile - 1) / kTile) * ((N1 + kTile - 1) / kTile);
+  psup_P_partial_kernel<<<dim3(ntiles, K), kGatherNT, 0, st>>>(n, N0, N1, U, V, R, psi, O, K,
+                                                               recompute_heat, part_num, part_den);
+  int rc = check_launch("psup_P_partial_kernel");
+  if (rc) return rc;
+  const int npix = N0 * N1;
+  psup_P_reduce_kernel<<<(npix + 255) / 256, 256, 0, st>>>(npix, K, part_num, part_den,
+                                                           recompute_heat, heatO, alpha, P);
+  return check_launch("psup_P_reduce_kernel");
+}
+
+// make_O_heatmap alone (era.py:412-417), used by the standalone C-ABI op
+__global__ void heat_O_partial_kernel(int n, int N0, int N1, int U, int V, const int* __restrict__ R,
+                                      const float2* __restrict__ O, int K, float2* __restrict__ part) {
+  const int npix = N0 * N1;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int k = blockIdx.y;
+  if (i >= npix) return;
+  const int a = i / N1, b = i % N1;
+  const int f0 = (int)(((long long)n * k) / K), f1 = (int)(((long long)n * (k + 1)) / K);
+  ff d = ff_zero();
+  for (int f = f0; f < f1; ++f) {
+    int uu = a - R[2 * f], vv = b - R[2 * f + 1];
+    if (uu >= U) uu -= U;
+    if (vv >= V) vv -= V;
+    d = ff_add(d, cabs2(__ldg(&O[(size_t)uu * V + vv])));
+  }
+  part[(size_t)k * npix + i] = make_float2(d.hi, d.lo);
+}
+
+__global__ void heat_O_reduce_kernel(int npix, int K, const float2* __restrict__ part,
+                                     double* __restrict__ heatO) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= npix) return;
+  ff d = ff_zero();
+  for (int k = 0; k < K; ++k) {
+    const float2 x = part[(size_t)k * npix + i];
+    d = ff_add(d, ff{x.x, x.y});
+  }
+  heatO[i] = ff_to_double(d);
+}
+
+int launch_heat_O(int n, int N0, int N1, int U, int V, const int* R, const float2* O, float2* part,
+                  int K, double* heatO, cudaStream_t st) {
+  const int npix = N0 * N1;
+  heat_O_partial_kernel<<<dim3((npix + 255) / 256, K), 256, 0, st>>>(n, N0, N1, U, V, R, O, K, part);
+  int rc = check_launch("heat_O_partial_kernel");
+  if (rc) return rc;
+  heat_O_reduce_kernel<<<(npix + 255) / 256, 256, 0, st>>>(npix, K, part, heatO);
+  return check_launch("heat_O_reduce_kernel");
+}
+
+// ------------------------------------------------------------------ frame mean
+// era.py:265-270 / dm.py:208-213: b = mean over frames, per detector pixel
+__global__ void frame_mean_partial_kernel(int n, int npix, const float* __restrict__ x, int K,
+                                          float2* __restrict__ part) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int k = blockIdx.y;
+  if (i >= npix) return;
+  const int f0 = (int)(((long long)n * k) / K), f1 = (int)(((long long)n * (k + 1)) / K);
+  ff s = ff_zero();
+  for (int f = f0; f < f1; ++f) s = ff_add(s, x[(size_t)f * npix + i]);
+  part[(size_t)k * npix + i] = make_float2(s.hi, s.lo);
+}
+
+__global__ void frame_mean_reduce_kernel(int n, int npix, int K, const float2* __restrict__ part,
+                                         float* __restrict__ mean) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= npix) return;
+  ff s = ff_zero();
+  for (int k = 0; k < K; ++k) {
+    const float2 x = part[(size_t)k * npix + i];
+    s = ff_add(s, ff{x.x, x.y});
+  }
+  mean[i] = (float)(ff_to_double(s) / (double)n);
+}
+
+int launch_frame_mean(int n, int npix, const float* x, float2* part, int K, float* mean,
+                      cudaStream_t st) {
+  frame_mean_partial_kernel<<<dim3((npix + 255) / 256, K), 256, 0, st>>>(n, npix, x, K, part);
+  int rc = check_launch("frame_mean_partial_kernel");
+  if (rc) return rc;
+  frame_mean_reduce_kernel<<<(npix + 255) / 256, 256, 0, st>>>(n, npix, K, part, mean);
+  return check_launch("frame_mean_reduce_kernel");
+}
+
+// ------------------------------------------------------------------ metrics
+// eCon numerator / denominator partials: sum |a-b|^2, sum |b|^2 (era.py:206-207)
+__global__ void diffnorm_kernel(const float2* __restrict__ a, const float2* __restrict__ b,
+                                long long count, double* __restrict__ part) {
+  __shared__ double red[32];
+  ff d = ff_zero(), c = ff_zero();
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < count;
+       i += (long long)gridDim.x * blockDim.x) {
+    const float2 x = a[i], y = b[i];
+    d = ff_add(d, cabs2(csub(x, y)));
+    c = ff_add(c, cabs2(y));
+  }
+  const double sd = block_sum_d(ff_to_double(d), red);
+  const double sc = block_sum_d(ff_to_double(c), red);
+  if (threadIdx.x == 0) {
+    part[2 * blockIdx.x] = sd;
+    part[2 * blockIdx.x + 1] = sc;
+  }
+}
+
+int launch_diffnorm(const float2* a, const float2* b, long long count, double* part, int nblocks,
+                    cudaStream_t st) {
+  diffnorm_kernel<<<nblocks, 256, 0, st>>>(a, b, count, part);
+  return check_launch("diffnorm_kernel");
+}
+
+// eMod = sqrt(sum err / I_norm) (era.py:210), eCon = sqrt(d / c) (era.py:207-208)
+__global__ void finalize_kernel(const double* __restrict__ err_part, int n,
+                                const double* __restrict__ dn_part, int ndn, double I_norm,
+                                double* hist_emod, double* hist_econ, int it) {
+  __shared__ double red[32];
+  double e = 0.0, d = 0.0, c = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) e += err_part[i];
+  for (int i = threadIdx.x; i < ndn; i += blockDim.x) {
+    d += dn_part[2 * i];
+    c += dn_part[2 * i + 1];
+  }
+  e = block_sum_d(e, red);
+  d = block_sum_d(d, red);
+  c = block_sum_d(c, red);
+  if (threadIdx.x == 0) {
+    if (hist_emod) hist_emod[it] = sqrt(e / I_norm);
+    if (hist_econ) hist_econ[it] = sqrt(d / c);
+  }
+}
+
+int launch_finalize(const double* err_part, int n, const double* dn_part, int ndn, double I_norm,
+                    double* hist_emod, double* hist_econ, int it, cudaStream_t st) {
+  finalize_kernel<<<1, 256, 0, st>>>(err_part, n, dn_part, ndn, I_norm, hist_emod, hist_econ, it);
+  return check_launch("finalize_kernel");
+}
+
+// ------------------------------------------------------------------ centring
+// era.py:172-186: cm = rint(centre_of_mass(|P|^2)) - shape // 2
+__global__ void probe_shift_kernel(const float2* __restrict__ P, int N0, int N1, int* shift) {
+  __shared__ double red[32];
+  ff s = ff_zero(), sa = ff_zero(), sb = ff_zero();
+  for (int i = threadIdx.x; i < N0 * N1; i += blockDim.x) {
+    const float w = cabs2(P[i]);
+    s = ff_add(s, w);
+    sa = ff_add(sa, w * (float)(i / N1));
+    sb = ff_add(sb, w * (float)(i % N1));
+  }
+  const double S = block_sum_d(ff_to_double(s), red);
+  const double SA = block_sum_d(ff_to_double(sa), red);
+  const double SB = block_sum_d(ff_to_double(sb), red);
+  if (threadIdx.x == 0) {
+    shift[0] = (int)rint(SA / S) - N0 / 2;
+    shift[1] = (int)rint(SB / S) - N1 / 2;
+  }
+}
+
+int launch_probe_shift(const float2* P, int N0, int N1, int* shift, cudaStream_t st) {
+  probe_shift_kernel<<<1, 1024, 0, st>>>(P, N0, N1, shift);
+  return check_launch("probe_shift_kernel");
+}
+
+// multiroll(x, -cm) (era.py:631-740): dst[i][j] = src[(i + s0) mod H][(j + s1) mod W]
+__global__ void roll_kernel(const float2* __restrict__ src, float2* __restrict__ dst, int nimg,
+                            int H, int W, const int* __restrict__ shift) {
+  const long long tot = (long long)nimg * H * W;
+  const int s0 = shift[0], s1 = shift[1];
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < tot;
+       i += (long long)gridDim.x * blockDim.x) {
+    const long long img = i / ((long long)H * W);
+    const int r = (int)((i / W) % H), c = (int)(i % W);
+    int rr = (r + s0) % H, cc = (c + s1) % W;
+    if (rr < 0) rr += H;
+    if (cc < 0) cc += W;
+    dst[i] = src[img * H * W + (long long)rr * W + cc];
+  }
+}
+
+int launch_roll(const float2* src, float2* dst, int nimg, int H, int W, const int* shift,
+                cudaStream_t st) {
+  long long tot = (long long)nimg * H * W;
+  int blocks = (int)((tot + 255) / 256);
+  if (blocks > 152 * 16) blocks = 152 * 16;
+  roll_kernel<<<blocks, 256, 0, st>>>(src, dst, nimg, H, W, shift);
+  return check_launch("roll_kernel");
+}
+
+// make_exits (era.py:426-433)
+__global__ void make_exits_kernel(int n, int N0, int N1, int U, int V, const int* __restrict__ R,
+                                  const float2* __restrict__ O, const float2* __restrict__ P,
+                                  float2* __restrict__ psi) {
+  const long long tot = (long long)n * N0 * N1;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < tot;
+       i += (long long)gridDim.x * blockDim.x) {
+    const int f = (int)(i / ((long long)N0 * N1));
+    const int a = (int)((i / N1) % N0), b = (int)(i % N1);
+    int u = a - R[2 * f], v = b - R[2 * f + 1];
+    u %= U;
+    v %= V;
+    if (u < 0) u += U;
+    if (v < 0) v += V;
+    psi[i] = cmul(O[(size_t)u * V + v], P[a * N1 + b]);
+  }
+}
+
+int launch_make_exits(int n, int N0, int N1, int U, int V, const int* R, const float2* O,
+                      const float2* P, float2* psi, cudaStream_t st) {
+  long long tot = (long long)n * N0 * N1;
+  int blocks = (int)((tot + 255) / 256);
+  if (blocks > 152 * 32) blocks = 152 * 32;
+  make_exits_kernel<<<blocks, 256, 0, st>>>(n, N0, N1, U, V, R, O, P, psi);
+  return check_launch("make_exits_kernel");
+}
+
+}  // namespace pty

@@ -27,15 +27,30 @@ def run_cases():
     return cases
 
 
-def initial_guess(method, O_true, P_true, B):
-    """Initial O, P, background for a method: O from ones when O is updated."""
+def default_object_shape(I, R):
+    """The preamble's default object shape (era.py:484-486)."""
+    return (I.shape[1] + R[:, 0].max() - R[:, 0].min(), I.shape[2] + R[:, 1].max() - R[:, 1].min())
+
+
+def initial_guess(method, O_true, P_true, B, I=None, R=None):
+    """Initial O, P, background for a method.
+
+    Methods 4 and 6 start from the reference's default object (O=None: ones).
+    Methods 1 and 3 start from ones plus seeded noise: with forward_sim's
+    band-limited pupil probe, O = ones makes |FFT(P O)| exactly zero outside the
+    pupil, Pmod_1 (no background term) then scales rounding noise up to the
+    measured amplitude, and the reference's own FP32 and FP64 runs disagree by
+    O(1) -- a comparison of any FP32 engine with FP64 would be meaningless.
+    """
     upd_O = method in (1, 3, 4, 6)
     upd_P = method in (2, 3, 5, 6)
     O0 = None if upd_O else O_true
+    if method in (1, 3) and I is not None:
+        rng = np.random.default_rng(11)
+        shp = default_object_shape(I, R)
+        O0 = np.ones(shp) + 0.1 * (rng.standard_normal(shp) + 1j * rng.standard_normal(shp))
     P0 = (P_true * np.exp(0.3j) * 0.9) if upd_P else P_true
     bg = None
     if method == 5:
         bg = B.astype(np.float64) + 1.0
     return O0, P0, bg
-
-

@@ -41,7 +41,7 @@ def base_problem(ref, seed=1234, shape_P=(32, 32), shape_O=(56, 56), ny=3, nx=3)
 def make_runs(ref, I, R, M, P, O, B):
     out = {}
     for name, drv, m, dt, kw in run_cases():
-        O0, P0, bg = initial_guess(m, O, P, B)
+        O0, P0, bg = initial_guess(m, O, P, B, I, R)
         if kw.get("probe_centering"):
             P0 = np.roll(P0, (3, -2), axis=(0, 1))   # give the centring a shift to undo
         Rc = R.copy()
@@ -77,7 +77,7 @@ def make_runs(ref, I, R, M, P, O, B):
 def make_ops(ref):
     era, dm = ref.era, ref.dm
     rng = np.random.default_rng(7)
-    n, N0, N1, U, V = 6, 16, 32, 40, 56
+    n, N0, N1, U, V = 4, 32, 64, 56, 88
     R = np.stack([-rng.integers(0, U - N0 + 1, n), -rng.integers(0, V - N1 + 1, n)], 1)
     O = rng.standard_normal((U, V)) + 1j * rng.standard_normal((U, V))
     P = rng.standard_normal((N0, N1)) + 1j * rng.standard_normal((N0, N1))

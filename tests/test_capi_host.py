@@ -1,0 +1,115 @@
+"""CPU-side checks of the C-ABI library and the Python host layer (no GPU calls)."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+from ptychography_gb300 import _engine, _native
+from oracle import ptycho_oracle as orc
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, "include", "ptycho_gb300.h")
+
+
+def header_functions():
+    src = open(HEADER).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"^\s*(?:const\s+)?\w+\**\s+\**(pty_\w+)\s*\(", src, flags=re.M)))
+
+
+def test_header_declares_entry_points():
+    names = header_functions()
+    for must in ("pty_plan_create", "pty_era", "pty_dm", "pty_pmod_1", "pty_psup_O", "pty_psup_P"):
+        assert must in names
+
+
+def test_library_exports_every_declared_symbol():
+    lib = _native.load()
+    for name in header_functions():
+        assert hasattr(lib, name), name
+        assert isinstance(getattr(lib, name), ctypes._CFuncPtr)
+
+
+def test_ctypes_table_matches_header():
+    assert set(_native.SIGNATURES) == set(header_functions())
+
+
+def test_struct_layouts_match_c():
+    # pty_options: 3 x int32, pad, int64, 2 x int32, 2 x double = 48 bytes
+    assert ctypes.sizeof(_native.Options) == 48
+    assert ctypes.sizeof(_native.Buffers) == 12 * ctypes.sizeof(ctypes.c_void_p)
+    assert ctypes.sizeof(_native.Geometry) == 20
+
+
+def test_version_and_shapes_without_gpu():
+    lib = _native.load()
+    assert lib.pty_version() >= 100
+    for n in (32, 64, 128):
+        assert lib.pty_shape_supported(n, n) == 1
+    assert lib.pty_shape_supported(48, 48) == 0
+    assert lib.pty_shape_supported(100, 128) == 0
+
+
+def test_plan_create_rejects_bad_geometry():
+    lib = _native.load()
+    plan = ctypes.c_void_p()
+    R = np.zeros((2, 2), dtype=np.int64)
+    g = _native.Geometry(2, 48, 48, 64, 64)          # no kernel for 48 x 48
+    rc = lib.pty_plan_create(ctypes.byref(g), R.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)),
+                             ctypes.byref(plan))
+    assert rc == 2 and b"not supported" in lib.pty_last_error()
+    g = _native.Geometry(2, 32, 32, 40, 40)
+    R = np.array([[0, 0], [-20, 0]], dtype=np.int64)  # window rows 20..52 > 40
+    rc = lib.pty_plan_create(ctypes.byref(g), R.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)),
+                             ctypes.byref(plan))
+    assert rc == 3 and b"outside the object" in lib.pty_last_error()
+    with pytest.raises(ValueError):
+        _native.check(rc)
+
+
+def test_method_choice_matches_reference():
+    assert _engine.choose_method(None, None, np.ones(1), None) == 1
+    assert _engine.choose_method(None, np.ones(1), None, None) == 2
+    assert _engine.choose_method(None, None, None, None) == 3
+    assert _engine.choose_method(None, None, None, 1.0) == 6
+    with pytest.raises(ValueError):
+        _engine.choose_method(7, None, None, None)
+
+
+def test_pmod_probe_schedule():
+    c = _engine.pmod_probe_count
+    assert c(False, 10) == 0 and c(None, 10) == 0
+    assert c(True, 10) == 1            # i < True  -> i == 0 only
+    assert c(3, 10) == 3 and c(2.5, 10) == 3
+    assert c(np.inf, 10) == 10
+
+
+def test_preamble_matches_oracle_rng_and_R_shift():
+    rng = np.random.default_rng(0)
+    I = rng.random((5, 32, 32)) * 10
+    R = -rng.integers(0, 10, (5, 2)) + 3
+    M = rng.random((32, 32)) > 0.1
+    R1, R2 = R.copy(), R.copy()
+    np.random.seed(3)
+    pre = _engine.Preamble(I, R1, None, None, 1, M, None, 6, "single")
+    np.random.seed(3)
+    st = orc.preamble(I, R2, None, None, 1, M, None, 6, "single")
+    assert np.array_equal(R1, R2) and R1.max(axis=0).tolist() == [0, 0]
+    assert np.array_equal(pre.P, st["P"]) and np.array_equal(pre.O, st["O"])
+    assert np.array_equal(pre.background, st["background"])
+    assert np.array_equal(pre.mask.astype(bool), st["mask"])
+    assert pre.I_norm == pytest.approx(float(st["I_norm"]), rel=1e-6)
+    np.testing.assert_allclose(pre.Pamp, st["Pamp"], rtol=1e-6)
+
+
+def test_engine_fails_loudly_without_gpu():
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    I = np.ones((2, 32, 32))
+    R = np.zeros((2, 2), dtype=int)
+    with pytest.raises(RuntimeError, match="CUDA GPU"):
+        _engine.run("era", I, R, np.ones((32, 32)), None, 1, 1, 1, None, 1, False, False, 1e-10,
+                    None, True)

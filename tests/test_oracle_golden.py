@@ -96,7 +96,7 @@ def test_ops_match_reference(ops):
 def run_oracle(case, problem):
     name, drv, m, dt, kw = case
     p = problem
-    O0, P0, bg = initial_guess(m, p["O"], p["P"], p["B"])
+    O0, P0, bg = initial_guess(m, p["O"], p["P"], p["B"], p["I"], p["R"])
     if kw.get("probe_centering"):
         P0 = np.roll(P0, (3, -2), axis=(0, 1))
     Rc = p["R"].copy()
