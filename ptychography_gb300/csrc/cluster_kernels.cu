@@ -1,11 +1,215 @@
-// 256 x 256 frames: one frame per 4-CTA cluster (placeholder until the
-// distributed-shared-memory transform lands).
+// 256 x 256 frames: one frame per 4-CTA thread-block cluster.
+//
+// A 256^2 complex64 frame (512 KB) does not fit one SM's shared memory, so the
+// 2-D transform is distributed over a cluster of C = 4 CTAs (one per SM) and
+// the two transposes go through distributed shared memory instead of HBM:
+//
+//   1. CTA r forms its 64 rows of the input wave (exit wave, psi, or the DM
+//      combination), row-FFTs them, and stores each transformed row straight
+//      into the column buffer of the CTA that owns those 64 columns
+//      (remote st.shared::cluster through map_shared_rank);
+//   2. cluster barrier;
+//   3. CTA r runs its 64 columns entirely locally: forward column FFT, the
+//      modulus constraint in registers, inverse column FFT, in place;
+//   4. cluster barrier;
+//   5. CTA r pulls its 64 rows back from the four column buffers, inverse
+//      row-FFTs them and writes the result to HBM;
+//   6. cluster barrier (no CTA leaves while others still read its buffer).
+//
+// HBM sees only the frame's input and output (plus the L2-resident object
+// window and probe), the same traffic as the single-CTA kernel for small frames.
+// Replaces the same reference functions as frame_kernels.cu.
+#include <cooperative_groups.h>
+
 #include "engine.h"
+#include "fft_line.cuh"
+#include "frame_ops.cuh"
+
+namespace cg = cooperative_groups;
 
 namespace pty {
-bool cluster_frame_supported() { return false; }
-int prepare_cluster_frame_kernels() { return set_error(PTY_ERR_SHAPE, "256x256 frames not built"); }
-int launch_cluster_frame_op(int, const FrameArgs&, int, cudaStream_t) {
-  return set_error(PTY_ERR_SHAPE, "256x256 frames not built");
+
+template <int N, int C>
+struct ClusterCfg {
+  static constexpr int A = LineGeom<N>::A, B = LineGeom<N>::B;  // rows and columns alike
+  static constexpr int NT = 512;
+  static constexpr int RPC = N / C;          // rows owned per CTA
+  static constexpr int CPC = N / C;          // columns owned per CTA
+  static constexpr int CP = CPC;             // column-buffer pitch (float2)
+  static constexpr int RF = NT / A;          // rows in flight per row sub-pass
+  static constexpr int ROWLEN = B * (A + 1); // padded row-exchange length
+  static constexpr int CW = NT / A;          // columns per column sub-pass
+  static constexpr int JPC = CPC / A;        // row registers per destination CTA
+  static constexpr size_t CBUF = (size_t)N * CP;
+  static constexpr size_t RSCR = (size_t)RF * ROWLEN;
+  static constexpr size_t SMEM = (CBUF + RSCR + N) * sizeof(float2) + 32 * sizeof(double);
+  static_assert(RPC % RF == 0 && CPC % CW == 0 && CW >= 32 && CPC % A == 0, "cluster split");
+  static_assert(SMEM <= 227 * 1024, "shared memory budget");
+};
+
+template <int N, int C, int OP>
+__global__ void __cluster_dims__(C, 1, 1) __launch_bounds__(512, 1)
+    cluster_frame_kernel(FrameArgs g) {
+  using K = ClusterCfg<N, C>;
+  constexpr int A = K::A, B = K::B, CP = K::CP, RPC = K::RPC, CPC = K::CPC, RF = K::RF, CW = K::CW;
+  constexpr int JPC = K::JPC;
+  constexpr bool INVERSE = OpTraits<OP>::INVERSE;
+  constexpr float kInv = 1.0f / (float)(N * N);
+
+  cg::cluster_group cluster = cg::this_cluster();
+  const int rank = (int)cluster.block_rank();
+  const int f = blockIdx.x / C;
+  const int tid = threadIdx.x;
+
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float2* cbuf = reinterpret_cast<float2*>(smem_raw);   // [N rows][CPC own columns]
+  float2* rscr = cbuf + K::CBUF;                          // [RF][ROWLEN] row exchange
+  float2* tw = rscr + K::RSCR;                            // [N]
+  double* red = reinterpret_cast<double*>(tw + N);
+  for (int i = tid; i < N; i += K::NT) tw[i] = g.tw0[i];
+
+  float2* rc[C];  // column buffers of every CTA of the cluster
+#pragma unroll
+  for (int q = 0; q < C; ++q) rc[q] = cluster.map_shared_rank(cbuf, q);
+
+  int r0 = 0, r1 = 0;
+  if (OpTraits<OP>::IN_EXIT || OpTraits<OP>::IN_DM) {
+    r0 = g.R[2 * f];
+    r1 = g.R[2 * f + 1];
+  }
+  const size_t fbase = (size_t)f * N * N;
+  float2* psi = g.psi + fbase;
+  __syncthreads();
+
+  const int t = tid % A, lr = tid / A;
+  float2* rs = rscr + lr * K::ROWLEN;
+
+  // ---------------- 1. forward row pass, pushed to the column owners
+#pragma unroll 1
+  for (int s = 0; s < RPC / RF; ++s) {
+    const int a = rank * RPC + s * RF + lr;
+    float2 v[B];
+#pragma unroll
+    for (int j = 0; j < B; ++j) v[j] = frame_input<N, OP>(g, r0, r1, psi, a, t + A * j);
+    line_stage1<N, -1>(v, t, tw);
+    __syncwarp();
+#pragma unroll
+    for (int k1 = 0; k1 < B; ++k1) rs[k1 * (A + 1) + t] = v[k1];
+    __syncwarp();
+    line_stage2<N, -1>(v, t, [&](int tt, int k1) { return rs[k1 * (A + 1) + tt]; });
+    // v[j] = X[a][t + A j]; column t + A j belongs to CTA j / JPC
+#pragma unroll
+    for (int j = 0; j < B; ++j) rc[j / JPC][a * CP + t + A * (j % JPC)] = v[j];
+  }
+  cluster.sync();
+
+  // ---------------- 3. column pass on the owned columns
+  ff err = ff_zero();
+#pragma unroll 1
+  for (int s = 0; s < CPC / CW; ++s) {
+    const int cl = s * CW + tid % CW, tc = tid / CW;
+    const int kc = rank * CPC + cl;
+    float2 v[B];
+#pragma unroll
+    for (int j = 0; j < B; ++j) v[j] = cbuf[(tc + A * j) * CP + cl];
+    line_stage1<N, -1>(v, tc, tw);
+    __syncthreads();
+#pragma unroll
+    for (int k1 = 0; k1 < B; ++k1) cbuf[(k1 * A + tc) * CP + cl] = v[k1];
+    __syncthreads();
+    line_stage2<N, -1>(v, tc, [&](int tt, int k1) { return cbuf[(k1 * A + tt) * CP + cl]; });
+#pragma unroll
+    for (int j = 0; j < B; ++j) frame_modulus<N, N, OP>(g, f, fbase, tc + A * j, kc, v[j], err);
+    if constexpr (INVERSE) {
+      line_stage1<N, +1>(v, tc, tw);
+      __syncthreads();
+#pragma unroll
+      for (int k1 = 0; k1 < B; ++k1) cbuf[(k1 * A + tc) * CP + cl] = v[k1];
+      __syncthreads();
+      line_stage2<N, +1>(v, tc, [&](int tt, int k1) { return cbuf[(k1 * A + tt) * CP + cl]; });
+      __syncthreads();
+#pragma unroll
+      for (int j = 0; j < B; ++j) cbuf[(tc + A * j) * CP + cl] = v[j];
+    }
+  }
+
+  if constexpr (INVERSE) {
+    cluster.sync();
+    // ---------------- 5. inverse row pass, pulled from the column owners
+#pragma unroll 1
+    for (int s = 0; s < RPC / RF; ++s) {
+      const int a = rank * RPC + s * RF + lr;
+      float2 v[B];
+#pragma unroll
+      for (int j = 0; j < B; ++j) v[j] = rc[j / JPC][a * CP + t + A * (j % JPC)];
+      line_stage1<N, +1>(v, t, tw);
+      __syncwarp();
+#pragma unroll
+      for (int k1 = 0; k1 < B; ++k1) rs[k1 * (A + 1) + t] = v[k1];
+      __syncwarp();
+      line_stage2<N, +1>(v, t, [&](int tt, int k1) { return rs[k1 * (A + 1) + tt]; });
+#pragma unroll
+      for (int j = 0; j < B; ++j) frame_output<N, OP>(g, r0, r1, psi, a, t + A * j, cscale(v[j], kInv));
+      __syncwarp();
+    }
+    cluster.sync();
+  }
+
+  if (g.err_part) {
+    const double sum = block_sum_d(ff_to_double(err), red);
+    if (tid == 0) g.err_part[(size_t)f * C + rank] = sum;
+  }
 }
+
+constexpr int kClusterN = 256, kClusterC = 4;
+
+template <int OP>
+static int set_cluster_attr() {
+  using K = ClusterCfg<kClusterN, kClusterC>;
+  cudaError_t e = cudaFuncSetAttribute(cluster_frame_kernel<kClusterN, kClusterC, OP>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)K::SMEM);
+  if (e != cudaSuccess) return set_cuda_error(e, "cluster_frame_kernel smem attribute");
+  return PTY_OK;
+}
+
+template <int OP>
+static int launch_cluster(const FrameArgs& a, int nframes, cudaStream_t st) {
+  using K = ClusterCfg<kClusterN, kClusterC>;
+  cluster_frame_kernel<kClusterN, kClusterC, OP><<<nframes * kClusterC, K::NT, K::SMEM, st>>>(a);
+  return check_launch("cluster_frame_kernel");
+}
+
+bool cluster_frame_supported() { return true; }
+
+int cluster_err_slots() { return kClusterC; }
+
+int prepare_cluster_frame_kernels() {
+  int rc = PTY_OK;
+  if (!rc) rc = set_cluster_attr<OP_EXIT1>();
+  if (!rc) rc = set_cluster_attr<OP_EXIT7>();
+  if (!rc) rc = set_cluster_attr<OP_PSI1>();
+  if (!rc) rc = set_cluster_attr<OP_PSI7>();
+  if (!rc) rc = set_cluster_attr<OP_DM1>();
+  if (!rc) rc = set_cluster_attr<OP_DM7>();
+  if (!rc) rc = set_cluster_attr<OP_MERR>();
+  if (!rc) rc = set_cluster_attr<OP_INTENS>();
+  if (!rc) rc = set_cluster_attr<OP_MERR_PSI>();
+  return rc;
+}
+
+int launch_cluster_frame_op(int op, const FrameArgs& a, int nframes, cudaStream_t st) {
+  switch (op) {
+    case OP_EXIT1: return launch_cluster<OP_EXIT1>(a, nframes, st);
+    case OP_EXIT7: return launch_cluster<OP_EXIT7>(a, nframes, st);
+    case OP_PSI1: return launch_cluster<OP_PSI1>(a, nframes, st);
+    case OP_PSI7: return launch_cluster<OP_PSI7>(a, nframes, st);
+    case OP_DM1: return launch_cluster<OP_DM1>(a, nframes, st);
+    case OP_DM7: return launch_cluster<OP_DM7>(a, nframes, st);
+    case OP_MERR: return launch_cluster<OP_MERR>(a, nframes, st);
+    case OP_INTENS: return launch_cluster<OP_INTENS>(a, nframes, st);
+    case OP_MERR_PSI: return launch_cluster<OP_MERR_PSI>(a, nframes, st);
+  }
+  return set_error(PTY_ERR_ARG, "unknown frame op");
+}
+
 }  // namespace pty

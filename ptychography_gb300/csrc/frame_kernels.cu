@@ -16,6 +16,7 @@
 // matching the reference's ifftshift-ed amp / mask.
 #include "engine.h"
 #include "fft_line.cuh"
+#include "frame_ops.cuh"
 
 namespace pty {
 
@@ -43,9 +44,7 @@ template <int N0, int N1, int OP>
 __global__ void __launch_bounds__(FrameCfg<N0, N1>::NT, 1) frame_kernel(FrameArgs g) {
   using C = FrameCfg<N0, N1>;
   constexpr int A0 = C::A0, B0 = C::B0, A1 = C::A1, B1 = C::B1, RP = C::RP, NT = C::NT;
-  constexpr bool IN_EXIT = (OP == OP_EXIT1 || OP == OP_EXIT7 || OP == OP_MERR || OP == OP_INTENS);
-  constexpr bool IN_DM = (OP == OP_DM1 || OP == OP_DM7);
-  constexpr bool INVERSE = !(OP == OP_MERR || OP == OP_MERR_PSI || OP == OP_INTENS);
+  constexpr bool INVERSE = OpTraits<OP>::INVERSE;
   constexpr float kInv = 1.0f / (float)(N0 * N1);
 
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -60,7 +59,7 @@ __global__ void __launch_bounds__(FrameCfg<N0, N1>::NT, 1) frame_kernel(FrameArg
   for (int i = tid; i < N1; i += NT) tw1[i] = g.tw1[i];
 
   int r0 = 0, r1 = 0;
-  if (IN_EXIT || IN_DM) {
+  if (OpTraits<OP>::IN_EXIT || OpTraits<OP>::IN_DM) {
     r0 = g.R[2 * f];
     r1 = g.R[2 * f + 1];
   }
@@ -68,34 +67,12 @@ __global__ void __launch_bounds__(FrameCfg<N0, N1>::NT, 1) frame_kernel(FrameArg
   float2* psi = g.psi + fbase;
   __syncthreads();
 
-  // exit wave P * O[window] at frame pixel (a, b)
-  auto exitw = [&](int a, int b) -> float2 {
-    int u = a - r0, v = b - r1;
-    if (u >= g.U) u -= g.U;
-    if (v >= g.V) v -= g.V;
-    return cmul(__ldg(&g.O[(size_t)u * g.V + v]), __ldg(&g.P[a * N1 + b]));
-  };
-
-  // ---------------- forward row pass
+  // ---------------- forward row pass (a row's A1 threads share a warp)
   for (int id = tid; id < N0 * A1; id += NT) {
     const int t = id % A1, a = id / A1;
     float2 v[B1];
 #pragma unroll
-    for (int j = 0; j < B1; ++j) {
-      const int b = t + A1 * j;
-      float2 x;
-      if constexpr (IN_EXIT) {
-        x = exitw(a, b);
-      } else if constexpr (IN_DM) {
-        // dm.py:94-95: e1 = psi - ex0 ; x = ex0 - e1
-        float2 ex0 = exitw(a, b);
-        float2 e1 = csub(psi[a * N1 + b], ex0);
-        x = csub(ex0, e1);
-      } else {
-        x = psi[a * N1 + b];
-      }
-      v[j] = x;
-    }
+    for (int j = 0; j < B1; ++j) v[j] = frame_input<N1, OP>(g, r0, r1, psi, a, t + A1 * j);
     line_stage1<N1, -1>(v, t, tw1);
     float2* row = fr + a * RP;
 #pragma unroll
@@ -126,59 +103,8 @@ __global__ void __launch_bounds__(FrameCfg<N0, N1>::NT, 1) frame_kernel(FrameArg
     for (int k1 = 0; k1 < B0; ++k1) fr[(k1 * A0 + t) * RP + cp] = v[k1];
     __syncthreads();
     line_stage2<N0, -1>(v, t, [&](int tt, int k1) { return fr[(k1 * A0 + tt) * RP + cp]; });
-
-    // v[j] = F[kr][c], kr = t + A0 j
 #pragma unroll
-    for (int j = 0; j < B0; ++j) {
-      const int kr = t + A0 * j;
-      const int pix = kr * N1 + c;
-      const float2 F = v[j];
-      const float msk = g.mask ? (float)g.mask[pix] : 1.0f;
-      if constexpr (OP == OP_INTENS) {
-        const int sr = (kr + N0 / 2) % N0, sc = (c + N1 / 2) % N1;
-        g.out_real[fbase + (size_t)sr * N1 + sc] = cabs2(F);
-      } else {
-        const float am = g.amp[(size_t)g.amp_stride * f + pix];
-        if constexpr (OP == OP_EXIT1 || OP == OP_PSI1 || OP == OP_DM1) {
-          // era.py:561-571
-          const float mag = sqrtf(cabs2(F)) + g.alpha;
-          if (g.err_part) {
-            const float d = mag - am;
-            err = ff_add(err, d * d * msk);
-          }
-          const float fac = (msk != 0.f) ? am / mag : 1.0f;
-          v[j] = cscale(F, fac);
-        } else if constexpr (OP == OP_EXIT7 || OP == OP_PSI7) {
-          // era.py:584-594
-          const float b = g.bg_in[(size_t)g.bg_stride * f + pix];
-          const float mag = sqrtf(cabs2(F) + b * b + g.alpha);
-          if (g.err_part) {
-            const float d = mag - am;
-            err = ff_add(err, d * d * msk);
-          }
-          const float fac = msk * am / mag;
-          v[j] = cscale(F, fac);
-          g.bg_out[fbase + pix] = b * fac;
-        } else if constexpr (OP == OP_DM7) {
-          // dm.py:219-224 on the background: g1 = g - b0 ; tb = b0 - g1 ; g = g1 + Pmod7(tb)
-          const float gs = g.bg_out[fbase + pix];
-          const float b0 = g.b0[pix];
-          const float g1 = gs - b0;
-          const float tb = b0 - g1;
-          const float mag = sqrtf(cabs2(F) + tb * tb + g.alpha);
-          const float fac = msk * am / mag;
-          v[j] = cscale(F, fac);
-          g.bg_out[fbase + pix] = g1 + tb * fac;
-        } else if constexpr (OP == OP_MERR || OP == OP_MERR_PSI) {
-          // dm.py:338-340, no alpha
-          const float b = g.bg_in ? g.bg_in[(size_t)g.bg_stride * f + pix] : 0.0f;
-          const float mag = sqrtf(cabs2(F) + b * b);
-          const float d = mag - am;
-          err = ff_add(err, msk * (d * d));
-        }
-      }
-    }
-
+    for (int j = 0; j < B0; ++j) frame_modulus<N0, N1, OP>(g, f, fbase, t + A0 * j, c, v[j], err);
     if constexpr (INVERSE) {
       line_stage1<N0, +1>(v, t, tw0);
       __syncthreads();
@@ -208,18 +134,8 @@ __global__ void __launch_bounds__(FrameCfg<N0, N1>::NT, 1) frame_kernel(FrameArg
       __syncwarp();
       line_stage2<N1, +1>(v, t, [&](int tt, int k1) { return row[k1 * (A1 + 1) + tt]; });
 #pragma unroll
-      for (int j = 0; j < B1; ++j) {
-        const int b = t + A1 * j;
-        const float2 r = cscale(v[j], kInv);
-        if constexpr (IN_DM) {
-          // dm.py:94-97: psi_new = (psi - ex0) + Pmod(2 ex0 - psi)
-          float2 ex0 = exitw(a, b);
-          float2 e1 = csub(psi[a * N1 + b], ex0);
-          psi[a * N1 + b] = cadd(e1, r);
-        } else {
-          psi[a * N1 + b] = r;
-        }
-      }
+      for (int j = 0; j < B1; ++j)
+        frame_output<N1, OP>(g, r0, r1, psi, a, t + A1 * j, cscale(v[j], kInv));
     }
   }
 
