@@ -1,0 +1,517 @@
+"""Benchmark of the ERA / DM reconstruction loop on one GB300 (or N replicas).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+                    [--workload c1|c0]
+
+Workload c1 (default, the headline): 1024 frames of 256 x 256 on a 32 x 32
+raster (step 24 px, +-3 px seeded jitter), object 1024 x 1024 (Gaussian-filtered
+random amplitude 0.5-1 and phase +-pi/2), probe a 64 px aperture with an 8 px
+Gaussian edge and quadratic phase, initial probe with that phase coefficient
+x1.2, additive background 0.01 mean(I) x smooth blob, Poisson noise at 1e6
+photons per frame, mask = 12 px beamstop + 0.5 % dead pixels.  All synthetic
+and seeded.  One step = one ERA iteration (method 6: object + probe +
+background) followed by one DM iteration (method 6) over all 1024 frames.
+Workload c0: 100 frames of 128 x 128, object 320 x 320, noise free, ERA method 1.
+
+Metric: frame-iterations per second (n_frames x iterations / s).  `value` is
+timed with CUDA events around device-resident steps; `e2e` runs the public
+pty.ERA / pty.DM calls on host arrays.  The exit waves (537 MB at c1) exceed the
+126 MB L2, so no L2 flush is needed between steps.
+
+--impl reference times the CPU oracle (a NumPy port of the reference's
+era.py / dm.py) on the host cores: one process per core, each on its own
+disjoint shard of frames (no all-reduce), every step a bounded sample.
+"""
+import argparse
+import ctypes
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+
+# --------------------------------------------------------------------------- workloads
+def _smooth01(rng, shape, sigma=4.0):
+    import scipy.ndimage as ndi
+    a = ndi.gaussian_filter(rng.random(shape), sigma)
+    return (a - a.min()) / (a.max() - a.min())
+
+
+def make_object(rng, U):
+    return (0.5 + 0.5 * _smooth01(rng, (U, U))) * np.exp(1j * np.pi * (_smooth01(rng, (U, U)) - 0.5))
+
+
+def make_probe(N, radius, edge, quad):
+    y, x = np.mgrid[:N, :N] - N / 2
+    r = np.sqrt(x ** 2 + y ** 2)
+    amp = np.exp(-np.clip(r - radius, 0, None) ** 2 / (2 * edge ** 2)) * (r < radius + 3 * edge)
+    return amp * np.exp(1j * quad * r ** 2)
+
+
+def raster(rng, side, step, jitter, N, U, offset=4):
+    pos = np.arange(side) * step + offset
+    R = -np.stack(np.meshgrid(pos, pos, indexing="ij"), -1).reshape(-1, 2)
+    R = R + rng.integers(-jitter, jitter + 1, R.shape)
+    return np.clip(R, -(U - N), 0).astype(np.int64)
+
+
+class Workload:
+    pass
+
+
+def workload_c1(exits_fn, frames=None):
+    """The 256^2 / 1024-frame job; `exits_fn(O, P, R)` returns |FFT2(P O[R])|^2 per frame."""
+    rng = np.random.default_rng(1)
+    N, U, side = 256, 1024, 32
+    w = Workload()
+    w.name = "c1"
+    w.O_true = make_object(rng, U)
+    w.P_true = make_probe(N, 64, 8, 0.0005)
+    w.P0 = make_probe(N, 64, 8, 0.0006)
+    w.R = raster(rng, side, 24, 3, N, U)
+    if frames is not None:
+        w.R = w.R[frames]
+    I = exits_fn(w.O_true, w.P_true, w.R)                      # unshifted |F|^2
+    y, x = np.mgrid[:N, :N] - N / 2
+    blob = np.fft.ifftshift(np.exp(-(x ** 2 + y ** 2) / (2 * 40.0 ** 2)))
+    I = I + 0.01 * I.mean() * blob
+    I = I * (1e6 / I.sum(axis=(1, 2), keepdims=True))
+    I = rng.poisson(I).astype(np.float32)
+    w.I = np.fft.fftshift(I, axes=(-2, -1))                    # centred, as recorded
+    M = np.ones((N, N), bool)
+    M[np.sqrt(x ** 2 + y ** 2) < 12] = False
+    M[rng.random((N, N)) < 0.005] = False
+    w.M = M
+    w.method = 6
+    w.N, w.U = N, U
+    return w
+
+
+def workload_c0(exits_fn):
+    rng = np.random.default_rng(0)
+    N, U = 128, 320
+    w = Workload()
+    w.name = "c0"
+    w.O_true = make_object(rng, U)
+    w.P_true = make_probe(N, 32, 4, 0.002)
+    w.P0 = w.P_true
+    w.R = raster(rng, 10, 16, 2, N, U, offset=16)
+    w.I = np.fft.fftshift(exits_fn(w.O_true, w.P_true, w.R), axes=(-2, -1)).astype(np.float32)
+    w.M = np.ones((N, N), bool)
+    w.method = 1
+    w.N, w.U = N, U
+    return w
+
+
+def numpy_intensities(O, P, R):
+    """|FFT2(P O[R])|^2 on the host (used only where no GPU is involved)."""
+    N = P.shape[0]
+    rows = (np.arange(N)[None, :] - R[:, 0:1])
+    cols = (np.arange(N)[None, :] - R[:, 1:2])
+    out = np.empty((len(R), N, N))
+    for i in range(0, len(R), 64):
+        ex = O[rows[i:i + 64, :, None], cols[i:i + 64, None, :]] * P
+        out[i:i + 64] = np.abs(np.fft.fft2(ex)) ** 2
+    return out
+
+
+def gpu_intensities(O, P, R):
+    from ptychography_gb300.forward_models import diffraction_intensities
+    I = diffraction_intensities(O, P, R)                       # fftshift(|F|^2)
+    return np.fft.ifftshift(I, axes=(-2, -1))
+
+
+# --------------------------------------------------------------------------- clocks
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu):
+        self.gpu, self.rows, self.proc = gpu, [], None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.Q,
+                 "--format=csv,noheader,nounits", "-lms", "50"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.t.join(timeout=2)
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4)
+                          if len(r) > 5 + i and r[5 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(self.rows)}
+
+
+# --------------------------------------------------------------------------- GPU arm
+class DeviceJob:
+    """Device-resident ERA/DM state of a workload, driven through the C ABI."""
+
+    def __init__(self, w, dev):
+        import torch
+        from ptychography_gb300 import _engine, _native
+        self.torch, self.lib, self.native = torch, _native.load(), _native
+        self.w, self.dev = w, dev
+        np.random.seed(12)
+        pre = _engine.Preamble(w.I, w.R.copy(), w.P0, None, 1, w.M, None, w.method, "single")
+        self.pre = pre
+        n, N0, N1 = pre.n, pre.N0, pre.N1
+        U, V = pre.O.shape
+        self.n, self.N, self.U, self.V = n, N0, U, V
+        R64 = np.ascontiguousarray(pre.R[:, :2], dtype=np.int64)
+        self.plan = ctypes.c_void_p()
+        _native.check(self.lib.pty_plan_create(ctypes.byref(_native.Geometry(n, N0, N1, U, V)),
+                                               R64.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)),
+                                               ctypes.byref(self.plan)))
+        t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)  # noqa: E731
+        I_d = t(pre.I.astype(np.float32))
+        self.amp = torch.empty((n, N0, N1), dtype=torch.float32, device=dev)
+        _native.check(self.lib.pty_amp_from_intensity(self.plan, self.p(I_d), 0, self.p(self.amp),
+                                                      self.sp()))
+        del I_d
+        self.O0 = pre.O.astype(np.complex64)
+        self.O = t(self.O0)
+        self.P = t(pre.P.astype(np.complex64))
+        self.psi = torch.empty((n, N0, N1), dtype=torch.complex64, device=dev)
+        self.mask = t(pre.mask) if pre.mask is not None else None
+        self.bg = t(pre.background) if pre.background is not None else None
+        self.bmean = torch.zeros((N0, N1), dtype=torch.float32, device=dev)
+        self.heat = torch.zeros((U, V), dtype=torch.float64, device=dev)
+        self.emod = torch.zeros(4096, dtype=torch.float64, device=dev)
+        self.econ = torch.zeros(4096, dtype=torch.float64, device=dev)
+        self.I_norm = pre.I_norm
+
+    def p(self, x):
+        return ctypes.c_void_p(x.data_ptr()) if x is not None else None
+
+    def sp(self):
+        return ctypes.c_void_p(self.torch.cuda.current_stream(self.dev).cuda_stream)
+
+    def run(self, kind, method, iters):
+        nat = self.native
+        buf = nat.Buffers(self.p(self.O), self.p(self.P), self.p(self.psi), self.p(self.amp),
+                          self.p(self.mask), self.p(self.bg), None, self.p(self.bmean),
+                          self.p(self.heat), None, self.p(self.emod), self.p(self.econ))
+        opt = nat.Options(method, 1, 1, 0, 0, 1, 1e-10, self.I_norm)
+        hv = ctypes.c_int32(0)
+        fn = self.lib.pty_era if kind == "era" else self.lib.pty_dm
+        nat.check(fn(self.plan, ctypes.byref(buf), ctypes.byref(opt), iters, ctypes.byref(hv), self.sp()))
+
+    def step(self):
+        if self.w.method == 6:
+            self.run("era", 6, 1)
+            self.run("dm", 6, 1)
+        else:
+            self.run("era", self.w.method, 1)
+
+    def frames_per_step(self):
+        return self.n * (2 if self.w.method == 6 else 1)
+
+    def close(self):
+        self.lib.pty_plan_destroy(self.plan)
+
+
+def event_time(torch, fn, reps):
+    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    s.record()
+    for _ in range(reps):
+        fn()
+    e.record()
+    torch.cuda.synchronize()
+    return s.elapsed_time(e) / 1e3
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def roofline_pmod7(job, torch, reps=20):
+    """Fused frame kernel (Pmod_7 form, the DM m6 modulus step) alone, event-timed.
+
+    Algorithmic bytes per frame: psi read 8 N^2 + psi write 8 N^2 + amp 4 N^2 +
+    background read 4 N^2 + background write 4 N^2 = 28 N^2.
+    """
+    lib, p = job.lib, job.p
+    job.lib.pty_make_exits(job.plan, p(job.O), p(job.P), p(job.psi), job.sp())
+    bg = job.bg if job.bg is not None else torch.ones_like(job.amp)
+    fn = lambda: lib.pty_pmod_7(job.plan, p(job.amp), p(bg), p(job.psi), p(job.mask), 1e-10, None,  # noqa: E731
+                                job.sp())
+    for _ in range(3):
+        fn()
+    t = event_time(torch, fn, reps) / reps
+    bytes_ = 28.0 * job.N * job.N * job.n
+    pk, kind = peaks()
+    gbs = bytes_ / t / 1e9
+    return {"kernel": "cluster_frame_kernel<256,4,PSI7>" if job.N == 256 else "frame_kernel<PSI7>",
+            "bound": "hbm", "achieved": round(gbs, 1), "peak": pk, "unit": "GB/s",
+            "frac": round(gbs / pk, 4), "peak_kind": kind, "traffic": None,
+            "launch_ms": round(t * 1e3, 4), "algorithmic_bytes": bytes_}
+
+
+def era_m1_rate(job, torch, K):
+    """Plain FP32 ERA (method 1, object only) on the same frames: rate and HBM fraction.
+
+    Algorithmic bytes per iteration: 20 N^2 per frame (amp 4, psi write 8,
+    psi read by the object gather 8) + 24 U V (object read, write, denominator).
+    """
+    job.O.copy_(torch.from_numpy(job.O0).to(job.dev))
+    for _ in range(3):
+        job.run("era", 1, 1)
+    t = event_time(torch, lambda: job.run("era", 1, 1), K) / K
+    bytes_ = 20.0 * job.N * job.N * job.n + 24.0 * job.U * job.V
+    pk, _ = peaks()
+    return {"frame_iters_per_s": round(job.n / t, 1), "ms_per_iter": round(t * 1e3, 4),
+            "hbm_gbs": round(bytes_ / t / 1e9, 1), "hbm_frac": round(bytes_ / t / 1e9 / pk, 4)}
+
+
+def e2e_public_api(w, K):
+    """The public API on host arrays: ERA (K iterations) then DM (K iterations)."""
+    import torch
+    import ptychography_gb300 as pty
+    torch.cuda.synchronize()
+    np.random.seed(13)
+    t0 = time.perf_counter()
+    if w.method == 6:
+        O, P, info = pty.ERA(w.I, w.R.copy(), w.P0, None, K, mask=w.M, method=6)
+        O, P, info2 = pty.DM(w.I, w.R.copy(), P, O, K, mask=w.M, method=6,
+                             background=info["background"])
+        res = (O, P, info2["eMod"][-1])
+    else:
+        O, info = pty.ERA(w.I, w.R.copy(), w.P0, None, K, mask=w.M, method=w.method)
+        res = (O, info["eMod"][-1])
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    n, N = w.I.shape[0], w.I.shape[1]
+    U = w.U
+    calls = 2 if w.method == 6 else 1
+    # per call: I (float32), background stack (float32), O, P, mask up; O, P,
+    # info['I'] (float32), heatmap (float64), histories and mean background down
+    h2d = calls * (n * N * N * 4 + (n * N * N * 4 if w.method >= 4 else 0) + U * U * 8 + N * N * 9)
+    d2h = calls * (U * U * 8 + N * N * 8 + n * N * N * 4 + U * U * 8 + 16 * K + N * N * 4)
+    frames = n * K * calls
+    return {"value": round(frames / dt, 1), "unit": "frame-iters/s",
+            "h2d_bytes_per_step": int(h2d / K), "d2h_bytes_per_step": int(d2h / K),
+            "wall_s": round(dt, 3), "final_eMod": float(res[-1])}
+
+
+# --------------------------------------------------------------------------- CPU oracle
+def _oracle_shard(args):
+    """One worker of the CPU baseline: oracle ERA m6 + DM m6, one iteration each."""
+    shard, seed_frames, method = args
+    sys.path.insert(0, ROOT)
+    from oracle import ptycho_oracle as orc
+    w = workload_c1(numpy_intensities, frames=seed_frames) if method == 6 else workload_c0(numpy_intensities)
+    np.random.seed(shard)
+    t0 = time.perf_counter()
+    if method == 6:
+        O, P, info = orc.ERA(w.I, w.R.copy(), w.P0, None, 1, mask=w.M, method=6, dtype="single")
+        orc.DM(w.I, w.R.copy(), P, O, 1, mask=w.M, method=6, dtype="single",
+               background=info["background"], full_output=False)
+        n_fi = 2 * len(w.R)
+    else:
+        orc.ERA(w.I, w.R.copy(), w.P0, None, 1, mask=w.M, method=1, dtype="single", full_output=False)
+        n_fi = len(w.R)
+    return n_fi, time.perf_counter() - t0
+
+
+def cpu_oracle_rate(method, shard_frames, cores, pool=None):
+    """Frame-iterations per second of the oracle on `cores` disjoint shards."""
+    chunks = [(i, np.arange(i * shard_frames, (i + 1) * shard_frames) % 1024, method)
+              for i in range(cores)]
+    t0 = time.perf_counter()
+    if pool is None:
+        res = [_oracle_shard(c) for c in chunks]
+    else:
+        res = pool.map(_oracle_shard, chunks)
+    wall = time.perf_counter() - t0
+    return sum(r[0] for r in res) / wall, wall
+
+
+# --------------------------------------------------------------------------- main
+def dist_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), \
+        int(os.environ.get("LOCAL_RANK", 0))
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    import multiprocessing as mp
+    cores = os.cpu_count() or 1
+    method = 6 if args.workload == "c1" else 1
+    shard = 16 if method == 6 else 100
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(cores) as pool:
+        for _ in range(args.warmup):
+            cpu_oracle_rate(method, shard, cores, pool)
+        rates, walls = [], []
+        for _ in range(args.steps):
+            r, wll = cpu_oracle_rate(method, shard, cores, pool)
+            rates.append(r)
+            walls.append(wll)
+    total_fi = (2 if method == 6 else 1) * shard * cores * args.steps
+    value = total_fi / sum(walls)
+    line = {
+        "impl": "reference", "metric": "frame-iters/s", "value": round(value, 2),
+        "unit": "frame-iters/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(1e3 * sum(walls) / args.steps, 2), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": workload_config(args.workload),
+        "cpu_baseline": {"value": round(value, 2), "unit": "frame-iters/s", "cores": cores,
+                         "kind": "port",
+                         "sample": "%d processes x %d disjoint frames, ERA m6 + DM m6 one iteration "
+                                   "each per step (oracle NumPy port, no all-reduce)" % (cores, shard)
+                         if method == 6 else "%d processes x 100 frames, ERA m1 one iteration" % cores},
+        "e2e": {"value": round(value, 2), "unit": "frame-iters/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def workload_config(name):
+    if name == "c1":
+        return {"workload": "ERA m6 then DM m6 (object+probe+background), 1024 frames 256x256, "
+                            "object 1024x1024, Poisson 1e6, beamstop+dead-pixel mask",
+                "n_frames": 1024, "frame": [256, 256], "object": [1024, 1024],
+                "step": "1 ERA-m6 iteration + 1 DM-m6 iteration over all frames",
+                "l2": "working set (psi 537 MB) larger than L2; no flush"}
+    return {"workload": "ERA m1 (object only), 100 frames 128x128, object 320x320, noise free",
+            "n_frames": 100, "frame": [128, 128], "object": [320, 320],
+            "step": "1 ERA-m1 iteration over all frames",
+            "l2": "working set 20 MB fits in L2: reported as an L2-resident case"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="c1", choices=["c1", "c0"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--frames", type=int, default=None,
+                    help="use only the first F frames of the c1 raster (profiling captures)")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    from ptychography_gb300 import _native
+    lib = _native.load()
+
+    if args.workload == "c1":
+        w = workload_c1(gpu_intensities, frames=np.arange(args.frames) if args.frames else None)
+    else:
+        w = workload_c0(gpu_intensities)
+    job = DeviceJob(w, dev)
+    for _ in range(args.warmup):
+        job.step()
+    torch.cuda.synchronize()
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    launches0 = lib.pty_launch_count()
+    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        s.record()
+        for _ in range(args.steps):
+            job.step()
+        e.record()
+        torch.cuda.synchronize()
+    barrier()
+    launches = lib.pty_launch_count() - launches0
+    t = s.elapsed_time(e) / 1e3
+    if world > 1:
+        tt = torch.tensor([t], device=dev)
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        t = float(tt.item())
+    frames = job.frames_per_step() * args.steps * world
+    value = frames / t
+
+    roof = roofline_pmod7(job, torch)
+    m1 = era_m1_rate(job, torch, max(args.steps, 10)) if args.workload == "c1" else None
+    job.close()
+    if rank != 0:
+        return 0
+
+    e2e = None if args.no_e2e else e2e_public_api(w, args.steps)
+    cpu = None
+    if not args.no_cpu_baseline:
+        method = w.method
+        shard = 48 if method == 6 else 100
+        r, wall = cpu_oracle_rate(method, shard, 1)
+        cpu = {"value": round(r, 2), "unit": "frame-iters/s", "cores": 1, "kind": "port",
+               "sample": ("ERA m6 + DM m6, one iteration each, on %d of the 1024 frames "
+                          "(oracle NumPy port, single process), %.1f s" % (shard, wall))
+               if method == 6 else "ERA m1 one iteration on the 100 frames, %.1f s" % wall}
+    line = {
+        "metric": "frame-iters/s", "value": round(value, 1), "unit": "frame-iters/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(1e3 * t / args.steps, 4), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": dict(workload_config(args.workload), parallelism="replicas" if world > 1 else "1 GPU"),
+        "gpu_launches": int(launches), "clocks": clk.summary(), "roofline": roof,
+        "cpu_baseline": cpu, "e2e": e2e,
+    }
+    if m1:
+        line["era_m1"] = m1
+    print(json.dumps(line))
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -126,6 +126,10 @@ int pty_amp_from_intensity(pty_plan* plan, const void* I, int32_t is_double, flo
 int pty_shape_supported(int32_t N0, int32_t N1);
 const char* pty_last_error(void);
 int pty_version(void);
+/* Kernels this library has launched in the process so far (direct launches
+ * plus the kernel nodes of replayed CUDA graphs).  No reference counterpart:
+ * it lets a caller confirm the GPU path ran. */
+int64_t pty_launch_count(void);
 
 #ifdef __cplusplus
 }

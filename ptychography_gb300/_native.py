@@ -55,8 +55,9 @@ SIGNATURES = {
     "pty_shape_supported": [c_int32, c_int32],
     "pty_last_error": [],
     "pty_version": [],
+    "pty_launch_count": [],
 }
-_RESTYPES = {"pty_last_error": ctypes.c_char_p}
+_RESTYPES = {"pty_last_error": ctypes.c_char_p, "pty_launch_count": ctypes.c_int64}
 
 
 class PtyError(RuntimeError):

@@ -7,6 +7,7 @@
 // gathers of overlap_kernels.cu, and the modulus projection is the fused frame
 // kernel.  Nothing is copied to the host inside the loop; the error histories
 // are written to device arrays.
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -28,9 +29,14 @@ int set_cuda_error(cudaError_t e, const char* where) {
   g_last_error = std::string(where) + ": " + cudaGetErrorString(e);
   return PTY_ERR_CUDA;
 }
+static std::atomic<long long> g_launches{0};
+void count_launches(long long k) { g_launches += k; }
+long long launch_total() { return g_launches.load(); }
+
 int check_launch(const char* where) {
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return set_cuda_error(e, where);
+  g_launches += 1;
   return PTY_OK;
 }
 
@@ -66,7 +72,8 @@ struct pty_plan {
   float2* d_part_den = nullptr;
   int Km = 1;                    // background-mean frame chunks
   float2* d_mean_part = nullptr;
-  double* d_err_part = nullptr;  // [n]
+  double* d_err_part = nullptr;  // [n * eslots]
+  int eslots = 1;                // error partials per frame
   int ndn = 64;                  // diffnorm blocks per array
   double* d_dn_part = nullptr;   // [2 arrays][ndn][2]
   int* d_shift = nullptr;
@@ -82,10 +89,13 @@ struct pty_plan {
   double* d_sum = nullptr;
   cudaStream_t cap = nullptr;    // capture stream
   cudaEvent_t ev_in = nullptr, ev_out = nullptr;
-  // last captured loop: replayed when a call repeats the same request
-  std::string graph_key;
-  cudaGraphExec_t graph_exec = nullptr;
-  int graph_heat_valid = 0;
+  // last captured loop of each kind (ERA, DM): replayed when a call repeats it
+  struct CachedGraph {
+    std::string key;
+    cudaGraphExec_t exec = nullptr;
+    int heat_valid = 0;
+    long long kernels = 0;
+  } graphs[2];
   std::vector<void*> allocs;
 };
 
@@ -132,13 +142,16 @@ extern "C" int pty_shape_supported(int32_t N0, int32_t N1) {
 
 extern "C" int pty_version(void) { return 100; }
 
+extern "C" int64_t pty_launch_count(void) { return (int64_t)launch_total(); }
+
 extern "C" const char* pty_last_error(void) { return g_last_error.c_str(); }
 
 extern "C" int pty_plan_destroy(pty_plan* p) {
   if (!p) return PTY_OK;
   for (void* a : p->allocs) cudaFree(a);
   if (p->d_psi_tmp) cudaFree(p->d_psi_tmp);
-  if (p->graph_exec) cudaGraphExecDestroy(p->graph_exec);
+  for (auto& cg : p->graphs)
+    if (cg.exec) cudaGraphExecDestroy(cg.exec);
   if (p->cap) cudaStreamDestroy(p->cap);
   if (p->ev_in) cudaEventDestroy(p->ev_in);
   if (p->ev_out) cudaEventDestroy(p->ev_out);
@@ -210,7 +223,8 @@ extern "C" int pty_plan_create(const pty_geometry* g, const int64_t* R_host, pty
   if ((rc = dalloc_t(p, &p->d_part_num, (size_t)p->K * npix))) return fail(rc);
   if ((rc = dalloc_t(p, &p->d_part_den, (size_t)p->K * npix))) return fail(rc);
   if ((rc = dalloc_t(p, &p->d_mean_part, (size_t)(p->Km > p->K ? p->Km : p->K) * npix))) return fail(rc);
-  if ((rc = dalloc_t(p, &p->d_err_part, (size_t)n))) return fail(rc);
+  p->eslots = frame_err_slots(N0, N1);
+  if ((rc = dalloc_t(p, &p->d_err_part, (size_t)n * p->eslots))) return fail(rc);
   if ((rc = dalloc_t(p, &p->d_dn_part, (size_t)4 * p->ndn))) return fail(rc);
   if ((rc = dalloc_t(p, &p->d_shift, 2))) return fail(rc);
   if ((rc = dalloc_t(p, &p->d_bakO, nobj))) return fail(rc);
@@ -338,13 +352,17 @@ static int run_on_stream(pty_plan* p, cudaStream_t user, bool graph, const std::
   PTY_CUDA(cudaEventRecord(p->ev_in, user));
   PTY_CUDA(cudaStreamWaitEvent(p->cap, p->ev_in, 0));
   int rc = PTY_OK;
-  if (graph && p->graph_exec && p->graph_key == key) {
-    cudaError_t e = cudaGraphLaunch(p->graph_exec, p->cap);
+  auto& slot = p->graphs[key[0] == 'D' ? 1 : 0];
+  if (graph && slot.exec && slot.key == key) {
+    cudaError_t e = cudaGraphLaunch(slot.exec, p->cap);
     if (e != cudaSuccess) rc = set_cuda_error(e, "graph replay");
-    heat_valid = p->graph_heat_valid != 0;
+    else count_launches(slot.kernels);
+    heat_valid = slot.heat_valid != 0;
   } else if (graph) {
     PTY_CUDA(cudaStreamBeginCapture(p->cap, cudaStreamCaptureModeThreadLocal));
+    const long long before = launch_total();
     rc = body(p->cap);
+    const long long nkern = launch_total() - before;
     cudaGraph_t g = nullptr;
     cudaError_t e = cudaStreamEndCapture(p->cap, &g);
     if (rc == PTY_OK && e != cudaSuccess) rc = set_cuda_error(e, "cudaStreamEndCapture");
@@ -356,10 +374,11 @@ static int run_on_stream(pty_plan* p, cudaStream_t user, bool graph, const std::
         rc = set_cuda_error(e, "graph launch");
         if (ge) cudaGraphExecDestroy(ge);
       } else {
-        if (p->graph_exec) cudaGraphExecDestroy(p->graph_exec);
-        p->graph_exec = ge;
-        p->graph_key = key;
-        p->graph_heat_valid = heat_valid ? 1 : 0;
+        if (slot.exec) cudaGraphExecDestroy(slot.exec);
+        slot.exec = ge;
+        slot.key = key;
+        slot.heat_valid = heat_valid ? 1 : 0;
+        slot.kernels = nkern;
       }
     }
     if (g) cudaGraphDestroy(g);
@@ -444,7 +463,7 @@ extern "C" int pty_era(pty_plan* p, const pty_buffers* b, const pty_options* o, 
       if (use_bg) PTY_TRY(launch_frame_mean(p->n, (int)npix, p->d_bgf, p->d_mean_part, p->Km, p->d_b0, st));
       int ndn = 0;
       PTY_TRY(econ_partials(p, upd, p->d_bakO, O, p->d_bakP, P, st, &ndn));
-      PTY_TRY(launch_finalize(p->d_err_part, p->n, p->d_dn_part, ndn, o->I_norm, b->eMod, b->eCon, i, st));
+      PTY_TRY(launch_finalize(p->d_err_part, p->n * p->eslots, p->d_dn_part, ndn, o->I_norm, b->eMod, b->eCon, i, st));
     }
     if (b->intensities) {  // era.py:295
       FrameArgs a = base_args(p);
@@ -593,7 +612,7 @@ extern "C" int pty_dm(pty_plan* p, const pty_buffers* b, const pty_options* o, i
       }
       int ndn = 0;
       PTY_TRY(econ_partials(p, upd, p->d_bakO, Os, p->d_bakP, Ps, st, &ndn));
-      PTY_TRY(launch_finalize(p->d_err_part, n, p->d_dn_part, ndn, o->I_norm, b->eMod, b->eCon, i, st));
+      PTY_TRY(launch_finalize(p->d_err_part, n * p->eslots, p->d_dn_part, ndn, o->I_norm, b->eMod, b->eCon, i, st));
       if (upd & 1) PTY_TRY(copy_d2d(p->d_bakO, Os, nobj * sizeof(float2), st));
       if (upd & 2) PTY_TRY(copy_d2d(p->d_bakP, Ps, npix * sizeof(float2), st));
     }
@@ -625,7 +644,7 @@ static __global__ void sum_kernel(const double* x, int n, double* out) {
 }
 
 static int sum_partials(pty_plan* p, double* out, cudaStream_t st) {
-  sum_kernel<<<1, 256, 0, st>>>(p->d_err_part, p->n, out);
+  sum_kernel<<<1, 256, 0, st>>>(p->d_err_part, p->n * p->eslots, out);
   return check_launch("sum_kernel");
 }
 

@@ -47,11 +47,16 @@ int launch_frame_op(int op, int N0, int N1, const FrameArgs& a, int nframes, cud
 bool cluster_frame_supported();
 int launch_cluster_frame_op(int op, const FrameArgs& a, int nframes, cudaStream_t st);
 int prepare_cluster_frame_kernels();
+int cluster_err_slots();
+// error-partial slots each frame writes (one per CTA working on it)
+inline int frame_err_slots(int N0, int N1) { return (N0 == 256 && N1 == 256) ? cluster_err_slots() : 1; }
 
 // error reporting (engine.cu)
 int set_error(int code, const char* msg);
 int set_cuda_error(cudaError_t e, const char* where);
-int check_launch(const char* where);
+int check_launch(const char* where);  // also counts the launch
+void count_launches(long long k);
+long long launch_total();
 
 // ------------------------------------------------------------ overlap kernels
 struct TileLists {
