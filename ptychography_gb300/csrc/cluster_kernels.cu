@@ -35,15 +35,15 @@ struct ClusterCfg {
   static constexpr int NT = 512;
   static constexpr int RPC = N / C;          // rows owned per CTA
   static constexpr int CPC = N / C;          // columns owned per CTA
-  static constexpr int CP = CPC;             // column-buffer pitch (float2)
+  static constexpr int CP = CPC + 1;         // column-buffer pitch (float2), odd
   static constexpr int RF = NT / A;          // rows in flight per row sub-pass
   static constexpr int ROWLEN = B * (A + 1); // padded row-exchange length
   static constexpr int CW = NT / A;          // columns per column sub-pass
   static constexpr int JPC = CPC / A;        // row registers per destination CTA
-  static constexpr size_t CBUF = (size_t)N * CP;
+  static constexpr size_t CBUF = (size_t)N * CP + N / A;  // + one skew slot per A rows
   static constexpr size_t RSCR = (size_t)RF * ROWLEN;
   static constexpr size_t SMEM = (CBUF + RSCR + N) * sizeof(float2) + 32 * sizeof(double);
-  static_assert(RPC % RF == 0 && CPC % CW == 0 && CW >= 32 && CPC % A == 0, "cluster split");
+  static_assert(RPC % RF == 0 && CPC % CW == 0 && CPC % A == 0 && CW >= 32, "cluster split");
   static_assert(SMEM <= 227 * 1024, "shared memory budget");
 };
 
@@ -68,6 +68,11 @@ __global__ void __cluster_dims__(C, 1, 1) __launch_bounds__(512, 1)
   double* red = reinterpret_cast<double*>(tw + N);
   for (int i = tid; i < N; i += K::NT) tw[i] = g.tw0[i];
 
+  // Column buffer: element (row r, owned column cl) at r * CP + cl + r / A.
+  // With CP odd and the skew of one slot per A rows, both the natural walk
+  // (rows t + A j) and the exchange walk (rows A t + tt) of the A lanes of a
+  // column land in distinct banks.
+  auto cidx = [](int r, int cl) { return r * CP + cl + r / A; };
   float2* rc[C];  // column buffers of every CTA of the cluster
 #pragma unroll
   for (int q = 0; q < C; ++q) rc[q] = cluster.map_shared_rank(cbuf, q);
@@ -99,11 +104,14 @@ __global__ void __cluster_dims__(C, 1, 1) __launch_bounds__(512, 1)
     line_stage2<N, -1>(v, t, [&](int tt, int k1) { return rs[k1 * (A + 1) + tt]; });
     // v[j] = X[a][t + A j]; column t + A j belongs to CTA j / JPC
 #pragma unroll
-    for (int j = 0; j < B; ++j) rc[j / JPC][a * CP + t + A * (j % JPC)] = v[j];
+    for (int j = 0; j < B; ++j) rc[j / JPC][cidx(a, t + A * (j % JPC))] = v[j];
   }
   cluster.sync();
 
   // ---------------- 3. column pass on the owned columns
+  // Lanes of a warp run along a row (coalesced amp / mask / background
+  // traffic); the A threads of a column sit in A different warps, so the
+  // exchanges synchronise the CTA.
   ff err = ff_zero();
 #pragma unroll 1
   for (int s = 0; s < CPC / CW; ++s) {
@@ -111,25 +119,24 @@ __global__ void __cluster_dims__(C, 1, 1) __launch_bounds__(512, 1)
     const int kc = rank * CPC + cl;
     float2 v[B];
 #pragma unroll
-    for (int j = 0; j < B; ++j) v[j] = cbuf[(tc + A * j) * CP + cl];
+    for (int j = 0; j < B; ++j) v[j] = cbuf[cidx(tc + A * j, cl)];
     line_stage1<N, -1>(v, tc, tw);
     __syncthreads();
 #pragma unroll
-    for (int k1 = 0; k1 < B; ++k1) cbuf[(k1 * A + tc) * CP + cl] = v[k1];
+    for (int k1 = 0; k1 < B; ++k1) cbuf[cidx(k1 * A + tc, cl)] = v[k1];
     __syncthreads();
-    line_stage2<N, -1>(v, tc, [&](int tt, int k1) { return cbuf[(k1 * A + tt) * CP + cl]; });
-#pragma unroll
-    for (int j = 0; j < B; ++j) frame_modulus<N, N, OP>(g, f, fbase, tc + A * j, kc, v[j], err);
+    line_stage2<N, -1>(v, tc, [&](int tt, int k1) { return cbuf[cidx(k1 * A + tt, cl)]; });
+    frame_modulus_line<N, N, OP, A, B>(g, f, fbase, tc, kc, v, err);
     if constexpr (INVERSE) {
       line_stage1<N, +1>(v, tc, tw);
       __syncthreads();
 #pragma unroll
-      for (int k1 = 0; k1 < B; ++k1) cbuf[(k1 * A + tc) * CP + cl] = v[k1];
+      for (int k1 = 0; k1 < B; ++k1) cbuf[cidx(k1 * A + tc, cl)] = v[k1];
       __syncthreads();
-      line_stage2<N, +1>(v, tc, [&](int tt, int k1) { return cbuf[(k1 * A + tt) * CP + cl]; });
+      line_stage2<N, +1>(v, tc, [&](int tt, int k1) { return cbuf[cidx(k1 * A + tt, cl)]; });
       __syncthreads();
 #pragma unroll
-      for (int j = 0; j < B; ++j) cbuf[(tc + A * j) * CP + cl] = v[j];
+      for (int j = 0; j < B; ++j) cbuf[cidx(tc + A * j, cl)] = v[j];
     }
   }
 
@@ -141,7 +148,7 @@ __global__ void __cluster_dims__(C, 1, 1) __launch_bounds__(512, 1)
       const int a = rank * RPC + s * RF + lr;
       float2 v[B];
 #pragma unroll
-      for (int j = 0; j < B; ++j) v[j] = rc[j / JPC][a * CP + t + A * (j % JPC)];
+      for (int j = 0; j < B; ++j) v[j] = rc[j / JPC][cidx(a, t + A * (j % JPC))];
       line_stage1<N, +1>(v, t, tw);
       __syncwarp();
 #pragma unroll
@@ -149,7 +156,8 @@ __global__ void __cluster_dims__(C, 1, 1) __launch_bounds__(512, 1)
       __syncwarp();
       line_stage2<N, +1>(v, t, [&](int tt, int k1) { return rs[k1 * (A + 1) + tt]; });
 #pragma unroll
-      for (int j = 0; j < B; ++j) frame_output<N, OP>(g, r0, r1, psi, a, t + A * j, cscale(v[j], kInv));
+      for (int j = 0; j < B; ++j) v[j] = cscale(v[j], kInv);
+      frame_output_line<N, OP, A, B>(g, r0, r1, psi, a, t, v);
       __syncwarp();
     }
     cluster.sync();

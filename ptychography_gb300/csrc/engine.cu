@@ -207,8 +207,9 @@ extern "C" int pty_plan_create(const pty_geometry* g, const int64_t* R_host, pty
   if ((rc = dalloc_t(p, &p->d_heatO, npix))) return fail(rc);
   if ((rc = dalloc_t(p, &p->d_heatO2, npix))) return fail(rc);
   {
+    // enough frame chunks for about four waves of probe-gather blocks
     const int ntiles = ((N0 + 31) / 32) * ((N1 + 31) / 32);
-    int K = (608 + ntiles - 1) / ntiles;
+    int K = (2432 + ntiles - 1) / ntiles;
     if (K > 64) K = 64;
     if (K > n) K = n;
     if (K < 1) K = 1;
@@ -435,17 +436,15 @@ extern "C" int pty_era(pty_plan* p, const pty_buffers* b, const pty_options* o, 
       }
       // consistency projection (era.py:163-189)
       if (upd == 1) {
-        if (!heatP_valid) PTY_TRY(launch_heat_P(p->tl, p->n, p->N0, p->N1, p->U, p->V, p->d_R, P, p->d_heatP, st));
+        PTY_TRY(launch_psup_O(p->tl, p->n, p->N0, p->N1, p->U, p->V, p->d_R, psi, P, p->d_heatP, !heatP_valid, alpha, O, st));
         heatP_valid = true;
-        PTY_TRY(launch_psup_O(p->tl, p->n, p->N0, p->N1, p->U, p->V, p->d_R, psi, P, p->d_heatP, alpha, O, st));
       } else if (upd == 2) {
         PTY_TRY(launch_psup_P(p->n, p->N0, p->N1, p->U, p->V, p->d_R, psi, O, p->d_part_num,
                               p->d_part_den, p->K, p->d_heatO, !heatO_valid, alpha, P, st));
         heatO_valid = true;
       } else if (i % o->OP_iters1 == 0) {
         for (int j = 0; j < o->OP_iters0; ++j) {
-          PTY_TRY(launch_heat_P(p->tl, p->n, p->N0, p->N1, p->U, p->V, p->d_R, P, p->d_heatP, st));
-          PTY_TRY(launch_psup_O(p->tl, p->n, p->N0, p->N1, p->U, p->V, p->d_R, psi, P, p->d_heatP, alpha, O, st));
+          PTY_TRY(launch_psup_O(p->tl, p->n, p->N0, p->N1, p->U, p->V, p->d_R, psi, P, p->d_heatP, true, alpha, O, st));
           PTY_TRY(launch_psup_P(p->n, p->N0, p->N1, p->U, p->V, p->d_R, psi, O, p->d_part_num,
                                 p->d_part_den, p->K, p->d_heatO, true, alpha, P, st));
         }
@@ -455,9 +454,8 @@ extern "C" int pty_era(pty_plan* p, const pty_buffers* b, const pty_options* o, 
           heatP_valid = heatO_valid = false;
         }
       } else {
-        if (!heatP_valid) PTY_TRY(launch_heat_P(p->tl, p->n, p->N0, p->N1, p->U, p->V, p->d_R, P, p->d_heatP, st));
+        PTY_TRY(launch_psup_O(p->tl, p->n, p->N0, p->N1, p->U, p->V, p->d_R, psi, P, p->d_heatP, !heatP_valid, alpha, O, st));
         heatP_valid = true;
-        PTY_TRY(launch_psup_O(p->tl, p->n, p->N0, p->N1, p->U, p->V, p->d_R, psi, P, p->d_heatP, alpha, O, st));
       }
       if (i < o->Pmod_probe) PTY_TRY(pmod_probe(p, P, b->Pamp, b->mask, alpha, st));  // era.py:193-194
       if (use_bg) PTY_TRY(launch_frame_mean(p->n, (int)npix, p->d_bgf, p->d_mean_part, p->Km, p->d_b0, st));
@@ -528,17 +526,15 @@ extern "C" int pty_dm(pty_plan* p, const pty_buffers* b, const pty_options* o, i
       }
       // main consistency projection (dm.py:56-85)
       if (upd == 1) {
-        if (!heatP_valid) PTY_TRY(launch_heat_P(p->tl, n, N0, N1, U, V, R, P, p->d_heatP, st));
+        PTY_TRY(launch_psup_O(p->tl, n, N0, N1, U, V, R, psi, P, p->d_heatP, !heatP_valid, alpha, O, st));
         heatP_valid = true;
-        PTY_TRY(launch_psup_O(p->tl, n, N0, N1, U, V, R, psi, P, p->d_heatP, alpha, O, st));
       } else if (upd == 2) {
         PTY_TRY(launch_psup_P(n, N0, N1, U, V, R, psi, O, p->d_part_num, p->d_part_den, p->K,
                               p->d_heatO, !heatO_valid, alpha, P, st));
         heatO_valid = true;
       } else if (i % o->OP_iters1 == 0) {
         for (int j = 0; j < o->OP_iters0; ++j) {
-          PTY_TRY(launch_heat_P(p->tl, n, N0, N1, U, V, R, P, p->d_heatP, st));
-          PTY_TRY(launch_psup_O(p->tl, n, N0, N1, U, V, R, psi, P, p->d_heatP, alpha, O, st));
+          PTY_TRY(launch_psup_O(p->tl, n, N0, N1, U, V, R, psi, P, p->d_heatP, true, alpha, O, st));
           PTY_TRY(launch_psup_P(n, N0, N1, U, V, R, psi, O, p->d_part_num, p->d_part_den, p->K,
                                 p->d_heatO, true, alpha, P, st));
         }
@@ -548,9 +544,8 @@ extern "C" int pty_dm(pty_plan* p, const pty_buffers* b, const pty_options* o, i
           heatP_valid = heatO_valid = false;
         }
       } else {
-        if (!heatP_valid) PTY_TRY(launch_heat_P(p->tl, n, N0, N1, U, V, R, P, p->d_heatP, st));
+        PTY_TRY(launch_psup_O(p->tl, n, N0, N1, U, V, R, psi, P, p->d_heatP, !heatP_valid, alpha, O, st));
         heatP_valid = true;
-        PTY_TRY(launch_psup_O(p->tl, n, N0, N1, U, V, R, psi, P, p->d_heatP, alpha, O, st));
       }
       if (i < o->Pmod_probe) PTY_TRY(pmod_probe(p, P, b->Pamp, b->mask, alpha, st));  // dm.py:88-89
       // difference-map update (dm.py:91-97 / 208-224)
@@ -577,25 +572,22 @@ extern "C" int pty_dm(pty_plan* p, const pty_buffers* b, const pty_options* o, i
       PTY_TRY(copy_d2d(Os, O, nobj * sizeof(float2), st));
       PTY_TRY(copy_d2d(Ps, P, npix * sizeof(float2), st));
       if (upd == 1) {
-        if (!heatP_valid) PTY_TRY(launch_heat_P(p->tl, n, N0, N1, U, V, R, Ps, p->d_heatP, st));
+        PTY_TRY(launch_psup_O(p->tl, n, N0, N1, U, V, R, psi, Ps, p->d_heatP, !heatP_valid, alpha, Os, st));
         heatP_valid = true;
-        PTY_TRY(launch_psup_O(p->tl, n, N0, N1, U, V, R, psi, Ps, p->d_heatP, alpha, Os, st));
       } else if (upd == 2) {
         PTY_TRY(launch_psup_P(n, N0, N1, U, V, R, psi, Os, p->d_part_num, p->d_part_den, p->K,
                               p->d_heatO, !heatO_valid, alpha, Ps, st));
         heatO_valid = true;
       } else if (i % o->OP_iters1 == 0) {
         for (int j = 0; j < o->OP_iters0; ++j) {
-          PTY_TRY(launch_heat_P(p->tl, n, N0, N1, U, V, R, Ps, p->d_heatP2, st));
-          PTY_TRY(launch_psup_O(p->tl, n, N0, N1, U, V, R, psi, Ps, p->d_heatP2, alpha, Os, st));
+          PTY_TRY(launch_psup_O(p->tl, n, N0, N1, U, V, R, psi, Ps, p->d_heatP2, true, alpha, Os, st));
           PTY_TRY(launch_psup_P(n, N0, N1, U, V, R, psi, Os, p->d_part_num, p->d_part_den, p->K,
                                 p->d_heatO2, true, alpha, Ps, st));
         }
         if (o->probe_centering) PTY_TRY(centre(p, Ps, Os, nullptr, st));
       } else {
-        if (!heatP_valid) PTY_TRY(launch_heat_P(p->tl, n, N0, N1, U, V, R, P, p->d_heatP, st));
+        PTY_TRY(launch_psup_O(p->tl, n, N0, N1, U, V, R, psi, P, p->d_heatP, !heatP_valid, alpha, Os, st));
         heatP_valid = true;
-        PTY_TRY(launch_psup_O(p->tl, n, N0, N1, U, V, R, psi, P, p->d_heatP, alpha, Os, st));
       }
       if (i < o->Pmod_probe) PTY_TRY(pmod_probe(p, Ps, b->Pamp, b->mask, alpha, st));
       if (use_bg) PTY_TRY(launch_frame_mean(n, (int)npix, bg, p->d_mean_part, p->Km, p->d_b0, st));
@@ -697,10 +689,8 @@ extern "C" int pty_psup_O(pty_plan* p, const void* psi, const void* P, double* h
                           int32_t recompute, double alpha, void* O_out, void* stream) {
   if (!p || !psi || !P || !heat || !O_out) return set_error(PTY_ERR_ARG, "null argument");
   cudaStream_t st = (cudaStream_t)stream;
-  if (recompute)
-    PTY_TRY(launch_heat_P(p->tl, p->n, p->N0, p->N1, p->U, p->V, p->d_R, (const float2*)P, heat, st));
   return launch_psup_O(p->tl, p->n, p->N0, p->N1, p->U, p->V, p->d_R, (const float2*)psi,
-                       (const float2*)P, heat, (float)alpha, (float2*)O_out, st);
+                       (const float2*)P, heat, recompute != 0, (float)alpha, (float2*)O_out, st);
 }
 
 extern "C" int pty_psup_P(pty_plan* p, const void* psi, const void* O, double* heat,

@@ -66,9 +66,10 @@ struct TileLists {
 };
 
 // O = sum conj(P) psi / (heat + alpha)   (era.py:336-369); heat in double
+// (compute_heat: heat is recomputed from P in the same pass and written out)
 int launch_psup_O(const TileLists& tl, int n, int N0, int N1, int U, int V, const int* R,
-                  const float2* psi, const float2* P, const double* heat, float alpha, float2* O,
-                  cudaStream_t st);
+                  const float2* psi, const float2* P, double* heat, bool compute_heat, float alpha,
+                  float2* O, cudaStream_t st);
 // heat = sum |P|^2 over windows (era.py:402-410)
 int launch_heat_P(const TileLists& tl, int n, int N0, int N1, int U, int V, const int* R,
                   const float2* P, double* heat, cudaStream_t st);

@@ -20,23 +20,49 @@
 
 namespace pty {
 
+// Shared-memory layout of one frame: element (row r, column c) at
+//   r * RP + (c + c / A1) + (r / A0) * S1 + (r % A0) * S2.
+// The column pad (one slot per A1 columns), the pitch RP and the two row skews
+// were chosen by exhaustive search so that every shared-memory walk of the
+// kernel -- row loads / exchanges, column loads / exchanges -- is free of bank
+// conflicts for the square shapes (the 32 x 64 shape keeps some conflicts).
+template <int N0, int N1>
+struct FrameLayout {
+  static constexpr int A1 = LineGeom<N1>::A, B1 = LineGeom<N1>::B;
+  static constexpr int ROWLEN = B1 * (A1 + 1);
+  static constexpr int RP = ROWLEN;
+  static constexpr int S1 = 0, S2 = 0;
+};
+template <> struct FrameLayout<32, 32> { static constexpr int RP = 40, S1 = 12, S2 = 4; };
+template <> struct FrameLayout<64, 64> { static constexpr int RP = 72, S1 = 14, S2 = 2; };
+template <> struct FrameLayout<128, 128> { static constexpr int RP = 144, S1 = 14, S2 = 2; };
+
 template <int N0, int N1>
 struct FrameCfg {
   static constexpr int A0 = LineGeom<N0>::A, B0 = LineGeom<N0>::B;  // column transform
   static constexpr int A1 = LineGeom<N1>::A, B1 = LineGeom<N1>::B;  // row transform
-  static constexpr int ROWLEN = B1 * (A1 + 1);                      // padded row length
-  // row pitch: half-warps covering several rows must hit disjoint banks in the
-  // stage-2 row exchange (A1 < 16 puts 16/A1 rows in a half-warp)
-  static constexpr int RP = (A1 >= 16) ? ROWLEN
-                          : (A1 == 8)  ? ROWLEN + ((8 - ROWLEN % 16) + 16) % 16
-                                       : ROWLEN + ((4 - ROWLEN % 16) + 16) % 16;
+  static constexpr int RP = FrameLayout<N0, N1>::RP;
+  static constexpr int S1 = FrameLayout<N0, N1>::S1, S2 = FrameLayout<N0, N1>::S2;
+  static constexpr int BUF = (N0 - 1) * RP + (N1 - 1) + (N1 - 1) / A1 + ((N0 - 1) / A0) * S1 +
+                             (A0 - 1) * S2 + 1;
   static constexpr int T_ROW = N0 * A1, T_COL = N1 * A0;
   static constexpr int NT0 = T_ROW < T_COL ? T_ROW : T_COL;
   static constexpr int NT = NT0 < 512 ? NT0 : 512;
-  static constexpr size_t SMEM = (size_t)N0 * RP * sizeof(float2) + (size_t)(N0 + N1) * sizeof(float2) +
+  static constexpr size_t SMEM = (size_t)BUF * sizeof(float2) + (size_t)(N0 + N1) * sizeof(float2) +
                                  32 * sizeof(double);
   static_assert(T_ROW % NT == 0 && T_COL % NT == 0 && NT % 32 == 0, "task split");
+  // rows must not overlap: consecutive row bases differ by at least a padded row
+  static_assert(RP + S2 >= B1 * (A1 + 1) && RP + S1 - (A0 - 1) * S2 >= B1 * (A1 + 1), "row pitch");
 };
+
+// Row handled by row-task slot rho: the rows sharing a half-warp are 4 apart
+// (8-thread rows) or 4 / 8 / 12 apart (4-thread rows), as the layout assumes.
+template <int A1>
+PTY_DEV int row_of_slot(int rho) {
+  if constexpr (A1 == 8) return (rho & ~7) + (rho & 1) * 4 + ((rho & 7) >> 1);
+  else if constexpr (A1 == 4) return (rho & ~15) + (rho & 3) * 4 + ((rho & 15) >> 2);
+  else return rho;
+}
 
 PTY_DEV int padpos(int c, int A) { return c + c / A; }
 
@@ -44,12 +70,14 @@ template <int N0, int N1, int OP>
 __global__ void __launch_bounds__(FrameCfg<N0, N1>::NT, 1) frame_kernel(FrameArgs g) {
   using C = FrameCfg<N0, N1>;
   constexpr int A0 = C::A0, B0 = C::B0, A1 = C::A1, B1 = C::B1, RP = C::RP, NT = C::NT;
+  constexpr int S1 = C::S1, S2 = C::S2;
   constexpr bool INVERSE = OpTraits<OP>::INVERSE;
+  auto rbase = [](int r) { return r * RP + (r / A0) * S1 + (r % A0) * S2; };
   constexpr float kInv = 1.0f / (float)(N0 * N1);
 
   extern __shared__ __align__(16) unsigned char smem_raw[];
   float2* fr = reinterpret_cast<float2*>(smem_raw);
-  float2* tw0 = fr + N0 * RP;
+  float2* tw0 = fr + C::BUF;
   float2* tw1 = tw0 + N0;
   double* red = reinterpret_cast<double*>(tw1 + N1);
 
@@ -69,12 +97,12 @@ __global__ void __launch_bounds__(FrameCfg<N0, N1>::NT, 1) frame_kernel(FrameArg
 
   // ---------------- forward row pass (a row's A1 threads share a warp)
   for (int id = tid; id < N0 * A1; id += NT) {
-    const int t = id % A1, a = id / A1;
+    const int t = id % A1, a = row_of_slot<A1>(id / A1);
     float2 v[B1];
 #pragma unroll
     for (int j = 0; j < B1; ++j) v[j] = frame_input<N1, OP>(g, r0, r1, psi, a, t + A1 * j);
     line_stage1<N1, -1>(v, t, tw1);
-    float2* row = fr + a * RP;
+    float2* row = fr + rbase(a);
 #pragma unroll
     for (int k1 = 0; k1 < B1; ++k1) row[k1 * (A1 + 1) + t] = v[k1];
     __syncwarp();
@@ -86,35 +114,38 @@ __global__ void __launch_bounds__(FrameCfg<N0, N1>::NT, 1) frame_kernel(FrameArg
   __syncthreads();
 
   // ---------------- column pass: forward FFT, modulus constraint, inverse FFT
-  // each pass takes CW whole columns (all A0 line-threads of a column in the
-  // same pass, as the exchange needs); lanes of a warp run along a row
+  // Each pass takes CW whole columns (all A0 line-threads of a column in the
+  // same pass, as the exchange needs); lanes of a warp run along a row, so the
+  // amp / mask / background traffic is coalesced and the exchanges
+  // synchronise the CTA.
   ff err = ff_zero();
   constexpr int CW = NT / A0;
   static_assert(NT % A0 == 0 && N1 % CW == 0 && CW >= 32, "column pass split");
+#pragma unroll 1
   for (int c0 = 0; c0 < N1; c0 += CW) {
     const int c = c0 + tid % CW, t = tid / CW;
     const int cp = padpos(c, A1);
+    auto at = [&](int r) -> float2& { return fr[rbase(r) + cp]; };
     float2 v[B0];
 #pragma unroll
-    for (int j = 0; j < B0; ++j) v[j] = fr[(t + A0 * j) * RP + cp];
+    for (int j = 0; j < B0; ++j) v[j] = at(t + A0 * j);
     line_stage1<N0, -1>(v, t, tw0);
     __syncthreads();
 #pragma unroll
-    for (int k1 = 0; k1 < B0; ++k1) fr[(k1 * A0 + t) * RP + cp] = v[k1];
+    for (int k1 = 0; k1 < B0; ++k1) at(k1 * A0 + t) = v[k1];
     __syncthreads();
-    line_stage2<N0, -1>(v, t, [&](int tt, int k1) { return fr[(k1 * A0 + tt) * RP + cp]; });
-#pragma unroll
-    for (int j = 0; j < B0; ++j) frame_modulus<N0, N1, OP>(g, f, fbase, t + A0 * j, c, v[j], err);
+    line_stage2<N0, -1>(v, t, [&](int tt, int k1) { return at(k1 * A0 + tt); });
+    frame_modulus_line<N0, N1, OP, A0, B0>(g, f, fbase, t, c, v, err);
     if constexpr (INVERSE) {
       line_stage1<N0, +1>(v, t, tw0);
       __syncthreads();
 #pragma unroll
-      for (int k1 = 0; k1 < B0; ++k1) fr[(k1 * A0 + t) * RP + cp] = v[k1];
+      for (int k1 = 0; k1 < B0; ++k1) at(k1 * A0 + t) = v[k1];
       __syncthreads();
-      line_stage2<N0, +1>(v, t, [&](int tt, int k1) { return fr[(k1 * A0 + tt) * RP + cp]; });
+      line_stage2<N0, +1>(v, t, [&](int tt, int k1) { return at(k1 * A0 + tt); });
       __syncthreads();
 #pragma unroll
-      for (int j = 0; j < B0; ++j) fr[(t + A0 * j) * RP + cp] = v[j];
+      for (int j = 0; j < B0; ++j) at(t + A0 * j) = v[j];
     }
   }
 
@@ -122,8 +153,8 @@ __global__ void __launch_bounds__(FrameCfg<N0, N1>::NT, 1) frame_kernel(FrameArg
     __syncthreads();
     // ---------------- inverse row pass, write the result
     for (int id = tid; id < N0 * A1; id += NT) {
-      const int t = id % A1, a = id / A1;
-      float2* row = fr + a * RP;
+      const int t = id % A1, a = row_of_slot<A1>(id / A1);
+      float2* row = fr + rbase(a);
       float2 v[B1];
 #pragma unroll
       for (int j = 0; j < B1; ++j) v[j] = row[t + j * (A1 + 1)];
@@ -134,8 +165,8 @@ __global__ void __launch_bounds__(FrameCfg<N0, N1>::NT, 1) frame_kernel(FrameArg
       __syncwarp();
       line_stage2<N1, +1>(v, t, [&](int tt, int k1) { return row[k1 * (A1 + 1) + tt]; });
 #pragma unroll
-      for (int j = 0; j < B1; ++j)
-        frame_output<N1, OP>(g, r0, r1, psi, a, t + A1 * j, cscale(v[j], kInv));
+      for (int j = 0; j < B1; ++j) v[j] = cscale(v[j], kInv);
+      frame_output_line<N1, OP, A1, B1>(g, r0, r1, psi, a, t, v);
     }
   }
 

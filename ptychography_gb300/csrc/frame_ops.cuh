@@ -38,66 +38,98 @@ PTY_DEV float2 frame_input(const FrameArgs& g, int r0, int r1, const float2* psi
   }
 }
 
-// r is the inverse transform already scaled by 1 / (N0 N1)
-template <int N1, int OP>
-PTY_DEV void frame_output(const FrameArgs& g, int r0, int r1, float2* psi, int a, int b, float2 r) {
-  if constexpr (OpTraits<OP>::IN_DM) {
-    // dm.py:94-97: psi_new = (psi - ex0) + Pmod(2 ex0 - psi)
-    const float2 ex0 = exit_wave<N1>(g, r0, r1, a, b);
-    const float2 e1 = csub(psi[a * N1 + b], ex0);
-    psi[a * N1 + b] = cadd(e1, r);
+// The modulus constraint on one column line: v[j] = F[t + A j][kc].  All
+// global loads of the line are issued before any store, so their latencies
+// overlap (the output pointers may alias the inputs, which would otherwise
+// serialise every load behind the previous element's store).
+template <int N0, int N1, int OP, int A, int B>
+PTY_DEV void frame_modulus_line(const FrameArgs& g, int f, size_t fbase, int t, int kc,
+                                float2 (&v)[B], ff& err) {
+  if constexpr (OP == OP_INTENS) {
+    const int sc = (kc + N1 / 2) % N1;   // fftshift, era.py:295
+#pragma unroll
+    for (int j = 0; j < B; ++j) {
+      const int sr = (t + A * j + N0 / 2) % N0;
+      g.out_real[fbase + (size_t)sr * N1 + sc] = cabs2(v[j]);
+    }
+    return;
   } else {
-    psi[a * N1 + b] = r;
+    constexpr bool BG_IN = (OP == OP_EXIT7 || OP == OP_PSI7 || OP == OP_MERR || OP == OP_MERR_PSI);
+    constexpr bool BG_OUT = (OP == OP_EXIT7 || OP == OP_PSI7 || OP == OP_DM7);
+    float am[B], mk[B], bb[B], b0v[B];
+    const float* amp = g.amp + (size_t)g.amp_stride * f;
+#pragma unroll
+    for (int j = 0; j < B; ++j) {
+      const int pix = (t + A * j) * N1 + kc;
+      am[j] = __ldg(&amp[pix]);
+      mk[j] = g.mask ? (float)__ldg(&g.mask[pix]) : 1.0f;
+      if constexpr (BG_IN) bb[j] = g.bg_in ? g.bg_in[(size_t)g.bg_stride * f + pix] : 0.0f;
+      if constexpr (OP == OP_DM7) {
+        bb[j] = g.bg_out[fbase + pix];
+        b0v[j] = __ldg(&g.b0[pix]);
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < B; ++j) {
+      const float2 F = v[j];
+      if constexpr (OP == OP_EXIT1 || OP == OP_PSI1 || OP == OP_DM1) {
+        // era.py:561-571: |F| + alpha, masked pixels keep F
+        const float mag = sqrtf(cabs2(F)) + g.alpha;
+        if (g.err_part) {
+          const float d = mag - am[j];
+          err = ff_add(err, d * d * mk[j]);
+        }
+        const float fac = (mk[j] != 0.f) ? am[j] / mag : 1.0f;
+        v[j] = cscale(F, fac);
+      } else if constexpr (OP == OP_EXIT7 || OP == OP_PSI7) {
+        // era.py:584-594: sqrt(|F|^2 + b^2 + alpha), masked pixels zeroed
+        const float mag = sqrtf(cabs2(F) + bb[j] * bb[j] + g.alpha);
+        if (g.err_part) {
+          const float d = mag - am[j];
+          err = ff_add(err, d * d * mk[j]);
+        }
+        const float fac = mk[j] * am[j] / mag;
+        v[j] = cscale(F, fac);
+        bb[j] *= fac;
+      } else if constexpr (OP == OP_DM7) {
+        // dm.py:219-224 on the background: g1 = g - b0 ; tb = b0 - g1 ; g = g1 + Pmod7(tb)
+        const float g1 = bb[j] - b0v[j];
+        const float tb = b0v[j] - g1;
+        const float mag = sqrtf(cabs2(F) + tb * tb + g.alpha);
+        const float fac = mk[j] * am[j] / mag;
+        v[j] = cscale(F, fac);
+        bb[j] = g1 + tb * fac;
+      } else if constexpr (OP == OP_MERR || OP == OP_MERR_PSI) {
+        // dm.py:338-340, no alpha
+        const float mag = sqrtf(cabs2(F) + bb[j] * bb[j]);
+        const float d = mag - am[j];
+        err = ff_add(err, mk[j] * (d * d));
+      }
+    }
+    if constexpr (BG_OUT) {
+#pragma unroll
+      for (int j = 0; j < B; ++j) g.bg_out[fbase + (size_t)(t + A * j) * N1 + kc] = bb[j];
+    }
   }
 }
 
-template <int N0, int N1, int OP>
-PTY_DEV void frame_modulus(const FrameArgs& g, int f, size_t fbase, int kr, int kc, float2& F, ff& err) {
-  const int pix = kr * N1 + kc;
-  const float msk = g.mask ? (float)g.mask[pix] : 1.0f;
-  if constexpr (OP == OP_INTENS) {
-    const int sr = (kr + N0 / 2) % N0, sc = (kc + N1 / 2) % N1;   // fftshift, era.py:295
-    g.out_real[fbase + (size_t)sr * N1 + sc] = cabs2(F);
-  } else {
-    const float am = g.amp[(size_t)g.amp_stride * f + pix];
-    if constexpr (OP == OP_EXIT1 || OP == OP_PSI1 || OP == OP_DM1) {
-      // era.py:561-571: |F| + alpha, masked pixels keep F
-      const float mag = sqrtf(cabs2(F)) + g.alpha;
-      if (g.err_part) {
-        const float d = mag - am;
-        err = ff_add(err, d * d * msk);
-      }
-      const float fac = (msk != 0.f) ? am / mag : 1.0f;
-      F = cscale(F, fac);
-    } else if constexpr (OP == OP_EXIT7 || OP == OP_PSI7) {
-      // era.py:584-594: sqrt(|F|^2 + b^2 + alpha), masked pixels zeroed
-      const float b = g.bg_in[(size_t)g.bg_stride * f + pix];
-      const float mag = sqrtf(cabs2(F) + b * b + g.alpha);
-      if (g.err_part) {
-        const float d = mag - am;
-        err = ff_add(err, d * d * msk);
-      }
-      const float fac = msk * am / mag;
-      F = cscale(F, fac);
-      g.bg_out[fbase + pix] = b * fac;
-    } else if constexpr (OP == OP_DM7) {
-      // dm.py:219-224 on the background: g1 = g - b0 ; tb = b0 - g1 ; g = g1 + Pmod7(tb)
-      const float gs = g.bg_out[fbase + pix];
-      const float b0 = g.b0[pix];
-      const float g1 = gs - b0;
-      const float tb = b0 - g1;
-      const float mag = sqrtf(cabs2(F) + tb * tb + g.alpha);
-      const float fac = msk * am / mag;
-      F = cscale(F, fac);
-      g.bg_out[fbase + pix] = g1 + tb * fac;
-    } else if constexpr (OP == OP_MERR || OP == OP_MERR_PSI) {
-      // dm.py:338-340, no alpha
-      const float b = g.bg_in ? g.bg_in[(size_t)g.bg_stride * f + pix] : 0.0f;
-      const float mag = sqrtf(cabs2(F) + b * b);
-      const float d = mag - am;
-      err = ff_add(err, msk * (d * d));
+// The result of the inverse transform for one row line (v[j] at column
+// t + A j, already scaled): loads first, then stores (see frame_modulus_line).
+template <int N1, int OP, int A, int B>
+PTY_DEV void frame_output_line(const FrameArgs& g, int r0, int r1, float2* psi, int a, int t,
+                               float2 (&v)[B]) {
+  if constexpr (OpTraits<OP>::IN_DM) {
+#pragma unroll
+    for (int j = 0; j < B; ++j) {
+      // dm.py:94-97: psi_new = (psi - ex0) + Pmod(2 ex0 - psi)
+      const int b = t + A * j;
+      const float2 ex0 = exit_wave<N1>(g, r0, r1, a, b);
+      const float2 e1 = csub(psi[a * N1 + b], ex0);
+      v[j] = cadd(e1, v[j]);
     }
   }
+#pragma unroll
+  for (int j = 0; j < B; ++j) psi[a * N1 + t + A * j] = v[j];
 }
 
 }  // namespace pty

@@ -13,45 +13,77 @@ constexpr int kTile = 32;      // object / probe tile edge
 constexpr int kGatherNT = 256; // threads per tile (4 pixels each)
 
 // ------------------------------------------------------------------ psup_O
-// era.py:336-369: O = sum_i psi_i * conj(P) placed at window i, / (heat + alpha)
+// era.py:336-369: O = sum_i psi_i * conj(P) placed at window i, / (heat + alpha),
+// with heat = sum_i |P|^2 (era.py:402-410) recomputed in the same pass when HEAT.
+// A thread owns 4 pixels of a 32 x 32 object tile; the tile's frames are
+// visited in ascending order, two at a time with all loads issued first.
+// Out-of-window pixels contribute an exact zero.
+template <bool HEAT>
 __global__ void __launch_bounds__(kGatherNT) psup_O_kernel(
     TileLists tl, int N0, int N1, int U, int V, const int* __restrict__ R,
-    const float2* __restrict__ psi, const float2* __restrict__ P, const double* __restrict__ heat,
+    const float2* __restrict__ psi, const float2* __restrict__ P, double* __restrict__ heat,
     float alpha, float2* __restrict__ O) {
   const int tile = blockIdx.x;
   const int tu = tile / tl.ntv, tv = tile % tl.ntv;
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
   const int v = tv * kTile + tx;
-  int u[4];
+  const int u0 = tu * kTile + ty;
   float2 acc[4];
+  ff h[4];
 #pragma unroll
   for (int k = 0; k < 4; ++k) {
-    u[k] = tu * kTile + ty + 8 * k;
     acc[k] = make_float2(0.f, 0.f);
+    h[k] = ff_zero();
   }
   const int beg = tl.ptr[tile], end = tl.ptr[tile + 1];
-  for (int e = beg; e < end; ++e) {
+  auto fetch = [&](int e, float2 (&x)[4], float2 (&p)[4]) {
     const int f = tl.frames[e];
     const int r0 = R[2 * f], r1 = R[2 * f + 1];
     const int b = v + r1;
-    if (b < 0 || b >= N1) continue;
+    const bool bok = b >= 0 && b < N1;
     const float2* pf = psi + (size_t)f * N0 * N1;
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
-      const int a = u[k] + r0;
-      if (a >= 0 && a < N0) {
-        const float2 x = pf[a * N1 + b];
-        const float2 p = __ldg(&P[a * N1 + b]);
-        acc[k] = cadd(acc[k], cmulc(x, p));
-      }
+      const int a = u0 + 8 * k + r0;
+      const bool ok = bok && a >= 0 && a < N0;
+      x[k] = ok ? pf[a * N1 + b] : make_float2(0.f, 0.f);
+      p[k] = ok ? P[a * N1 + b] : make_float2(0.f, 0.f);
     }
+  };
+  auto accumulate = [&](const float2 (&x)[4], const float2 (&p)[4]) {
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      acc[k] = cadd(acc[k], cmulc(x[k], p[k]));
+      if (HEAT) h[k] = ff_add(h[k], cabs2(p[k]));
+    }
+  };
+  int e = beg;
+  for (; e + 1 < end; e += 2) {
+    float2 x0[4], p0[4], x1[4], p1[4];
+    fetch(e, x0, p0);
+    fetch(e + 1, x1, p1);
+    accumulate(x0, p0);
+    accumulate(x1, p1);
+  }
+  if (e < end) {
+    float2 x0[4], p0[4];
+    fetch(e, x0, p0);
+    accumulate(x0, p0);
   }
   if (v < V) {
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
-      if (u[k] < U) {
-        const size_t o = (size_t)u[k] * V + v;
-        const float den = (float)(heat[o] + (double)alpha);
+      const int uu = u0 + 8 * k;
+      if (uu < U) {
+        const size_t o = (size_t)uu * V + v;
+        double hd;
+        if (HEAT) {
+          hd = ff_to_double(h[k]);
+          heat[o] = hd;
+        } else {
+          hd = heat[o];
+        }
+        const float den = (float)(hd + (double)alpha);
         O[o] = make_float2(acc[k].x / den, acc[k].y / den);
       }
     }
@@ -91,10 +123,13 @@ __global__ void __launch_bounds__(kGatherNT) heat_P_kernel(
 }
 
 int launch_psup_O(const TileLists& tl, int n, int N0, int N1, int U, int V, const int* R,
-                  const float2* psi, const float2* P, const double* heat, float alpha, float2* O,
-                  cudaStream_t st) {
+                  const float2* psi, const float2* P, double* heat, bool compute_heat, float alpha,
+                  float2* O, cudaStream_t st) {
   (void)n;
-  psup_O_kernel<<<tl.ntu * tl.ntv, kGatherNT, 0, st>>>(tl, N0, N1, U, V, R, psi, P, heat, alpha, O);
+  if (compute_heat)
+    psup_O_kernel<true><<<tl.ntu * tl.ntv, kGatherNT, 0, st>>>(tl, N0, N1, U, V, R, psi, P, heat, alpha, O);
+  else
+    psup_O_kernel<false><<<tl.ntu * tl.ntv, kGatherNT, 0, st>>>(tl, N0, N1, U, V, R, psi, P, heat, alpha, O);
   return check_launch("psup_O_kernel");
 }
 
@@ -126,7 +161,7 @@ __global__ void __launch_bounds__(kGatherNT) psup_P_partial_kernel(
     den[q] = ff_zero();
   }
   if (b < N1) {
-    for (int f = f0; f < f1; ++f) {
+    auto fetch = [&](int f, float2 (&x)[4], float2 (&o)[4]) {
       const int r0 = R[2 * f], r1 = R[2 * f + 1];
       const float2* pf = psi + (size_t)f * N0 * N1;
       int vv = b - r1;
@@ -137,11 +172,32 @@ __global__ void __launch_bounds__(kGatherNT) psup_P_partial_kernel(
         if (a < N0) {
           int uu = a - r0;
           if (uu >= U) uu -= U;
-          const float2 o = __ldg(&O[(size_t)uu * V + vv]);
-          num[q] = cadd(num[q], cmulc(pf[a * N1 + b], o));
-          if (want_den) den[q] = ff_add(den[q], cabs2(o));
+          o[q] = __ldg(&O[(size_t)uu * V + vv]);
+          x[q] = pf[a * N1 + b];
+        } else {
+          o[q] = x[q] = make_float2(0.f, 0.f);
         }
       }
+    };
+    auto accumulate = [&](const float2 (&x)[4], const float2 (&o)[4]) {
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        num[q] = cadd(num[q], cmulc(x[q], o[q]));
+        if (want_den) den[q] = ff_add(den[q], cabs2(o[q]));
+      }
+    };
+    int f = f0;
+    for (; f + 1 < f1; f += 2) {
+      float2 x0[4], o0[4], x1[4], o1[4];
+      fetch(f, x0, o0);
+      fetch(f + 1, x1, o1);
+      accumulate(x0, o0);
+      accumulate(x1, o1);
+    }
+    if (f < f1) {
+      float2 x0[4], o0[4];
+      fetch(f, x0, o0);
+      accumulate(x0, o0);
     }
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
@@ -373,30 +429,25 @@ int launch_roll(const float2* src, float2* dst, int nimg, int H, int W, const in
   return check_launch("roll_kernel");
 }
 
-// make_exits (era.py:426-433)
-__global__ void make_exits_kernel(int n, int N0, int N1, int U, int V, const int* __restrict__ R,
+// make_exits (era.py:426-433): grid (row, frame), threads along the row
+__global__ void make_exits_kernel(int N0, int N1, int U, int V, const int* __restrict__ R,
                                   const float2* __restrict__ O, const float2* __restrict__ P,
                                   float2* __restrict__ psi) {
-  const long long tot = (long long)n * N0 * N1;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < tot;
-       i += (long long)gridDim.x * blockDim.x) {
-    const int f = (int)(i / ((long long)N0 * N1));
-    const int a = (int)((i / N1) % N0), b = (int)(i % N1);
-    int u = a - R[2 * f], v = b - R[2 * f + 1];
-    u %= U;
-    v %= V;
-    if (u < 0) u += U;
+  const int a = blockIdx.x, f = blockIdx.y;
+  int u = (a - R[2 * f]) % U;
+  if (u < 0) u += U;
+  const int r1 = R[2 * f + 1];
+  float2* out = psi + ((size_t)f * N0 + a) * N1;
+  for (int b = threadIdx.x; b < N1; b += blockDim.x) {
+    int v = (b - r1) % V;
     if (v < 0) v += V;
-    psi[i] = cmul(O[(size_t)u * V + v], P[a * N1 + b]);
+    out[b] = cmul(O[(size_t)u * V + v], P[a * N1 + b]);
   }
 }
 
 int launch_make_exits(int n, int N0, int N1, int U, int V, const int* R, const float2* O,
                       const float2* P, float2* psi, cudaStream_t st) {
-  long long tot = (long long)n * N0 * N1;
-  int blocks = (int)((tot + 255) / 256);
-  if (blocks > 152 * 32) blocks = 152 * 32;
-  make_exits_kernel<<<blocks, 256, 0, st>>>(n, N0, N1, U, V, R, O, P, psi);
+  make_exits_kernel<<<dim3(N0, n), N1 < 256 ? N1 : 256, 0, st>>>(N0, N1, U, V, R, O, P, psi);
   return check_launch("make_exits_kernel");
 }
 
