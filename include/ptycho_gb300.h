@@ -122,6 +122,25 @@ int pty_background_mean(pty_plan* plan, const float* background, float* mean_out
  * I is float32 (is_double = 0) or float64 (is_double = 1), centred order. */
 int pty_amp_from_intensity(pty_plan* plan, const void* I, int32_t is_double, float* amp,
                            void* stream);
+/* Probe update for callers that cannot allocate device memory.  No
+ * counterpart in the reference: it computes what pty_psup_P computes
+ * (psup_P, era.py:371-400) without a plan, for code that must not call
+ * cudaMalloc -- an application that owns the whole device budget, an
+ * allocator that forbids foreign allocations, or a loop that must not block
+ * on one.  Every input and output is the caller's: R_host is the int64
+ * [n][2] scan offsets on the host (validated like pty_plan_create); psi,
+ * O, O_heatmap (float64 [N0][N1], recomputed when recompute_heatmap != 0)
+ * and P_out are device pointers.  The partial sums and the device copy of R
+ * live in fixed arrays compiled into the library (8 MiB + 128 KiB on every
+ * GPU that loads it, until the process exits); sizes beyond them --
+ * N0 * N1 > 65536 or n_frames > 16384 -- are rejected with PTY_ERR_RANGE.
+ * The first call on a device looks those arrays up for that device; make it
+ * before any stream capture.  All calls share the arrays, so calls whose GPU
+ * work overlaps (other streams, other host threads) race; nothing in them
+ * needs clearing between calls, as each call writes every slot it reads. */
+int pty_psup_P_noalloc(const pty_geometry* geom, const int64_t* R_host, const void* psi,
+                       const void* O, double* O_heatmap, int32_t recompute_heatmap, double alpha,
+                       void* P_out, void* stream);
 /* 1 if the frame shape N0 x N1 has a fused FFT kernel. */
 int pty_shape_supported(int32_t N0, int32_t N1);
 const char* pty_last_error(void);

@@ -52,6 +52,8 @@ SIGNATURES = {
     "pty_intensities": [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p],
     "pty_background_mean": [c_void_p, c_void_p, c_void_p, c_void_p],
     "pty_amp_from_intensity": [c_void_p, c_void_p, c_int32, c_void_p, c_void_p],
+    "pty_psup_P_noalloc": [ctypes.POINTER(Geometry), ctypes.POINTER(c_int64), c_void_p, c_void_p,
+                           c_void_p, c_int32, c_double, c_void_p, c_void_p],
     "pty_shape_supported": [c_int32, c_int32],
     "pty_last_error": [],
     "pty_version": [],
