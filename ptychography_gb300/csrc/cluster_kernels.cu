@@ -32,7 +32,7 @@ namespace pty {
 template <int N, int C>
 struct ClusterCfg {
   static constexpr int A = LineGeom<N>::A, B = LineGeom<N>::B;  // rows and columns alike
-  static constexpr int NT = 512;
+  static constexpr int NT = C >= 8 ? 256 : 512;      // 8-CTA clusters: two CTAs per SM
   static constexpr int RPC = N / C;          // rows owned per CTA
   static constexpr int CPC = N / C;          // columns owned per CTA
   static constexpr int CP = CPC + 1;         // column-buffer pitch (float2), odd
@@ -43,12 +43,12 @@ struct ClusterCfg {
   static constexpr size_t CBUF = (size_t)N * CP + N / A;  // + one skew slot per A rows
   static constexpr size_t RSCR = (size_t)RF * ROWLEN;
   static constexpr size_t SMEM = (CBUF + RSCR + N) * sizeof(float2) + 32 * sizeof(double);
-  static_assert(RPC % RF == 0 && CPC % CW == 0 && CPC % A == 0 && CW >= 32, "cluster split");
+  static_assert(RPC % RF == 0 && CPC % CW == 0 && CPC % A == 0 && CW >= 16, "cluster split");
   static_assert(SMEM <= 227 * 1024, "shared memory budget");
 };
 
 template <int N, int C, int OP>
-__global__ void __cluster_dims__(C, 1, 1) __launch_bounds__(512, 1)
+__global__ void __cluster_dims__(C, 1, 1) __launch_bounds__(ClusterCfg<N, C>::NT, 512 / ClusterCfg<N, C>::NT)
     cluster_frame_kernel(FrameArgs g) {
   using K = ClusterCfg<N, C>;
   constexpr int A = K::A, B = K::B, CP = K::CP, RPC = K::RPC, CPC = K::CPC, RF = K::RF, CW = K::CW;
@@ -169,7 +169,7 @@ __global__ void __cluster_dims__(C, 1, 1) __launch_bounds__(512, 1)
   }
 }
 
-constexpr int kClusterN = 256, kClusterC = 4;
+constexpr int kClusterN = 256, kClusterC = 8;
 
 template <int OP>
 static int set_cluster_attr() {

@@ -15,6 +15,36 @@
 #pragma once
 #include "pty_common.cuh"
 
+// x * W^E with W = exp(-2 pi i / R) (forward) or its conjugate (inverse).
+// Multiples of R/8 reduce to swaps, negations and one scale by sqrt(1/2), so
+// no multiply is spent on +-1 or +-i (whose float constants would not be exact).
+template <int E, int R, int DIR>
+PTY_DEV float2 tw_mul(float2 x) {
+  constexpr int e0 = ((E % R) + R) % R;
+  constexpr int e = (DIR < 0) ? e0 : (R - e0) % R;   // inverse: conj(W^e) = W^(R-e)
+  constexpr float h = 0.70710678118654752440f;       // sqrt(1/2)
+  if constexpr (e == 0) {
+    return x;
+  } else if constexpr (4 * e == R) {                  // -i
+    return make_float2(x.y, -x.x);
+  } else if constexpr (2 * e == R) {                  // -1
+    return make_float2(-x.x, -x.y);
+  } else if constexpr (4 * e == 3 * R) {              // +i
+    return make_float2(-x.y, x.x);
+  } else if constexpr (8 * e == R) {                  // h - h i
+    return make_float2(h * (x.x + x.y), h * (x.y - x.x));
+  } else if constexpr (8 * e == 3 * R) {              // -h - h i
+    return make_float2(h * (x.y - x.x), -h * (x.x + x.y));
+  } else if constexpr (8 * e == 5 * R) {              // -h + h i
+    return make_float2(-h * (x.x + x.y), h * (x.x - x.y));
+  } else if constexpr (8 * e == 7 * R) {              // h + h i
+    return make_float2(h * (x.x - x.y), h * (x.x + x.y));
+  } else {
+    constexpr float wr = (float)ctrig::wre(e, R), wi = (float)ctrig::wim(e, R);
+    return cmul(x, make_float2(wr, wi));
+  }
+}
+
 template <int DIR>
 PTY_DEV void bfly4(float2& a, float2& b, float2& c, float2& d) {
   // X0 = a+b+c+d, X2 = a-b+c-d, X1/X3 = (a-c) -/+ i (b-d) (forward)
@@ -53,15 +83,10 @@ PTY_DEV void dft(float2 (&x)[R]) {
     dft<M, DIR>(s3);
     sfor<0, M>([&](auto ik) {
       constexpr int k = decltype(ik)::value;
-      float2 a = s0[k], b = s1[k], c = s2[k], d = s3[k];
-      if constexpr (k != 0) {
-        constexpr float w1r = (float)ctrig::wre(k, R), w1i = (float)ctrig::wim(k, R);
-        constexpr float w2r = (float)ctrig::wre(2 * k, R), w2i = (float)ctrig::wim(2 * k, R);
-        constexpr float w3r = (float)ctrig::wre(3 * k, R), w3i = (float)ctrig::wim(3 * k, R);
-        b = ctw<DIR>(b, make_float2(w1r, w1i));
-        c = ctw<DIR>(c, make_float2(w2r, w2i));
-        d = ctw<DIR>(d, make_float2(w3r, w3i));
-      }
+      float2 a = s0[k];
+      float2 b = tw_mul<k, R, DIR>(s1[k]);
+      float2 c = tw_mul<2 * k, R, DIR>(s2[k]);
+      float2 d = tw_mul<3 * k, R, DIR>(s3[k]);
       bfly4<DIR>(a, b, c, d);
       x[k] = a;
       x[k + M] = b;
@@ -80,11 +105,8 @@ PTY_DEV void dft(float2 (&x)[R]) {
     dft<M, DIR>(s1);
     sfor<0, M>([&](auto ik) {
       constexpr int k = decltype(ik)::value;
-      float2 a = s0[k], b = s1[k];
-      if constexpr (k != 0) {
-        constexpr float wr = (float)ctrig::wre(k, R), wi = (float)ctrig::wim(k, R);
-        b = ctw<DIR>(b, make_float2(wr, wi));
-      }
+      float2 a = s0[k];
+      float2 b = tw_mul<k, R, DIR>(s1[k]);
       x[k] = cadd(a, b);
       x[k + M] = csub(a, b);
     });

@@ -15,13 +15,12 @@ struct OpTraits {
   static constexpr bool INVERSE = !(OP == OP_MERR || OP == OP_MERR_PSI || OP == OP_INTENS);
 };
 
-// exit wave P * O[window] (era.py:426-433) at frame pixel (a, b)
+// exit wave P * O[window] (era.py:426-433) at frame pixel (a, b).  Plan
+// creation guarantees every window lies inside the object, so the periodic
+// wrap of the reference's roll never triggers and is not evaluated.
 template <int N1>
 PTY_DEV float2 exit_wave(const FrameArgs& g, int r0, int r1, int a, int b) {
-  int u = a - r0, v = b - r1;
-  if (u >= g.U) u -= g.U;
-  if (v >= g.V) v -= g.V;
-  return cmul(__ldg(&g.O[(size_t)u * g.V + v]), __ldg(&g.P[a * N1 + b]));
+  return cmul(__ldg(&g.O[(size_t)(a - r0) * g.V + (b - r1)]), __ldg(&g.P[a * N1 + b]));
 }
 
 template <int N1, int OP>
@@ -72,37 +71,40 @@ PTY_DEV void frame_modulus_line(const FrameArgs& g, int f, size_t fbase, int t, 
 #pragma unroll
     for (int j = 0; j < B; ++j) {
       const float2 F = v[j];
+      // square roots and quotients use the hardware reciprocal square root
+      // (a few ulp; the engine's tolerances are 1e-5 relative)
       if constexpr (OP == OP_EXIT1 || OP == OP_PSI1 || OP == OP_DM1) {
         // era.py:561-571: |F| + alpha, masked pixels keep F
-        const float mag = sqrtf(cabs2(F)) + g.alpha;
+        const float x2 = cabs2(F);
+        const float mag = (x2 > 0.f ? x2 * rsqrtf(x2) : 0.f) + g.alpha;
         if (g.err_part) {
           const float d = mag - am[j];
           err = ff_add(err, d * d * mk[j]);
         }
-        const float fac = (mk[j] != 0.f) ? am[j] / mag : 1.0f;
+        const float fac = (mk[j] != 0.f) ? __fdividef(am[j], mag) : 1.0f;
         v[j] = cscale(F, fac);
       } else if constexpr (OP == OP_EXIT7 || OP == OP_PSI7) {
         // era.py:584-594: sqrt(|F|^2 + b^2 + alpha), masked pixels zeroed
-        const float mag = sqrtf(cabs2(F) + bb[j] * bb[j] + g.alpha);
+        const float x2 = cabs2(F) + bb[j] * bb[j] + g.alpha;
+        const float rs = rsqrtf(x2);
         if (g.err_part) {
-          const float d = mag - am[j];
+          const float d = x2 * rs - am[j];
           err = ff_add(err, d * d * mk[j]);
         }
-        const float fac = mk[j] * am[j] / mag;
+        const float fac = mk[j] * am[j] * rs;
         v[j] = cscale(F, fac);
         bb[j] *= fac;
       } else if constexpr (OP == OP_DM7) {
         // dm.py:219-224 on the background: g1 = g - b0 ; tb = b0 - g1 ; g = g1 + Pmod7(tb)
         const float g1 = bb[j] - b0v[j];
         const float tb = b0v[j] - g1;
-        const float mag = sqrtf(cabs2(F) + tb * tb + g.alpha);
-        const float fac = mk[j] * am[j] / mag;
+        const float fac = mk[j] * am[j] * rsqrtf(cabs2(F) + tb * tb + g.alpha);
         v[j] = cscale(F, fac);
         bb[j] = g1 + tb * fac;
       } else if constexpr (OP == OP_MERR || OP == OP_MERR_PSI) {
         // dm.py:338-340, no alpha
-        const float mag = sqrtf(cabs2(F) + bb[j] * bb[j]);
-        const float d = mag - am[j];
+        const float x2 = cabs2(F) + bb[j] * bb[j];
+        const float d = (x2 > 0.f ? x2 * rsqrtf(x2) : 0.f) - am[j];
         err = ff_add(err, mk[j] * (d * d));
       }
     }
