@@ -179,15 +179,15 @@ extern "C" int pty_plan_create(const pty_geometry* g, const int64_t* R_host, pty
   int rc = PTY_OK;
   auto fail = [&](int code) { pty_plan_destroy(p); return code; };
 
-  // per-tile ascending frame lists for the object gathers
-  const int T = 32;
-  const int ntu = (U + T - 1) / T, ntv = (V + T - 1) / T;
+  // per-tile ascending frame lists for the object gathers (16-row x 32-column tiles)
+  const int T = 32, TR = 16;
+  const int ntu = (U + TR - 1) / TR, ntv = (V + T - 1) / T;
   std::vector<int> ptr((size_t)ntu * ntv + 1, 0), frames;
   {
     std::vector<std::vector<int>> lists((size_t)ntu * ntv);
     for (int f = 0; f < n; ++f) {
       const int u0 = -R[2 * f], v0 = -R[2 * f + 1];
-      const int tu0 = u0 / T, tu1 = (u0 + N0 - 1) / T, tv0 = v0 / T, tv1 = (v0 + N1 - 1) / T;
+      const int tu0 = u0 / TR, tu1 = (u0 + N0 - 1) / TR, tv0 = v0 / T, tv1 = (v0 + N1 - 1) / T;
       for (int tu = tu0; tu <= tu1 && tu < ntu; ++tu)
         for (int tv = tv0; tv <= tv1 && tv < ntv; ++tv) lists[(size_t)tu * ntv + tv].push_back(f);
     }
@@ -208,7 +208,7 @@ extern "C" int pty_plan_create(const pty_geometry* g, const int64_t* R_host, pty
   if ((rc = dalloc_t(p, &p->d_heatO2, npix))) return fail(rc);
   {
     // enough frame chunks for about four waves of probe-gather blocks
-    const int ntiles = ((N0 + 31) / 32) * ((N1 + 31) / 32);
+    const int ntiles = ((N0 + 15) / 16) * ((N1 + 31) / 32);
     int K = (2432 + ntiles - 1) / ntiles;
     if (K > 64) K = 64;
     if (K > n) K = n;
@@ -251,7 +251,7 @@ extern "C" int pty_plan_create(const pty_geometry* g, const int64_t* R_host, pty
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&p->ev_in, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&p->ev_out, cudaEventDisableTiming);
   if (e != cudaSuccess) return fail(set_cuda_error(e, "pty_plan_create"));
-  p->tl = TileLists{T, T, ntu, ntv, p->d_tile_ptr, p->d_tile_frames};
+  p->tl = TileLists{TR, T, ntu, ntv, p->d_tile_ptr, p->d_tile_frames};
   if ((rc = prepare_kernels(N0, N1))) return fail(rc);
   *out = p;
   return PTY_OK;

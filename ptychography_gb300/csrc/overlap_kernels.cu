@@ -9,15 +9,17 @@
 
 namespace pty {
 
-constexpr int kTile = 32;      // object / probe tile edge
-constexpr int kGatherNT = 256; // threads per tile (4 pixels each)
+constexpr int kTile = 32;      // tile width (columns) of the object / probe gathers
+constexpr int kTileRows = 16;  // tile height (rows)
+constexpr int kGatherNT = 256; // threads per tile: 32 columns x 8 rows, 2 pixels each
+constexpr int kPrefetch = 4;   // frames whose loads are issued together
 
 // ------------------------------------------------------------------ psup_O
 // era.py:336-369: O = sum_i psi_i * conj(P) placed at window i, / (heat + alpha),
 // with heat = sum_i |P|^2 (era.py:402-410) recomputed in the same pass when HEAT.
-// A thread owns 4 pixels of a 32 x 32 object tile; the tile's frames are
-// visited in ascending order, two at a time with all loads issued first.
-// Out-of-window pixels contribute an exact zero.
+// A thread owns 2 pixels (rows ty, ty + 8) of a 16 x 32 object tile; the tile's
+// frames are visited in ascending order, kPrefetch at a time with all their
+// loads issued first.  Out-of-window pixels contribute an exact zero.
 template <bool HEAT>
 __global__ void __launch_bounds__(kGatherNT) psup_O_kernel(
     TileLists tl, int N0, int N1, int U, int V, const int* __restrict__ R,
@@ -27,52 +29,52 @@ __global__ void __launch_bounds__(kGatherNT) psup_O_kernel(
   const int tu = tile / tl.ntv, tv = tile % tl.ntv;
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
   const int v = tv * kTile + tx;
-  const int u0 = tu * kTile + ty;
-  float2 acc[4];
-  ff h[4];
+  const int u0 = tu * kTileRows + ty;
+  float2 acc[2];
+  ff h[2];
 #pragma unroll
-  for (int k = 0; k < 4; ++k) {
+  for (int k = 0; k < 2; ++k) {
     acc[k] = make_float2(0.f, 0.f);
     h[k] = ff_zero();
   }
   const int beg = tl.ptr[tile], end = tl.ptr[tile + 1];
-  auto fetch = [&](int e, float2 (&x)[4], float2 (&p)[4]) {
+  auto fetch = [&](int e, float2 (&x)[2], float2 (&p)[2]) {
     const int f = tl.frames[e];
     const int r0 = R[2 * f], r1 = R[2 * f + 1];
     const int b = v + r1;
     const bool bok = b >= 0 && b < N1;
     const float2* pf = psi + (size_t)f * N0 * N1;
 #pragma unroll
-    for (int k = 0; k < 4; ++k) {
+    for (int k = 0; k < 2; ++k) {
       const int a = u0 + 8 * k + r0;
       const bool ok = bok && a >= 0 && a < N0;
       x[k] = ok ? pf[a * N1 + b] : make_float2(0.f, 0.f);
       p[k] = ok ? P[a * N1 + b] : make_float2(0.f, 0.f);
     }
   };
-  auto accumulate = [&](const float2 (&x)[4], const float2 (&p)[4]) {
+  auto accumulate = [&](const float2 (&x)[2], const float2 (&p)[2]) {
 #pragma unroll
-    for (int k = 0; k < 4; ++k) {
+    for (int k = 0; k < 2; ++k) {
       acc[k] = cadd(acc[k], cmulc(x[k], p[k]));
       if (HEAT) h[k] = ff_add(h[k], cabs2(p[k]));
     }
   };
   int e = beg;
-  for (; e + 1 < end; e += 2) {
-    float2 x0[4], p0[4], x1[4], p1[4];
-    fetch(e, x0, p0);
-    fetch(e + 1, x1, p1);
-    accumulate(x0, p0);
-    accumulate(x1, p1);
+  for (; e + kPrefetch <= end; e += kPrefetch) {
+    float2 x[kPrefetch][2], p[kPrefetch][2];
+#pragma unroll
+    for (int q = 0; q < kPrefetch; ++q) fetch(e + q, x[q], p[q]);
+#pragma unroll
+    for (int q = 0; q < kPrefetch; ++q) accumulate(x[q], p[q]);
   }
-  if (e < end) {
-    float2 x0[4], p0[4];
-    fetch(e, x0, p0);
-    accumulate(x0, p0);
+  for (; e < end; ++e) {
+    float2 x[2], p[2];
+    fetch(e, x, p);
+    accumulate(x, p);
   }
   if (v < V) {
 #pragma unroll
-    for (int k = 0; k < 4; ++k) {
+    for (int k = 0; k < 2; ++k) {
       const int uu = u0 + 8 * k;
       if (uu < U) {
         const size_t o = (size_t)uu * V + v;
@@ -98,9 +100,9 @@ __global__ void __launch_bounds__(kGatherNT) heat_P_kernel(
   const int tu = tile / tl.ntv, tv = tile % tl.ntv;
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
   const int v = tv * kTile + tx;
-  ff acc[4];
+  ff acc[2];
 #pragma unroll
-  for (int k = 0; k < 4; ++k) acc[k] = ff_zero();
+  for (int k = 0; k < 2; ++k) acc[k] = ff_zero();
   const int beg = tl.ptr[tile], end = tl.ptr[tile + 1];
   for (int e = beg; e < end; ++e) {
     const int f = tl.frames[e];
@@ -108,15 +110,15 @@ __global__ void __launch_bounds__(kGatherNT) heat_P_kernel(
     const int b = v + r1;
     if (b < 0 || b >= N1) continue;
 #pragma unroll
-    for (int k = 0; k < 4; ++k) {
-      const int a = tu * kTile + ty + 8 * k + r0;
+    for (int k = 0; k < 2; ++k) {
+      const int a = tu * kTileRows + ty + 8 * k + r0;
       if (a >= 0 && a < N0) acc[k] = ff_add(acc[k], cabs2(__ldg(&P[a * N1 + b])));
     }
   }
   if (v < V) {
 #pragma unroll
-    for (int k = 0; k < 4; ++k) {
-      const int uu = tu * kTile + ty + 8 * k;
+    for (int k = 0; k < 2; ++k) {
+      const int uu = tu * kTileRows + ty + 8 * k;
       if (uu < U) heat[(size_t)uu * V + v] = ff_to_double(acc[k]);
     }
   }
@@ -142,7 +144,9 @@ int launch_heat_P(const TileLists& tl, int n, int N0, int N1, int U, int V, cons
 
 // ------------------------------------------------------------------ psup_P
 // era.py:371-400 (+ make_O_heatmap era.py:412-417): per probe pixel, sum over
-// frames of psi_i * conj(O_i) and |O_i|^2.  Grid: probe tiles x K frame chunks.
+// frames of psi_i * conj(O_i) and |O_i|^2.  Grid: 16 x 32 probe tiles x K frame
+// chunks; a thread owns 2 pixels (rows ty, ty + 8) and issues the loads of
+// kPrefetch frames together.
 __global__ void __launch_bounds__(kGatherNT) psup_P_partial_kernel(
     int n, int N0, int N1, int U, int V, const int* __restrict__ R, const float2* __restrict__ psi,
     const float2* __restrict__ O, int K, bool want_den, float2* __restrict__ part_num,
@@ -153,55 +157,52 @@ __global__ void __launch_bounds__(kGatherNT) psup_P_partial_kernel(
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
   const int b = tv * kTile + tx;
   const int f0 = (int)(((long long)n * k) / K), f1 = (int)(((long long)n * (k + 1)) / K);
-  float2 num[4];
-  ff den[4];
+  float2 num[2];
+  ff den[2];
 #pragma unroll
-  for (int q = 0; q < 4; ++q) {
+  for (int q = 0; q < 2; ++q) {
     num[q] = make_float2(0.f, 0.f);
     den[q] = ff_zero();
   }
   if (b < N1) {
-    auto fetch = [&](int f, float2 (&x)[4], float2 (&o)[4]) {
+    auto fetch = [&](int f, float2 (&x)[2], float2 (&o)[2]) {
       const int r0 = R[2 * f], r1 = R[2 * f + 1];
       const float2* pf = psi + (size_t)f * N0 * N1;
-      int vv = b - r1;
-      if (vv >= V) vv -= V;
+      const int vv = b - r1;
 #pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        const int a = tu * kTile + ty + 8 * q;
+      for (int q = 0; q < 2; ++q) {
+        const int a = tu * kTileRows + ty + 8 * q;
         if (a < N0) {
-          int uu = a - r0;
-          if (uu >= U) uu -= U;
-          o[q] = __ldg(&O[(size_t)uu * V + vv]);
+          o[q] = __ldg(&O[(size_t)(a - r0) * V + vv]);
           x[q] = pf[a * N1 + b];
         } else {
           o[q] = x[q] = make_float2(0.f, 0.f);
         }
       }
     };
-    auto accumulate = [&](const float2 (&x)[4], const float2 (&o)[4]) {
+    auto accumulate = [&](const float2 (&x)[2], const float2 (&o)[2]) {
 #pragma unroll
-      for (int q = 0; q < 4; ++q) {
+      for (int q = 0; q < 2; ++q) {
         num[q] = cadd(num[q], cmulc(x[q], o[q]));
         if (want_den) den[q] = ff_add(den[q], cabs2(o[q]));
       }
     };
     int f = f0;
-    for (; f + 1 < f1; f += 2) {
-      float2 x0[4], o0[4], x1[4], o1[4];
-      fetch(f, x0, o0);
-      fetch(f + 1, x1, o1);
-      accumulate(x0, o0);
-      accumulate(x1, o1);
+    for (; f + kPrefetch <= f1; f += kPrefetch) {
+      float2 x[kPrefetch][2], o[kPrefetch][2];
+#pragma unroll
+      for (int q = 0; q < kPrefetch; ++q) fetch(f + q, x[q], o[q]);
+#pragma unroll
+      for (int q = 0; q < kPrefetch; ++q) accumulate(x[q], o[q]);
     }
-    if (f < f1) {
-      float2 x0[4], o0[4];
-      fetch(f, x0, o0);
-      accumulate(x0, o0);
+    for (; f < f1; ++f) {
+      float2 x[2], o[2];
+      fetch(f, x, o);
+      accumulate(x, o);
     }
 #pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      const int a = tu * kTile + ty + 8 * q;
+    for (int q = 0; q < 2; ++q) {
+      const int a = tu * kTileRows + ty + 8 * q;
       if (a < N0) {
         const size_t o = (size_t)k * N0 * N1 + (size_t)a * N1 + b;
         part_num[o] = num[q];
@@ -241,7 +242,7 @@ __global__ void psup_P_reduce_kernel(int npix, int K, const float2* __restrict__
 int launch_psup_P(int n, int N0, int N1, int U, int V, const int* R, const float2* psi,
                   const float2* O, float2* part_num, float2* part_den, int K, double* heatO,
                   bool recompute_heat, float alpha, float2* P, cudaStream_t st) {
-  const int ntiles = ((N0 + kTile - 1) / kTile) * ((N1 + kTile - 1) / kTile);
+  const int ntiles = ((N0 + kTileRows - 1) / kTileRows) * ((N1 + kTile - 1) / kTile);
   psup_P_partial_kernel<<<dim3(ntiles, K), kGatherNT, 0, st>>>(n, N0, N1, U, V, R, psi, O, K,
                                                                recompute_heat, part_num, part_den);
   int rc = check_launch("psup_P_partial_kernel");
@@ -429,25 +430,25 @@ int launch_roll(const float2* src, float2* dst, int nimg, int H, int W, const in
   return check_launch("roll_kernel");
 }
 
-// make_exits (era.py:426-433): grid (row, frame), threads along the row
+// make_exits (era.py:426-433): grid (8-row band, frame), threads along a row.
+// Plan creation guarantees every window lies inside the object.
 __global__ void make_exits_kernel(int N0, int N1, int U, int V, const int* __restrict__ R,
                                   const float2* __restrict__ O, const float2* __restrict__ P,
                                   float2* __restrict__ psi) {
-  const int a = blockIdx.x, f = blockIdx.y;
-  int u = (a - R[2 * f]) % U;
-  if (u < 0) u += U;
-  const int r1 = R[2 * f + 1];
-  float2* out = psi + ((size_t)f * N0 + a) * N1;
-  for (int b = threadIdx.x; b < N1; b += blockDim.x) {
-    int v = (b - r1) % V;
-    if (v < 0) v += V;
-    out[b] = cmul(O[(size_t)u * V + v], P[a * N1 + b]);
+  const int f = blockIdx.y;
+  const int r0 = R[2 * f], r1 = R[2 * f + 1];
+  const int npix = 8 * N1;
+  const int a0 = blockIdx.x * 8;
+  float2* out = psi + ((size_t)f * N0 + a0) * N1;
+  for (int i = threadIdx.x; i < npix; i += blockDim.x) {
+    const int a = a0 + i / N1, b = i % N1;
+    if (a < N0) out[i] = cmul(__ldg(&O[(size_t)(a - r0) * V + (b - r1)]), __ldg(&P[a * N1 + b]));
   }
 }
 
 int launch_make_exits(int n, int N0, int N1, int U, int V, const int* R, const float2* O,
                       const float2* P, float2* psi, cudaStream_t st) {
-  make_exits_kernel<<<dim3(N0, n), N1 < 256 ? N1 : 256, 0, st>>>(N0, N1, U, V, R, O, P, psi);
+  make_exits_kernel<<<dim3((N0 + 7) / 8, n), 256, 0, st>>>(N0, N1, U, V, R, O, P, psi);
   return check_launch("make_exits_kernel");
 }
 
