@@ -281,11 +281,15 @@ def roofline_pmod7(job, torch, reps=20):
         fn()
     t = event_time(torch, fn, reps) / reps
     bytes_ = 28.0 * job.N * job.N * job.n
+    # DRAM bytes (read + write) of one launch from the ncu capture in
+    # profiles/cluster_frame_kernel_psi7_256x256x256.md (410.0 MB for 256 frames),
+    # scaled by frames; recorded for the 256 x 256 kernel only
+    traffic = round(410.0e6 * job.n / 256) if job.N == 256 else None
     pk, kind = peaks()
     gbs = bytes_ / t / 1e9
     return {"kernel": "cluster_frame_kernel<256,4,PSI7>" if job.N == 256 else "frame_kernel<PSI7>",
             "bound": "hbm", "achieved": round(gbs, 1), "peak": pk, "unit": "GB/s",
-            "frac": round(gbs / pk, 4), "peak_kind": kind, "traffic": None,
+            "frac": round(gbs / pk, 4), "peak_kind": kind, "traffic": traffic,
             "launch_ms": round(t * 1e3, 4), "algorithmic_bytes": bytes_}
 
 

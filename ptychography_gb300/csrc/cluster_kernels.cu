@@ -29,6 +29,13 @@ namespace cg = cooperative_groups;
 
 namespace pty {
 
+// Cluster barrier without memory ordering: used only to keep every CTA's
+// shared memory alive until the others have finished reading it, which needs
+// no release of this CTA's own (global) stores.
+PTY_DEV void cluster_sync_relaxed() {
+  asm volatile("barrier.cluster.arrive.relaxed.aligned;\n\tbarrier.cluster.wait.aligned;" ::: "memory");
+}
+
 template <int N, int C>
 struct ClusterCfg {
   static constexpr int A = LineGeom<N>::A, B = LineGeom<N>::B;  // rows and columns alike
@@ -45,6 +52,8 @@ struct ClusterCfg {
   static constexpr size_t SMEM = (CBUF + RSCR + N) * sizeof(float2) + 32 * sizeof(double);
   static_assert(RPC % RF == 0 && CPC % CW == 0 && CPC % A == 0 && CW >= 16, "cluster split");
   static_assert(SMEM <= 227 * 1024, "shared memory budget");
+  // the column pass exchanges through the (then idle) row scratch
+  static_assert((size_t)N * CW <= RSCR, "column exchange fits the row scratch");
 };
 
 template <int N, int C, int OP>
@@ -110,31 +119,34 @@ __global__ void __cluster_dims__(C, 1, 1) __launch_bounds__(ClusterCfg<N, C>::NT
 
   // ---------------- 3. column pass on the owned columns
   // Lanes of a warp run along a row (coalesced amp / mask / background
-  // traffic); the A threads of a column sit in A different warps, so the
-  // exchanges synchronise the CTA.
+  // traffic); the A threads of a column sit in A different warps.  The
+  // exchanges go through the row scratch, idle during this pass, as a
+  // [row slot][CW columns] array, so loads of the column buffer and exchange
+  // writes never collide and fewer CTA barriers are needed.
   ff err = ff_zero();
+  float2* xb = rscr;
 #pragma unroll 1
   for (int s = 0; s < CPC / CW; ++s) {
-    const int cl = s * CW + tid % CW, tc = tid / CW;
+    const int cw = tid % CW, tc = tid / CW;
+    const int cl = s * CW + cw;
     const int kc = rank * CPC + cl;
     float2 v[B];
 #pragma unroll
     for (int j = 0; j < B; ++j) v[j] = cbuf[cidx(tc + A * j, cl)];
     line_stage1<N, -1>(v, tc, tw);
-    __syncthreads();
+    if (s > 0) __syncthreads();   // previous sub-pass done reading xb
 #pragma unroll
-    for (int k1 = 0; k1 < B; ++k1) cbuf[cidx(k1 * A + tc, cl)] = v[k1];
+    for (int k1 = 0; k1 < B; ++k1) xb[(k1 * A + tc) * CW + cw] = v[k1];
     __syncthreads();
-    line_stage2<N, -1>(v, tc, [&](int tt, int k1) { return cbuf[cidx(k1 * A + tt, cl)]; });
+    line_stage2<N, -1>(v, tc, [&](int tt, int k1) { return xb[(k1 * A + tt) * CW + cw]; });
     frame_modulus_line<N, N, OP, A, B>(g, f, fbase, tc, kc, v, err);
     if constexpr (INVERSE) {
       line_stage1<N, +1>(v, tc, tw);
       __syncthreads();
 #pragma unroll
-      for (int k1 = 0; k1 < B; ++k1) cbuf[cidx(k1 * A + tc, cl)] = v[k1];
+      for (int k1 = 0; k1 < B; ++k1) xb[(k1 * A + tc) * CW + cw] = v[k1];
       __syncthreads();
-      line_stage2<N, +1>(v, tc, [&](int tt, int k1) { return cbuf[cidx(k1 * A + tt, cl)]; });
-      __syncthreads();
+      line_stage2<N, +1>(v, tc, [&](int tt, int k1) { return xb[(k1 * A + tt) * CW + cw]; });
 #pragma unroll
       for (int j = 0; j < B; ++j) cbuf[cidx(tc + A * j, cl)] = v[j];
     }
@@ -160,7 +172,9 @@ __global__ void __cluster_dims__(C, 1, 1) __launch_bounds__(ClusterCfg<N, C>::NT
       frame_output_line<N, OP, A, B>(g, r0, r1, psi, a, t, v);
       __syncwarp();
     }
-    cluster.sync();
+    // the pulled values are consumed before each CTA arrives, so a relaxed
+    // barrier suffices to keep the column buffers alive until every pull is done
+    cluster_sync_relaxed();
   }
 
   if (g.err_part) {

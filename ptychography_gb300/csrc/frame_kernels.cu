@@ -48,8 +48,11 @@ struct FrameCfg {
   static constexpr int T_ROW = N0 * A1, T_COL = N1 * A0;
   static constexpr int NT0 = T_ROW < T_COL ? T_ROW : T_COL;
   static constexpr int NT = NT0 < 512 ? NT0 : 512;
-  static constexpr size_t SMEM = (size_t)BUF * sizeof(float2) + (size_t)(N0 + N1) * sizeof(float2) +
-                                 32 * sizeof(double);
+  static constexpr int CW = NT / A0;                 // columns per column pass
+  static constexpr size_t XB = (size_t)N0 * CW;       // column exchange buffer (float2)
+  static constexpr size_t SMEM = ((size_t)BUF + XB) * sizeof(float2) +
+                                 (size_t)(N0 + N1) * sizeof(float2) + 32 * sizeof(double);
+  static_assert(SMEM <= 227 * 1024, "shared memory budget");
   static_assert(T_ROW % NT == 0 && T_COL % NT == 0 && NT % 32 == 0, "task split");
   // rows must not overlap: consecutive row bases differ by at least a padded row
   static_assert(RP + S2 >= B1 * (A1 + 1) && RP + S1 - (A0 - 1) * S2 >= B1 * (A1 + 1), "row pitch");
@@ -77,7 +80,8 @@ __global__ void __launch_bounds__(FrameCfg<N0, N1>::NT, 1) frame_kernel(FrameArg
 
   extern __shared__ __align__(16) unsigned char smem_raw[];
   float2* fr = reinterpret_cast<float2*>(smem_raw);
-  float2* tw0 = fr + C::BUF;
+  float2* xb = fr + C::BUF;   // column exchange: [row slot][CW columns]
+  float2* tw0 = xb + C::XB;
   float2* tw1 = tw0 + N0;
   double* red = reinterpret_cast<double*>(tw1 + N1);
 
@@ -116,34 +120,35 @@ __global__ void __launch_bounds__(FrameCfg<N0, N1>::NT, 1) frame_kernel(FrameArg
   // ---------------- column pass: forward FFT, modulus constraint, inverse FFT
   // Each pass takes CW whole columns (all A0 line-threads of a column in the
   // same pass, as the exchange needs); lanes of a warp run along a row, so the
-  // amp / mask / background traffic is coalesced and the exchanges
-  // synchronise the CTA.
+  // amp / mask / background traffic is coalesced.  The exchanges go through a
+  // separate [row slot][CW columns] buffer, so frame loads and exchange writes
+  // never collide and fewer CTA barriers are needed.
   ff err = ff_zero();
-  constexpr int CW = NT / A0;
+  constexpr int CW = C::CW;
   static_assert(NT % A0 == 0 && N1 % CW == 0 && CW >= 32, "column pass split");
 #pragma unroll 1
   for (int c0 = 0; c0 < N1; c0 += CW) {
-    const int c = c0 + tid % CW, t = tid / CW;
+    const int cw = tid % CW, t = tid / CW;
+    const int c = c0 + cw;
     const int cp = padpos(c, A1);
     auto at = [&](int r) -> float2& { return fr[rbase(r) + cp]; };
     float2 v[B0];
 #pragma unroll
     for (int j = 0; j < B0; ++j) v[j] = at(t + A0 * j);
     line_stage1<N0, -1>(v, t, tw0);
-    __syncthreads();
+    if (c0 > 0) __syncthreads();   // previous pass done reading xb
 #pragma unroll
-    for (int k1 = 0; k1 < B0; ++k1) at(k1 * A0 + t) = v[k1];
+    for (int k1 = 0; k1 < B0; ++k1) xb[(k1 * A0 + t) * CW + cw] = v[k1];
     __syncthreads();
-    line_stage2<N0, -1>(v, t, [&](int tt, int k1) { return at(k1 * A0 + tt); });
+    line_stage2<N0, -1>(v, t, [&](int tt, int k1) { return xb[(k1 * A0 + tt) * CW + cw]; });
     frame_modulus_line<N0, N1, OP, A0, B0>(g, f, fbase, t, c, v, err);
     if constexpr (INVERSE) {
       line_stage1<N0, +1>(v, t, tw0);
       __syncthreads();
 #pragma unroll
-      for (int k1 = 0; k1 < B0; ++k1) at(k1 * A0 + t) = v[k1];
+      for (int k1 = 0; k1 < B0; ++k1) xb[(k1 * A0 + t) * CW + cw] = v[k1];
       __syncthreads();
-      line_stage2<N0, +1>(v, t, [&](int tt, int k1) { return at(k1 * A0 + tt); });
-      __syncthreads();
+      line_stage2<N0, +1>(v, t, [&](int tt, int k1) { return xb[(k1 * A0 + tt) * CW + cw]; });
 #pragma unroll
       for (int j = 0; j < B0; ++j) at(t + A0 * j) = v[j];
     }

@@ -56,6 +56,7 @@ PTY_DEV void frame_modulus_line(const FrameArgs& g, int f, size_t fbase, int t, 
     constexpr bool BG_IN = (OP == OP_EXIT7 || OP == OP_PSI7 || OP == OP_MERR || OP == OP_MERR_PSI);
     constexpr bool BG_OUT = (OP == OP_EXIT7 || OP == OP_PSI7 || OP == OP_DM7);
     float am[B], mk[B], bb[B], b0v[B];
+    float line_err = 0.f;   // FP32 over one line (B terms), folded into err once
     const float* amp = g.amp + (size_t)g.amp_stride * f;
 #pragma unroll
     for (int j = 0; j < B; ++j) {
@@ -77,20 +78,16 @@ PTY_DEV void frame_modulus_line(const FrameArgs& g, int f, size_t fbase, int t, 
         // era.py:561-571: |F| + alpha, masked pixels keep F
         const float x2 = cabs2(F);
         const float mag = (x2 > 0.f ? x2 * rsqrtf(x2) : 0.f) + g.alpha;
-        if (g.err_part) {
-          const float d = mag - am[j];
-          err = ff_add(err, d * d * mk[j]);
-        }
+        const float d = mag - am[j];
+        line_err += d * d * mk[j];
         const float fac = (mk[j] != 0.f) ? __fdividef(am[j], mag) : 1.0f;
         v[j] = cscale(F, fac);
       } else if constexpr (OP == OP_EXIT7 || OP == OP_PSI7) {
         // era.py:584-594: sqrt(|F|^2 + b^2 + alpha), masked pixels zeroed
         const float x2 = cabs2(F) + bb[j] * bb[j] + g.alpha;
         const float rs = rsqrtf(x2);
-        if (g.err_part) {
-          const float d = x2 * rs - am[j];
-          err = ff_add(err, d * d * mk[j]);
-        }
+        const float d = x2 * rs - am[j];
+        line_err += d * d * mk[j];
         const float fac = mk[j] * am[j] * rs;
         v[j] = cscale(F, fac);
         bb[j] *= fac;
@@ -105,9 +102,10 @@ PTY_DEV void frame_modulus_line(const FrameArgs& g, int f, size_t fbase, int t, 
         // dm.py:338-340, no alpha
         const float x2 = cabs2(F) + bb[j] * bb[j];
         const float d = (x2 > 0.f ? x2 * rsqrtf(x2) : 0.f) - am[j];
-        err = ff_add(err, mk[j] * (d * d));
+        line_err += mk[j] * (d * d);
       }
     }
+    err = ff_add(err, line_err);
     if constexpr (BG_OUT) {
 #pragma unroll
       for (int j = 0; j < B; ++j) g.bg_out[fbase + (size_t)(t + A * j) * N1 + kc] = bb[j];
