@@ -115,6 +115,13 @@ int pty_model_error_1(pty_plan* plan, const float* amp, const void* psi, const u
                       void* stream);
 /* info['I'] = fftshift |FFT(P * O[R])|^2, era.py:295 */
 int pty_intensities(pty_plan* plan, const void* O, const void* P, float* I_out, void* stream);
+/* Exit waves of Back_projection, back_projection.py:74-78: for every frame,
+ * exits = ifftn(mask_c * sqrt(I)_c * exp(i angle(fftn(P)))), where amp and mask
+ * are given in the engine's unshifted order (as for pty_pmod_1) and are used in
+ * the reference's centred order, and phase holds the unit phasors
+ * exp(i angle(fftn(P))) (complex64 [N0][N1], natural FFT order).  Even sizes. */
+int pty_back_project(pty_plan* plan, const float* amp, const uint8_t* mask, const void* phase,
+                     void* exits, void* stream);
 /* Per-frame mean of a background stack, era.py:265-270 */
 int pty_background_mean(pty_plan* plan, const float* background, float* mean_out, void* stream);
 

@@ -23,7 +23,7 @@ import scipy.ndimage
 __all__ = [
     "multiroll", "make_exits", "pmod_1", "Pmod_1", "pmod_7", "Pmod_7", "Pmod_P",
     "psup_O", "psup_P", "make_P_heatmap", "make_O_heatmap", "model_error_1",
-    "preamble", "probe_shift", "ERA", "DM", "forward_sim_from_object",
+    "preamble", "probe_shift", "ERA", "DM", "forward_sim_from_object", "Back_projection",
 ]
 
 
@@ -457,3 +457,27 @@ def forward_sim_from_object(O, shape_P=(32, 64), A=14, defocus=0., photons_pupil
     if not (isinstance(B, int) and B == 0):
         B = B.astype(I.dtype)
     return I, R, M, P, O, B
+
+
+# --------------------------------------------------------------------------
+# Back_projection (back_projection.py:4-88)
+# --------------------------------------------------------------------------
+def Back_projection(I, R, P, O, mask=1, alpha=1.0e-10, full_output=True):
+    """Back projection with the probe's far-field phases (back_projection.py:4-88).
+
+    The reference calls the nonexistent ``era.psup_O_1``; the object update it
+    means is ``psup_O`` (era.py:336-369), used here.  ``sqrt(I)`` and ``mask``
+    are used in the given (centred) order against the unshifted fftn(P) phases.
+    """
+    if O is None:
+        O = np.ones((I.shape[1] + R[:, 0].max() - R[:, 0].min(),
+                     I.shape[2] + R[:, 1].max() - R[:, 1].min()), dtype=P.dtype)
+    R[:, 0] -= R[:, 0].max()
+    R[:, 1] -= R[:, 1].max()
+    amp = np.sqrt(I.astype(np.float64))
+    exits = mask * amp * np.exp(1J * np.angle(np.fft.fftn(P)))
+    exits = np.fft.ifftn(exits, axes=(-2, -1))
+    O, heat = psup_O(exits, P, R, O.shape, None, alpha)
+    if full_output:
+        return O, {"exits": exits, "heatmap": heat}
+    return O

@@ -8,10 +8,12 @@ forward_sim API of andyofmelbourne/Ptychography.
 The reconstruction loops run in libptycho_gb300.so (hand-written sm_103a CUDA,
 C ABI in include/ptycho_gb300.h); Python prepares inputs and returns outputs.
 """
-from . import dm, era, forward_models  # noqa: F401
+from . import back_projection, dm, era, forward_models  # noqa: F401
+from .back_projection import Back_projection
 from .dm import DM
 from .era import ERA
 from .forward_models import forward_sim
 
-__all__ = ["ERA", "DM", "forward_sim", "era", "dm", "forward_models"]
+__all__ = ["ERA", "DM", "forward_sim", "Back_projection", "era", "dm", "forward_models",
+           "back_projection"]
 __version__ = "0.1.0"

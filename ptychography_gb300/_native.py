@@ -51,6 +51,7 @@ SIGNATURES = {
                           c_void_p],
     "pty_intensities": [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p],
     "pty_background_mean": [c_void_p, c_void_p, c_void_p, c_void_p],
+    "pty_back_project": [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p],
     "pty_amp_from_intensity": [c_void_p, c_void_p, c_int32, c_void_p, c_void_p],
     "pty_psup_P_noalloc": [ctypes.POINTER(Geometry), ctypes.POINTER(c_int64), c_void_p, c_void_p,
                            c_void_p, c_int32, c_double, c_void_p, c_void_p],

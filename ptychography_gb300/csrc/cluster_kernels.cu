@@ -104,13 +104,13 @@ __global__ void __cluster_dims__(C, 1, 1) __launch_bounds__(ClusterCfg<N, C>::NT
     const int a = rank * RPC + s * RF + lr;
     float2 v[B];
 #pragma unroll
-    for (int j = 0; j < B; ++j) v[j] = frame_input<N, OP>(g, r0, r1, psi, a, t + A * j);
-    line_stage1<N, -1>(v, t, tw);
+    for (int j = 0; j < B; ++j) v[j] = frame_input<N, OP>(g, f, r0, r1, psi, a, t + A * j);
+    line_stage1<N, OpTraits<OP>::FIRST_DIR>(v, t, tw);
     __syncwarp();
 #pragma unroll
     for (int k1 = 0; k1 < B; ++k1) rs[k1 * (A + 1) + t] = v[k1];
     __syncwarp();
-    line_stage2<N, -1>(v, t, [&](int tt, int k1) { return rs[k1 * (A + 1) + tt]; });
+    line_stage2<N, OpTraits<OP>::FIRST_DIR>(v, t, [&](int tt, int k1) { return rs[k1 * (A + 1) + tt]; });
     // v[j] = X[a][t + A j]; column t + A j belongs to CTA j / JPC
 #pragma unroll
     for (int j = 0; j < B; ++j) rc[j / JPC][cidx(a, t + A * (j % JPC))] = v[j];
@@ -133,12 +133,12 @@ __global__ void __cluster_dims__(C, 1, 1) __launch_bounds__(ClusterCfg<N, C>::NT
     float2 v[B];
 #pragma unroll
     for (int j = 0; j < B; ++j) v[j] = cbuf[cidx(tc + A * j, cl)];
-    line_stage1<N, -1>(v, tc, tw);
+    line_stage1<N, OpTraits<OP>::FIRST_DIR>(v, tc, tw);
     if (s > 0) __syncthreads();   // previous sub-pass done reading xb
 #pragma unroll
     for (int k1 = 0; k1 < B; ++k1) xb[(k1 * A + tc) * CW + cw] = v[k1];
     __syncthreads();
-    line_stage2<N, -1>(v, tc, [&](int tt, int k1) { return xb[(k1 * A + tt) * CW + cw]; });
+    line_stage2<N, OpTraits<OP>::FIRST_DIR>(v, tc, [&](int tt, int k1) { return xb[(k1 * A + tt) * CW + cw]; });
     frame_modulus_line<N, N, OP, A, B>(g, f, fbase, tc, kc, v, err);
     if constexpr (INVERSE) {
       line_stage1<N, +1>(v, tc, tw);
@@ -216,6 +216,7 @@ int prepare_cluster_frame_kernels() {
   if (!rc) rc = set_cluster_attr<OP_MERR>();
   if (!rc) rc = set_cluster_attr<OP_INTENS>();
   if (!rc) rc = set_cluster_attr<OP_MERR_PSI>();
+  if (!rc) rc = set_cluster_attr<OP_BP>();
   return rc;
 }
 
@@ -230,6 +231,7 @@ int launch_cluster_frame_op(int op, const FrameArgs& a, int nframes, cudaStream_
     case OP_MERR: return launch_cluster<OP_MERR>(a, nframes, st);
     case OP_INTENS: return launch_cluster<OP_INTENS>(a, nframes, st);
     case OP_MERR_PSI: return launch_cluster<OP_MERR_PSI>(a, nframes, st);
+    case OP_BP: return launch_cluster<OP_BP>(a, nframes, st);
   }
   return set_error(PTY_ERR_ARG, "unknown frame op");
 }

@@ -266,6 +266,8 @@ static FrameArgs base_args(const pty_plan* p) {
   a.tw0 = p->d_tw0;
   a.tw1 = p->d_tw1;
   a.amp_stride = (long long)p->N0 * p->N1;
+  a.N0h = p->N0 / 2;
+  a.N1h = p->N1 / 2;
   return a;
 }
 
@@ -737,6 +739,18 @@ extern "C" int pty_intensities(pty_plan* p, const void* O, const void* P, float*
   a.P = (const float2*)P;
   a.out_real = I_out;
   return frame_op(p, OP_INTENS, a, p->n, (cudaStream_t)stream);
+}
+
+extern "C" int pty_back_project(pty_plan* p, const float* amp, const uint8_t* mask,
+                                const void* phase, void* exits, void* stream) {
+  if (!p || !amp || !phase || !exits) return set_error(PTY_ERR_ARG, "null argument");
+  if ((p->N0 & 1) || (p->N1 & 1)) return set_error(PTY_ERR_SHAPE, "back projection needs even frame sizes");
+  FrameArgs a = base_args(p);
+  a.amp = amp;
+  a.mask = mask;
+  a.P = (const float2*)phase;
+  a.psi = (float2*)exits;
+  return frame_op(p, OP_BP, a, p->n, (cudaStream_t)stream);
 }
 
 extern "C" int pty_background_mean(pty_plan* p, const float* background, float* mean_out,

@@ -19,6 +19,7 @@ enum FrameOp {
   OP_MERR = 6,   // P*O[R] -> FFT -> model error (no alpha)                    (model_error_1)
   OP_INTENS = 7, // P*O[R] -> FFT -> fftshift |F|^2                            (info['I'])
   OP_MERR_PSI = 8, // psi -> FFT -> model error                                (model_error_1)
+  OP_BP = 9,     // mask * sqrt(I) * exp(i arg FFT(P)) -> IFFT -> psi           (Back_projection)
 };
 
 struct FrameArgs {
@@ -37,6 +38,7 @@ struct FrameArgs {
   float* out_real;           // [n][N0][N1] intensities (OP_INTENS)
   double* err_part;          // [n] per-frame error partials, or nullptr
   float alpha;
+  int N0h, N1h;              // N0 / 2, N1 / 2 (back-projection index roll)
   const float2* tw0;         // twiddles of the column transform (length N0)
   const float2* tw1;         // twiddles of the row transform (length N1)
 };

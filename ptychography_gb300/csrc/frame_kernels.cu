@@ -104,13 +104,13 @@ __global__ void __launch_bounds__(FrameCfg<N0, N1>::NT, 1) frame_kernel(FrameArg
     const int t = id % A1, a = row_of_slot<A1>(id / A1);
     float2 v[B1];
 #pragma unroll
-    for (int j = 0; j < B1; ++j) v[j] = frame_input<N1, OP>(g, r0, r1, psi, a, t + A1 * j);
-    line_stage1<N1, -1>(v, t, tw1);
+    for (int j = 0; j < B1; ++j) v[j] = frame_input<N1, OP>(g, f, r0, r1, psi, a, t + A1 * j);
+    line_stage1<N1, OpTraits<OP>::FIRST_DIR>(v, t, tw1);
     float2* row = fr + rbase(a);
 #pragma unroll
     for (int k1 = 0; k1 < B1; ++k1) row[k1 * (A1 + 1) + t] = v[k1];
     __syncwarp();
-    line_stage2<N1, -1>(v, t, [&](int tt, int k1) { return row[k1 * (A1 + 1) + tt]; });
+    line_stage2<N1, OpTraits<OP>::FIRST_DIR>(v, t, [&](int tt, int k1) { return row[k1 * (A1 + 1) + tt]; });
     __syncwarp();
 #pragma unroll
     for (int j = 0; j < B1; ++j) row[t + j * (A1 + 1)] = v[j];
@@ -135,12 +135,12 @@ __global__ void __launch_bounds__(FrameCfg<N0, N1>::NT, 1) frame_kernel(FrameArg
     float2 v[B0];
 #pragma unroll
     for (int j = 0; j < B0; ++j) v[j] = at(t + A0 * j);
-    line_stage1<N0, -1>(v, t, tw0);
+    line_stage1<N0, OpTraits<OP>::FIRST_DIR>(v, t, tw0);
     if (c0 > 0) __syncthreads();   // previous pass done reading xb
 #pragma unroll
     for (int k1 = 0; k1 < B0; ++k1) xb[(k1 * A0 + t) * CW + cw] = v[k1];
     __syncthreads();
-    line_stage2<N0, -1>(v, t, [&](int tt, int k1) { return xb[(k1 * A0 + tt) * CW + cw]; });
+    line_stage2<N0, OpTraits<OP>::FIRST_DIR>(v, t, [&](int tt, int k1) { return xb[(k1 * A0 + tt) * CW + cw]; });
     frame_modulus_line<N0, N1, OP, A0, B0>(g, f, fbase, t, c, v, err);
     if constexpr (INVERSE) {
       line_stage1<N0, +1>(v, t, tw0);
@@ -209,6 +209,7 @@ static int launch_op(int op, const FrameArgs& a, int nframes, cudaStream_t st) {
     case OP_MERR: return launch_one<N0, N1, OP_MERR>(a, nframes, st);
     case OP_INTENS: return launch_one<N0, N1, OP_INTENS>(a, nframes, st);
     case OP_MERR_PSI: return launch_one<N0, N1, OP_MERR_PSI>(a, nframes, st);
+    case OP_BP: return launch_one<N0, N1, OP_BP>(a, nframes, st);
   }
   return set_error(PTY_ERR_ARG, "unknown frame op");
 }
@@ -225,6 +226,7 @@ static int prepare_shape() {
   if (!rc) rc = set_attr<N0, N1, OP_MERR>();
   if (!rc) rc = set_attr<N0, N1, OP_INTENS>();
   if (!rc) rc = set_attr<N0, N1, OP_MERR_PSI>();
+  if (!rc) rc = set_attr<N0, N1, OP_BP>();
   return rc;
 }
 

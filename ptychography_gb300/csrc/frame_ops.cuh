@@ -12,7 +12,10 @@ template <int OP>
 struct OpTraits {
   static constexpr bool IN_EXIT = (OP == OP_EXIT1 || OP == OP_EXIT7 || OP == OP_MERR || OP == OP_INTENS);
   static constexpr bool IN_DM = (OP == OP_DM1 || OP == OP_DM7);
-  static constexpr bool INVERSE = !(OP == OP_MERR || OP == OP_MERR_PSI || OP == OP_INTENS);
+  // a second (inverse) half after the column constraint
+  static constexpr bool INVERSE = !(OP == OP_MERR || OP == OP_MERR_PSI || OP == OP_INTENS || OP == OP_BP);
+  // direction of the first half: OP_BP is a single inverse transform
+  static constexpr int FIRST_DIR = (OP == OP_BP) ? +1 : -1;
 };
 
 // exit wave P * O[window] (era.py:426-433) at frame pixel (a, b).  Plan
@@ -24,7 +27,7 @@ PTY_DEV float2 exit_wave(const FrameArgs& g, int r0, int r1, int a, int b) {
 }
 
 template <int N1, int OP>
-PTY_DEV float2 frame_input(const FrameArgs& g, int r0, int r1, const float2* psi, int a, int b) {
+PTY_DEV float2 frame_input(const FrameArgs& g, int f, int r0, int r1, const float2* psi, int a, int b) {
   if constexpr (OpTraits<OP>::IN_EXIT) {
     return exit_wave<N1>(g, r0, r1, a, b);
   } else if constexpr (OpTraits<OP>::IN_DM) {
@@ -32,6 +35,15 @@ PTY_DEV float2 frame_input(const FrameArgs& g, int r0, int r1, const float2* psi
     const float2 ex0 = exit_wave<N1>(g, r0, r1, a, b);
     const float2 e1 = csub(psi[a * N1 + b], ex0);
     return csub(ex0, e1);
+  } else if constexpr (OP == OP_BP) {
+    // back_projection.py:74-77: mask * sqrt(I) * exp(i angle(fftn(P))), with the
+    // reference's centred-order amp and mask taken from the engine's unshifted
+    // buffers (ifftshift of an even length is a half-length roll), and g.P
+    // holding the unit phasors of fftn(P) in natural order
+    const int pa = (a + g.N0h) % (2 * g.N0h), pb = (b + g.N1h) % (2 * g.N1h);
+    const int pix = pa * N1 + pb;
+    const float m = g.mask ? (float)g.mask[pix] : 1.0f;
+    return cscale(__ldg(&g.P[a * N1 + b]), m * g.amp[(size_t)g.amp_stride * f + pix]);
   } else {
     return psi[a * N1 + b];
   }
@@ -51,6 +63,12 @@ PTY_DEV void frame_modulus_line(const FrameArgs& g, int f, size_t fbase, int t, 
       const int sr = (t + A * j + N0 / 2) % N0;
       g.out_real[fbase + (size_t)sr * N1 + sc] = cabs2(v[j]);
     }
+    return;
+  } else if constexpr (OP == OP_BP) {
+    // the inverse transform is complete: write psi, scaled 1 / (N0 N1) as ifftn
+    constexpr float kInv = 1.0f / (float)(N0 * N1);
+#pragma unroll
+    for (int j = 0; j < B; ++j) g.psi[fbase + (size_t)(t + A * j) * N1 + kc] = cscale(v[j], kInv);
     return;
   } else {
     constexpr bool BG_IN = (OP == OP_EXIT7 || OP == OP_PSI7 || OP == OP_MERR || OP == OP_MERR_PSI);

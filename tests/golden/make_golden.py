@@ -117,6 +117,16 @@ def main():
         ny=3, nx=2, random_offset=4, background=3, mask=8, counting_statistics=True)
     np.savez_compressed(os.path.join(HERE, "forward_sim_rect.npz"), I=I2, R=R2, M=M2, P=P2,
                         O=O2, B=B2, seed=4321)
+    # Back_projection (back_projection.py:4-88) on the base problem.  The probe
+    # is perturbed by seeded noise: forward_sim's band-limited pupil has exact
+    # spectral zeros whose angle() is rounding noise, which would make the
+    # back-projected phases depend on the FFT library's rounding.
+    rng = np.random.default_rng(21)
+    Pb = P * (1 + 0.1 * (rng.standard_normal(P.shape) + 1j * rng.standard_normal(P.shape)))
+    Rb = R.copy()
+    Ob, info_b = ref.back_projection.Back_projection(I, Rb, Pb, None, mask=M, alpha=1e-10)
+    np.savez_compressed(os.path.join(HERE, "back_projection.npz"), O=Ob, heatmap=info_b["heatmap"],
+                        exits=info_b["exits"], R_after=Rb, P=Pb)
     print("ops ...")
     np.savez_compressed(os.path.join(HERE, "ops.npz"), **make_ops(ref))
     print("runs ...")

@@ -15,6 +15,10 @@ Rewrites (each is a pure syntax/semantics port of Python 2 behaviour):
   * ``np.array(a.shape)/2``   -> ``//2`` (Python 2 integer division, probe centring)
   * ``np.array(zip(...))``    -> ``np.array(list(zip(...)))`` (forward_models.py:152)
   * the ``if __name__ == '__main__'`` tail is dropped (self-tests call undefined names)
+
+``back_projection.py`` calls ``era.psup_O_1``, which the reference never
+defines; ``era.psup_O`` (the object update with that signature) is bound under
+that name so the function can run.
 """
 import os
 import re
@@ -109,4 +113,6 @@ def load_reference():
     ns.era = _load("era")
     ns.dm = _load("dm")
     ns.forward_models = _load("forward_models")
+    ns.era.psup_O_1 = ns.era.psup_O
+    ns.back_projection = _load("back_projection")
     return ns

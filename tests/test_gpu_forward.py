@@ -36,3 +36,14 @@ def test_forward_sim_rect_default_shape():
     # Poisson draws of FP32 intensities agree with the FP64 ones except at most
     # where lam sits on a sampling boundary
     assert np.mean(I == d["I"]) > 0.999
+
+
+def test_back_projection_matches_reference():
+    d = np.load(os.path.join(GOLD, "back_projection.npz"))
+    p = np.load(os.path.join(GOLD, "forward_sim.npz"))
+    Rc = p["R"].copy()
+    O, info = pty.Back_projection(p["I"], Rc, d["P"], None, mask=p["M"])
+    assert np.array_equal(Rc, d["R_after"])
+    assert rel(info["exits"], d["exits"]) < 2e-6
+    assert rel(info["heatmap"], d["heatmap"]) < 1e-7
+    assert rel(O, d["O"]) < 2e-6

@@ -129,3 +129,14 @@ def test_runs_match_reference(case, problem, runs):
         assert _rel(info["heatmap"], g("heatmap")) < tol
     if name + "/background" in runs.files:
         assert _rel(info["background"], g("background")) < tol
+
+
+def test_back_projection_matches_reference(problem):
+    d = _load("back_projection.npz")
+    p = problem
+    Rc = p["R"].copy()
+    O, info = orc.Back_projection(p["I"], Rc, d["P"], None, mask=p["M"])
+    assert np.array_equal(Rc, d["R_after"])
+    assert _rel(O, d["O"]) < 1e-12
+    assert _rel(info["exits"], d["exits"]) < 1e-12
+    assert _rel(info["heatmap"], d["heatmap"]) < 1e-12
