@@ -1,8 +1,10 @@
-// 256 x 256 frames: one frame per 4-CTA thread-block cluster.
+// 256 x 256 and 512 x 512 frames: one frame per thread-block cluster.
 //
-// A 256^2 complex64 frame (512 KB) does not fit one SM's shared memory, so the
-// 2-D transform is distributed over a cluster of C = 4 CTAs (one per SM) and
-// the two transposes go through distributed shared memory instead of HBM:
+// A 256^2 complex64 frame (512 KB) or 512^2 frame (2 MB) does not fit one SM's
+// shared memory, so the 2-D transform is distributed over a cluster of C CTAs
+// (8 for 256^2, two per SM; 16 for 512^2, one per SM), each owning N / C rows
+// and N / C columns, and the two transposes go through distributed shared
+// memory instead of HBM:
 //
 //   1. CTA r forms its 64 rows of the input wave (exit wave, psi, or the DM
 //      combination), row-FFTs them, and stores each transformed row straight
@@ -54,10 +56,11 @@ struct ClusterCfg {
   static_assert(SMEM <= 227 * 1024, "shared memory budget");
   // the column pass exchanges through the (then idle) row scratch
   static_assert((size_t)N * CW <= RSCR, "column exchange fits the row scratch");
+  static constexpr int MINB = SMEM <= 113 * 1024 ? 2 : 1;   // CTAs per SM the budget allows
 };
 
 template <int N, int C, int OP>
-__global__ void __cluster_dims__(C, 1, 1) __launch_bounds__(ClusterCfg<N, C>::NT, 512 / ClusterCfg<N, C>::NT)
+__global__ void __launch_bounds__(ClusterCfg<N, C>::NT, ClusterCfg<N, C>::MINB)
     cluster_frame_kernel(FrameArgs g) {
   using K = ClusterCfg<N, C>;
   constexpr int A = K::A, B = K::B, CP = K::CP, RPC = K::RPC, CPC = K::CPC, RF = K::RF, CW = K::CW;
@@ -82,9 +85,8 @@ __global__ void __cluster_dims__(C, 1, 1) __launch_bounds__(ClusterCfg<N, C>::NT
   // (rows t + A j) and the exchange walk (rows A t + tt) of the A lanes of a
   // column land in distinct banks.
   auto cidx = [](int r, int cl) { return r * CP + cl + r / A; };
-  float2* rc[C];  // column buffers of every CTA of the cluster
-#pragma unroll
-  for (int q = 0; q < C; ++q) rc[q] = cluster.map_shared_rank(cbuf, q);
+  // column buffer of cluster rank q (q is a compile-time constant at every use)
+  auto rc = [&](int q) { return cluster.map_shared_rank(cbuf, q); };
 
   int r0 = 0, r1 = 0;
   if (OpTraits<OP>::IN_EXIT || OpTraits<OP>::IN_DM) {
@@ -113,7 +115,7 @@ __global__ void __cluster_dims__(C, 1, 1) __launch_bounds__(ClusterCfg<N, C>::NT
     line_stage2<N, OpTraits<OP>::FIRST_DIR>(v, t, [&](int tt, int k1) { return rs[k1 * (A + 1) + tt]; });
     // v[j] = X[a][t + A j]; column t + A j belongs to CTA j / JPC
 #pragma unroll
-    for (int j = 0; j < B; ++j) rc[j / JPC][cidx(a, t + A * (j % JPC))] = v[j];
+    for (int j = 0; j < B; ++j) rc(j / JPC)[cidx(a, t + A * (j % JPC))] = v[j];
   }
   cluster.sync();
 
@@ -160,7 +162,7 @@ __global__ void __cluster_dims__(C, 1, 1) __launch_bounds__(ClusterCfg<N, C>::NT
       const int a = rank * RPC + s * RF + lr;
       float2 v[B];
 #pragma unroll
-      for (int j = 0; j < B; ++j) v[j] = rc[j / JPC][cidx(a, t + A * (j % JPC))];
+      for (int j = 0; j < B; ++j) v[j] = rc(j / JPC)[cidx(a, t + A * (j % JPC))];
       line_stage1<N, +1>(v, t, tw);
       __syncwarp();
 #pragma unroll
@@ -183,57 +185,111 @@ __global__ void __cluster_dims__(C, 1, 1) __launch_bounds__(ClusterCfg<N, C>::NT
   }
 }
 
-constexpr int kClusterN = 256, kClusterC = 8;
+// 256 x 256 frames: 8-CTA clusters (two CTAs per SM); 512 x 512 frames:
+// 16-CTA clusters (non-portable size, one CTA per SM).
+template <int N>
+struct ClusterOf;
+template <> struct ClusterOf<256> { static constexpr int C = 8; };
+template <> struct ClusterOf<512> { static constexpr int C = 16; };
 
-template <int OP>
+template <int N, int OP>
 static int set_cluster_attr() {
-  using K = ClusterCfg<kClusterN, kClusterC>;
-  cudaError_t e = cudaFuncSetAttribute(cluster_frame_kernel<kClusterN, kClusterC, OP>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)K::SMEM);
-  if (e != cudaSuccess) return set_cuda_error(e, "cluster_frame_kernel smem attribute");
+  constexpr int C = ClusterOf<N>::C;
+  using K = ClusterCfg<N, C>;
+  auto fn = cluster_frame_kernel<N, C, OP>;
+  cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)K::SMEM);
+  if (e == cudaSuccess && C > 8) e = cudaFuncSetAttribute(fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+  if (e != cudaSuccess) return set_cuda_error(e, "cluster_frame_kernel attributes");
   return PTY_OK;
 }
 
-template <int OP>
+template <int N, int OP>
 static int launch_cluster(const FrameArgs& a, int nframes, cudaStream_t st) {
-  using K = ClusterCfg<kClusterN, kClusterC>;
-  cluster_frame_kernel<kClusterN, kClusterC, OP><<<nframes * kClusterC, K::NT, K::SMEM, st>>>(a);
+  constexpr int C = ClusterOf<N>::C;
+  using K = ClusterCfg<N, C>;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(nframes * C);
+  cfg.blockDim = dim3(K::NT);
+  cfg.dynamicSmemBytes = K::SMEM;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = C;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  cudaError_t e = cudaLaunchKernelEx(&cfg, cluster_frame_kernel<N, C, OP>, a);
+  if (e != cudaSuccess) return set_cuda_error(e, "cluster_frame_kernel launch");
   return check_launch("cluster_frame_kernel");
 }
 
-bool cluster_frame_supported() { return true; }
-
-int cluster_err_slots() { return kClusterC; }
-
-int prepare_cluster_frame_kernels() {
+template <int N>
+static int prepare_n() {
   int rc = PTY_OK;
-  if (!rc) rc = set_cluster_attr<OP_EXIT1>();
-  if (!rc) rc = set_cluster_attr<OP_EXIT7>();
-  if (!rc) rc = set_cluster_attr<OP_PSI1>();
-  if (!rc) rc = set_cluster_attr<OP_PSI7>();
-  if (!rc) rc = set_cluster_attr<OP_DM1>();
-  if (!rc) rc = set_cluster_attr<OP_DM7>();
-  if (!rc) rc = set_cluster_attr<OP_MERR>();
-  if (!rc) rc = set_cluster_attr<OP_INTENS>();
-  if (!rc) rc = set_cluster_attr<OP_MERR_PSI>();
-  if (!rc) rc = set_cluster_attr<OP_BP>();
-  return rc;
+  if (!rc) rc = set_cluster_attr<N, OP_EXIT1>();
+  if (!rc) rc = set_cluster_attr<N, OP_EXIT7>();
+  if (!rc) rc = set_cluster_attr<N, OP_PSI1>();
+  if (!rc) rc = set_cluster_attr<N, OP_PSI7>();
+  if (!rc) rc = set_cluster_attr<N, OP_DM1>();
+  if (!rc) rc = set_cluster_attr<N, OP_DM7>();
+  if (!rc) rc = set_cluster_attr<N, OP_MERR>();
+  if (!rc) rc = set_cluster_attr<N, OP_INTENS>();
+  if (!rc) rc = set_cluster_attr<N, OP_MERR_PSI>();
+  if (!rc) rc = set_cluster_attr<N, OP_BP>();
+  if (rc) return rc;
+  // refuse the shape when no cluster of this size can be resident on the GPU
+  constexpr int C = ClusterOf<N>::C;
+  using K = ClusterCfg<N, C>;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(C);
+  cfg.blockDim = dim3(K::NT);
+  cfg.dynamicSmemBytes = K::SMEM;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = C;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  int nclusters = 0;
+  cudaError_t e = cudaOccupancyMaxActiveClusters(&nclusters, cluster_frame_kernel<N, C, OP_PSI7>, &cfg);
+  if (e != cudaSuccess) return set_cuda_error(e, "cudaOccupancyMaxActiveClusters");
+  if (nclusters < 1) return set_error(PTY_ERR_UNSUPPORTED, "no cluster for this frame size fits the GPU");
+  return PTY_OK;
 }
 
-int launch_cluster_frame_op(int op, const FrameArgs& a, int nframes, cudaStream_t st) {
+template <int N>
+static int launch_n(int op, const FrameArgs& a, int nframes, cudaStream_t st) {
   switch (op) {
-    case OP_EXIT1: return launch_cluster<OP_EXIT1>(a, nframes, st);
-    case OP_EXIT7: return launch_cluster<OP_EXIT7>(a, nframes, st);
-    case OP_PSI1: return launch_cluster<OP_PSI1>(a, nframes, st);
-    case OP_PSI7: return launch_cluster<OP_PSI7>(a, nframes, st);
-    case OP_DM1: return launch_cluster<OP_DM1>(a, nframes, st);
-    case OP_DM7: return launch_cluster<OP_DM7>(a, nframes, st);
-    case OP_MERR: return launch_cluster<OP_MERR>(a, nframes, st);
-    case OP_INTENS: return launch_cluster<OP_INTENS>(a, nframes, st);
-    case OP_MERR_PSI: return launch_cluster<OP_MERR_PSI>(a, nframes, st);
-    case OP_BP: return launch_cluster<OP_BP>(a, nframes, st);
+    case OP_EXIT1: return launch_cluster<N, OP_EXIT1>(a, nframes, st);
+    case OP_EXIT7: return launch_cluster<N, OP_EXIT7>(a, nframes, st);
+    case OP_PSI1: return launch_cluster<N, OP_PSI1>(a, nframes, st);
+    case OP_PSI7: return launch_cluster<N, OP_PSI7>(a, nframes, st);
+    case OP_DM1: return launch_cluster<N, OP_DM1>(a, nframes, st);
+    case OP_DM7: return launch_cluster<N, OP_DM7>(a, nframes, st);
+    case OP_MERR: return launch_cluster<N, OP_MERR>(a, nframes, st);
+    case OP_INTENS: return launch_cluster<N, OP_INTENS>(a, nframes, st);
+    case OP_MERR_PSI: return launch_cluster<N, OP_MERR_PSI>(a, nframes, st);
+    case OP_BP: return launch_cluster<N, OP_BP>(a, nframes, st);
   }
   return set_error(PTY_ERR_ARG, "unknown frame op");
+}
+
+bool cluster_frame_supported(int N) { return N == 256 || N == 512; }
+
+int cluster_err_slots(int N) { return N == 512 ? ClusterOf<512>::C : ClusterOf<256>::C; }
+
+int prepare_cluster_frame_kernels(int N) {
+  if (N == 256) return prepare_n<256>();
+  if (N == 512) return prepare_n<512>();
+  return set_error(PTY_ERR_SHAPE, "no cluster kernel for this frame size");
+}
+
+int launch_cluster_frame_op(int N, int op, const FrameArgs& a, int nframes, cudaStream_t st) {
+  if (N == 256) return launch_n<256>(op, a, nframes, st);
+  if (N == 512) return launch_n<512>(op, a, nframes, st);
+  return set_error(PTY_ERR_SHAPE, "no cluster kernel for this frame size");
 }
 
 }  // namespace pty

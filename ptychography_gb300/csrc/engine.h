@@ -46,12 +46,14 @@ struct FrameArgs {
 bool frame_shape_supported(int N0, int N1);
 int prepare_frame_kernels(int N0, int N1);
 int launch_frame_op(int op, int N0, int N1, const FrameArgs& a, int nframes, cudaStream_t st);
-bool cluster_frame_supported();
-int launch_cluster_frame_op(int op, const FrameArgs& a, int nframes, cudaStream_t st);
-int prepare_cluster_frame_kernels();
-int cluster_err_slots();
+bool cluster_frame_supported(int N);
+int launch_cluster_frame_op(int N, int op, const FrameArgs& a, int nframes, cudaStream_t st);
+int prepare_cluster_frame_kernels(int N);
+int cluster_err_slots(int N);
 // error-partial slots each frame writes (one per CTA working on it)
-inline int frame_err_slots(int N0, int N1) { return (N0 == 256 && N1 == 256) ? cluster_err_slots() : 1; }
+inline int frame_err_slots(int N0, int N1) {
+  return (N0 == N1 && (N0 == 256 || N0 == 512)) ? cluster_err_slots(N0) : 1;
+}
 
 // error reporting (engine.cu)
 int set_error(int code, const char* msg);

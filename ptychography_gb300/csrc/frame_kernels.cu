@@ -235,13 +235,13 @@ int prepare_frame_kernels(int N0, int N1) {
   if (N0 == 64 && N1 == 64) return prepare_shape<64, 64>();
   if (N0 == 128 && N1 == 128) return prepare_shape<128, 128>();
   if (N0 == 32 && N1 == 64) return prepare_shape<32, 64>();
-  if (N0 == 256 && N1 == 256) return prepare_cluster_frame_kernels();
+  if (N0 == N1 && cluster_frame_supported(N0)) return prepare_cluster_frame_kernels(N0);
   return set_error(PTY_ERR_SHAPE, "frame shape not supported by the fused FFT kernels");
 }
 
 bool frame_shape_supported(int N0, int N1) {
   auto ok = [](int n) { return n == 32 || n == 64 || n == 128; };
-  if (N0 == 256 && N1 == 256) return cluster_frame_supported();
+  if (N0 == N1 && cluster_frame_supported(N0)) return true;
   return ok(N0) && ok(N1) && (N0 == N1 || (N0 == 32 && N1 == 64));
 }
 
@@ -251,7 +251,7 @@ int launch_frame_op(int op, int N0, int N1, const FrameArgs& a, int nframes, cud
   if (N0 == 64 && N1 == 64) return launch_op<64, 64>(op, a, nframes, st);
   if (N0 == 128 && N1 == 128) return launch_op<128, 128>(op, a, nframes, st);
   if (N0 == 32 && N1 == 64) return launch_op<32, 64>(op, a, nframes, st);
-  if (N0 == 256 && N1 == 256) return launch_cluster_frame_op(op, a, nframes, st);
+  if (N0 == N1 && cluster_frame_supported(N0)) return launch_cluster_frame_op(N0, op, a, nframes, st);
   return set_error(PTY_ERR_UNSUPPORTED, "frame shape not supported by the fused FFT kernels");
 }
 
