@@ -86,6 +86,16 @@ int pty_era(pty_plan* plan, const pty_buffers* buf, const pty_options* opt, int3
 int pty_dm(pty_plan* plan, const pty_buffers* buf, const pty_options* opt, int32_t iters,
            int32_t* heatmap_valid, void* stream);
 
+/* Many independent reconstructions at once: the batched form of pty_era
+ * (kind 0) or pty_dm (kind 1), for nrec distinct plans with their own buffers
+ * and options.  No reference counterpart (the reference runs one
+ * reconstruction per call).  All loops are captured into one CUDA graph with
+ * one branch per reconstruction, launched once; heatmap_valid (host, nrec
+ * entries) as in pty_era. */
+int pty_run_batch(int32_t kind, pty_plan* const* plans, const pty_buffers* bufs,
+                  const pty_options* opts, int32_t nrec, int32_t iters, int32_t* heatmap_valid,
+                  void* stream);
+
 /* Single operators (each replaces the reference function it names). */
 /* make_exits, era.py:426-433 */
 int pty_make_exits(pty_plan* plan, const void* O, const void* P, void* psi, void* stream);

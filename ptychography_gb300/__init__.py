@@ -10,10 +10,10 @@ C ABI in include/ptycho_gb300.h); Python prepares inputs and returns outputs.
 """
 from . import back_projection, dm, era, forward_models  # noqa: F401
 from .back_projection import Back_projection
-from .dm import DM
-from .era import ERA
+from .dm import DM, DM_batch
+from .era import ERA, ERA_batch
 from .forward_models import forward_sim
 
-__all__ = ["ERA", "DM", "forward_sim", "Back_projection", "era", "dm", "forward_models",
+__all__ = ["ERA", "DM", "ERA_batch", "DM_batch", "forward_sim", "Back_projection", "era", "dm", "forward_models",
            "back_projection"]
 __version__ = "0.1.0"

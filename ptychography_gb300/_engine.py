@@ -118,73 +118,78 @@ def _ptr(t):
     return ctypes.c_void_p(t.data_ptr()) if t is not None else None
 
 
-def run(kind, I, R, P, O, iters, OP_iters, mask, background, method, Pmod_probe,
-        probe_centering, alpha, dtype, full_output, use_graph=True):
-    """Run ERA (kind='era') or DM (kind='dm') on the GPU; return the reference's outputs."""
-    torch = _torch()
-    lib = _native.load()
-    pre = Preamble(I, R, P, O, OP_iters, mask, background, method, dtype)
-    iters = int(iters)
-    dev = torch.device("cuda", torch.cuda.current_device())
-    n, N0, N1 = pre.n, pre.N0, pre.N1
-    U, V = pre.O.shape
+class _Job:
+    """One reconstruction's plan and device buffers (era.py:435-548 set-up on the GPU)."""
 
-    geom = _native.Geometry(n, N0, N1, U, V)
-    R64 = np.ascontiguousarray(pre.R[:, :2], dtype=np.int64)
-    plan = ctypes.c_void_p()
-    _native.check(lib.pty_plan_create(ctypes.byref(geom),
-                                      R64.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)),
-                                      ctypes.byref(plan)))
-    try:
-        stream = torch.cuda.current_stream(dev)
-        sp = ctypes.c_void_p(stream.cuda_stream)
-        Iin = pre.I
-        if Iin.dtype not in (np.float32, np.float64):
-            Iin = Iin.astype(np.float64)
-        I_d = torch.from_numpy(np.ascontiguousarray(Iin)).to(dev, non_blocking=False)
-        amp = torch.empty((n, N0, N1), dtype=torch.float32, device=dev)
-        _native.check(lib.pty_amp_from_intensity(plan, _ptr(I_d), int(Iin.dtype == np.float64),
-                                                 _ptr(amp), sp))
-        del I_d
-        O_d = torch.from_numpy(np.ascontiguousarray(pre.O.astype(np.complex64))).to(dev)
-        P_d = torch.from_numpy(np.ascontiguousarray(pre.P.astype(np.complex64))).to(dev)
-        psi = torch.empty((n, N0, N1), dtype=torch.complex64, device=dev)
-        mask_d = torch.from_numpy(pre.mask).to(dev) if pre.mask is not None else None
-        bg_d = torch.from_numpy(pre.background).to(dev) if pre.background is not None else None
-        npm = pmod_probe_count(Pmod_probe, iters)
-        Pamp_d = torch.from_numpy(pre.Pamp).to(dev) if npm > 0 else None
-        bmean = torch.zeros((N0, N1), dtype=torch.float32, device=dev) if bg_d is not None else None
-        heat = torch.zeros((U, V), dtype=torch.float64, device=dev)
-        inten = (torch.empty((n, N0, N1), dtype=torch.float32, device=dev)
-                 if full_output and iters > 0 else None)
-        emod = torch.zeros(max(iters, 1), dtype=torch.float64, device=dev)
-        econ = torch.zeros(max(iters, 1), dtype=torch.float64, device=dev)
+    def __init__(self, lib, dev, sp, kind, I, R, P, O, iters, OP_iters, mask, background, method,
+                 Pmod_probe, probe_centering, alpha, dtype, full_output, use_graph):
+        torch = _torch()
+        self.lib, self.kind, self.full_output = lib, kind, full_output
+        pre = self.pre = Preamble(I, R, P, O, OP_iters, mask, background, method, dtype)
+        self.iters = iters = int(iters)
+        n, N0, N1 = pre.n, pre.N0, pre.N1
+        U, V = pre.O.shape
+        geom = _native.Geometry(n, N0, N1, U, V)
+        R64 = np.ascontiguousarray(pre.R[:, :2], dtype=np.int64)
+        self.plan = ctypes.c_void_p()
+        _native.check(lib.pty_plan_create(ctypes.byref(geom),
+                                          R64.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)),
+                                          ctypes.byref(self.plan)))
+        try:
+            Iin = pre.I
+            if Iin.dtype not in (np.float32, np.float64):
+                Iin = Iin.astype(np.float64)
+            I_d = torch.from_numpy(np.ascontiguousarray(Iin)).to(dev, non_blocking=False)
+            amp = torch.empty((n, N0, N1), dtype=torch.float32, device=dev)
+            _native.check(lib.pty_amp_from_intensity(self.plan, _ptr(I_d),
+                                                     int(Iin.dtype == np.float64), _ptr(amp), sp))
+            del I_d
+            self.O_d = torch.from_numpy(np.ascontiguousarray(pre.O.astype(np.complex64))).to(dev)
+            self.P_d = torch.from_numpy(np.ascontiguousarray(pre.P.astype(np.complex64))).to(dev)
+            psi = torch.empty((n, N0, N1), dtype=torch.complex64, device=dev)
+            mask_d = torch.from_numpy(pre.mask).to(dev) if pre.mask is not None else None
+            bg_d = torch.from_numpy(pre.background).to(dev) if pre.background is not None else None
+            npm = pmod_probe_count(Pmod_probe, iters)
+            Pamp_d = torch.from_numpy(pre.Pamp).to(dev) if npm > 0 else None
+            self.bmean = (torch.zeros((N0, N1), dtype=torch.float32, device=dev)
+                          if bg_d is not None else None)
+            self.heat = torch.zeros((U, V), dtype=torch.float64, device=dev)
+            self.inten = (torch.empty((n, N0, N1), dtype=torch.float32, device=dev)
+                          if full_output and iters > 0 else None)
+            self.emod = torch.zeros(max(iters, 1), dtype=torch.float64, device=dev)
+            self.econ = torch.zeros(max(iters, 1), dtype=torch.float64, device=dev)
+            # keep every buffer the library writes alive for the job's lifetime
+            self._keep = (amp, psi, mask_d, bg_d, Pamp_d)
+            self.buf = _native.Buffers(_ptr(self.O_d), _ptr(self.P_d), _ptr(psi), _ptr(amp),
+                                       _ptr(mask_d), _ptr(bg_d), _ptr(Pamp_d), _ptr(self.bmean),
+                                       _ptr(self.heat), _ptr(self.inten), _ptr(self.emod),
+                                       _ptr(self.econ))
+            self.opt = _native.Options(pre.method, pre.OP_iters[0], pre.OP_iters[1], npm,
+                                       int(bool(probe_centering)), int(bool(use_graph)),
+                                       float(alpha), pre.I_norm)
+        except BaseException:
+            self.close()
+            raise
+        self.heat_valid = 0
 
-        buf = _native.Buffers(_ptr(O_d), _ptr(P_d), _ptr(psi), _ptr(amp), _ptr(mask_d), _ptr(bg_d),
-                              _ptr(Pamp_d), _ptr(bmean), _ptr(heat), _ptr(inten), _ptr(emod),
-                              _ptr(econ))
-        opt = _native.Options(pre.method, pre.OP_iters[0], pre.OP_iters[1], npm,
-                              int(bool(probe_centering)), int(bool(use_graph)), float(alpha),
-                              pre.I_norm)
-        hv = ctypes.c_int32(0)
-        fn = lib.pty_era if kind == "era" else lib.pty_dm
-        _native.check(fn(plan, ctypes.byref(buf), ctypes.byref(opt), iters, ctypes.byref(hv), sp))
-        stream.synchronize()
-
-        O_out = O_d.cpu().numpy().astype(pre.cdt)
-        P_out = P_d.cpu().numpy().astype(pre.cdt)
+    def outputs(self):
+        """The reference's return value (era.py:300-332 / dm.py:300-333)."""
+        pre, kind, iters = self.pre, self.kind, self.iters
+        O_out = self.O_d.cpu().numpy().astype(pre.cdt)
+        P_out = self.P_d.cpu().numpy().astype(pre.cdt)
         upd = pre.update
-        if not full_output:
+        if not self.full_output:
             return O_out if upd == "O" else P_out if upd == "P" else (O_out, P_out)
         rt = pre.rdt
         info = {
-            "I": inten.cpu().numpy().astype(rt) if inten is not None else None,
-            "eMod": [rt(x) for x in emod.cpu().numpy()[:iters]],
-            "eCon": [rt(x) for x in econ.cpu().numpy()[:iters]],
-            "heatmap": heat.cpu().numpy().astype(rt) if (hv.value and upd != "P") else None,
+            "I": self.inten.cpu().numpy().astype(rt) if self.inten is not None else None,
+            "eMod": [rt(x) for x in self.emod.cpu().numpy()[:iters]],
+            "eCon": [rt(x) for x in self.econ.cpu().numpy()[:iters]],
+            "heatmap": (self.heat.cpu().numpy().astype(rt)
+                        if (self.heat_valid and upd != "P") else None),
         }
-        if bmean is not None:
-            info["background"] = (np.fft.fftshift(bmean.cpu().numpy()) ** 2).astype(rt)
+        if self.bmean is not None:
+            info["background"] = (np.fft.fftshift(self.bmean.cpu().numpy()) ** 2).astype(rt)
         elif kind == "era" and pre.user_background is not None:
             b = np.asarray(pre.user_background)                   # era.py:311-314
             info["background"] = np.fft.fftshift(b[0] if b.ndim == 3 else b) ** 2
@@ -193,5 +198,86 @@ def run(kind, I, R, P, O, iters, OP_iters, mask, background, method, Pmod_probe,
         if upd == "P":
             return P_out, info
         return O_out, P_out, info
+
+    def close(self):
+        if self.plan:
+            self.lib.pty_plan_destroy(self.plan)
+            self.plan = ctypes.c_void_p()
+
+
+def run(kind, I, R, P, O, iters, OP_iters, mask, background, method, Pmod_probe,
+        probe_centering, alpha, dtype, full_output, use_graph=True):
+    """Run ERA (kind='era') or DM (kind='dm') on the GPU; return the reference's outputs."""
+    torch = _torch()
+    lib = _native.load()
+    dev = torch.device("cuda", torch.cuda.current_device())
+    stream = torch.cuda.current_stream(dev)
+    sp = ctypes.c_void_p(stream.cuda_stream)
+    job = _Job(lib, dev, sp, kind, I, R, P, O, iters, OP_iters, mask, background, method,
+               Pmod_probe, probe_centering, alpha, dtype, full_output, use_graph)
+    try:
+        hv = ctypes.c_int32(0)
+        fn = lib.pty_era if kind == "era" else lib.pty_dm
+        _native.check(fn(job.plan, ctypes.byref(job.buf), ctypes.byref(job.opt), job.iters,
+                         ctypes.byref(hv), sp))
+        stream.synchronize()
+        job.heat_valid = hv.value
+        return job.outputs()
     finally:
-        lib.pty_plan_destroy(plan)
+        job.close()
+
+
+_PROBLEM_KEYS = ("I", "R", "P", "O", "mask", "background", "method", "OP_iters", "Pmod_probe",
+                 "probe_centering", "alpha", "dtype")
+
+
+def run_batch(kind, problems, iters, defaults):
+    """Many independent reconstructions in one graph launch (pty_run_batch).
+
+    ``problems``: a sequence of dicts with the per-problem arguments of ERA/DM
+    (``I``, ``R``, ``P``, ``O`` and optionally any of ``mask``, ``background``,
+    ``method``, ``OP_iters``, ``Pmod_probe``, ``probe_centering``, ``alpha``,
+    ``dtype``), or of ``(I, R, P, O)`` tuples.  ``defaults`` supplies the
+    arguments a problem leaves out.  Preambles run in list order, so NumPy's
+    global RNG is drawn exactly as by the same ERA/DM calls made one after
+    another; ``R`` arrays are shifted in place as the single call does.
+    Returns the list of per-problem return values.
+    """
+    torch = _torch()
+    lib = _native.load()
+    dev = torch.device("cuda", torch.cuda.current_device())
+    stream = torch.cuda.current_stream(dev)
+    sp = ctypes.c_void_p(stream.cuda_stream)
+    jobs = []
+    try:
+        for prob in problems:
+            if not isinstance(prob, dict):
+                I, R, P, O = prob
+                prob = {"I": I, "R": R, "P": P, "O": O}
+            unknown = set(prob) - set(_PROBLEM_KEYS)
+            if unknown:
+                raise ValueError("unknown problem keys: %s" % sorted(unknown))
+            a = dict(defaults)
+            a.update(prob)
+            jobs.append(_Job(lib, dev, sp, kind, a["I"], a["R"], a.get("P"), a.get("O"), iters,
+                             a["OP_iters"], a["mask"], a["background"], a["method"],
+                             a["Pmod_probe"], a["probe_centering"], a["alpha"], a["dtype"],
+                             a["full_output"], True))
+        if not jobs:
+            return []
+        nrec = len(jobs)
+        plans = (ctypes.c_void_p * nrec)(*[j.plan.value for j in jobs])
+        bufs = (_native.Buffers * nrec)(*[j.buf for j in jobs])
+        opts = (_native.Options * nrec)(*[j.opt for j in jobs])
+        hv = (ctypes.c_int32 * nrec)()
+        _native.check(lib.pty_run_batch(0 if kind == "era" else 1, plans, bufs, opts, nrec,
+                                        int(iters), hv, sp))
+        stream.synchronize()
+        out = []
+        for j, h in zip(jobs, hv):
+            j.heat_valid = h
+            out.append(j.outputs())
+        return out
+    finally:
+        for j in jobs:
+            j.close()

@@ -39,6 +39,8 @@ SIGNATURES = {
                 ctypes.POINTER(c_int32), c_void_p],
     "pty_dm": [c_void_p, ctypes.POINTER(Buffers), ctypes.POINTER(Options), c_int32,
                ctypes.POINTER(c_int32), c_void_p],
+    "pty_run_batch": [c_int32, ctypes.POINTER(c_void_p), ctypes.POINTER(Buffers), ctypes.POINTER(Options),
+                      c_int32, c_int32, ctypes.POINTER(c_int32), c_void_p],
     "pty_make_exits": [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p],
     "pty_pmod_1": [c_void_p, c_void_p, c_void_p, c_void_p, c_double, c_void_p, c_void_p],
     "pty_pmod_7": [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_double, c_void_p, c_void_p],

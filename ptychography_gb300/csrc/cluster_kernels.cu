@@ -41,7 +41,8 @@ PTY_DEV void cluster_sync_relaxed() {
 template <int N, int C>
 struct ClusterCfg {
   static constexpr int A = LineGeom<N>::A, B = LineGeom<N>::B;  // rows and columns alike
-  static constexpr int NT = C >= 8 ? 256 : 512;      // 8-CTA clusters: two CTAs per SM
+  // 8- and 16-CTA clusters and 192^2 frames: 256 threads per CTA
+  static constexpr int NT = (C >= 8 || N == 192) ? 256 : 512;
   static constexpr int RPC = N / C;          // rows owned per CTA
   static constexpr int CPC = N / C;          // columns owned per CTA
   static constexpr int CP = CPC + 1;         // column-buffer pitch (float2), odd
@@ -189,6 +190,7 @@ __global__ void __launch_bounds__(ClusterCfg<N, C>::NT, ClusterCfg<N, C>::MINB)
 // 16-CTA clusters (non-portable size, one CTA per SM).
 template <int N>
 struct ClusterOf;
+template <> struct ClusterOf<192> { static constexpr int C = 2; };
 template <> struct ClusterOf<256> { static constexpr int C = 8; };
 template <> struct ClusterOf<512> { static constexpr int C = 16; };
 
@@ -276,17 +278,21 @@ static int launch_n(int op, const FrameArgs& a, int nframes, cudaStream_t st) {
   return set_error(PTY_ERR_ARG, "unknown frame op");
 }
 
-bool cluster_frame_supported(int N) { return N == 256 || N == 512; }
+bool cluster_frame_supported(int N) { return N == 192 || N == 256 || N == 512; }
 
-int cluster_err_slots(int N) { return N == 512 ? ClusterOf<512>::C : ClusterOf<256>::C; }
+int cluster_err_slots(int N) {
+  return N == 512 ? ClusterOf<512>::C : N == 192 ? ClusterOf<192>::C : ClusterOf<256>::C;
+}
 
 int prepare_cluster_frame_kernels(int N) {
+  if (N == 192) return prepare_n<192>();
   if (N == 256) return prepare_n<256>();
   if (N == 512) return prepare_n<512>();
   return set_error(PTY_ERR_SHAPE, "no cluster kernel for this frame size");
 }
 
 int launch_cluster_frame_op(int N, int op, const FrameArgs& a, int nframes, cudaStream_t st) {
+  if (N == 192) return launch_n<192>(op, a, nframes, st);
   if (N == 256) return launch_n<256>(op, a, nframes, st);
   if (N == 512) return launch_n<512>(op, a, nframes, st);
   return set_error(PTY_ERR_SHAPE, "no cluster kernel for this frame size");

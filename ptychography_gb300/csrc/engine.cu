@@ -74,7 +74,7 @@ struct pty_plan {
   float2* d_mean_part = nullptr;
   double* d_err_part = nullptr;  // [n * eslots]
   int eslots = 1;                // error partials per frame
-  int ndn = 64;                  // diffnorm blocks per array
+  int ndn = 304;                 // diffnorm blocks per array (two per SM)
   double* d_dn_part = nullptr;   // [2 arrays][ndn][2]
   int* d_shift = nullptr;
   float2* d_bakO = nullptr;
@@ -96,6 +96,7 @@ struct pty_plan {
     int heat_valid = 0;
     long long kernels = 0;
   } graphs[2];
+  cudaGraphExec_t batch_exec = nullptr;   // last batch graph launched from this plan
   std::vector<void*> allocs;
 };
 
@@ -122,6 +123,7 @@ static void twiddles(int L, std::vector<float2>& out) {
     case 32: A = 4; B = 8; break;
     case 64: A = 8; B = 8; break;
     case 128: A = 8; B = 16; break;
+    case 192: A = 8; B = 24; break;
     case 256: A = 16; B = 16; break;
     default: A = 16; B = 32; break;
   }
@@ -152,6 +154,7 @@ extern "C" int pty_plan_destroy(pty_plan* p) {
   if (p->d_psi_tmp) cudaFree(p->d_psi_tmp);
   for (auto& cg : p->graphs)
     if (cg.exec) cudaGraphExecDestroy(cg.exec);
+  if (p->batch_exec) cudaGraphExecDestroy(p->batch_exec);
   if (p->cap) cudaStreamDestroy(p->cap);
   if (p->ev_in) cudaEventDestroy(p->ev_in);
   if (p->ev_out) cudaEventDestroy(p->ev_out);
@@ -402,20 +405,27 @@ static int update_mask(int method) {  // 1 = O, 2 = P, 3 = OP
 }
 
 // ------------------------------------------------------------------ ERA
-extern "C" int pty_era(pty_plan* p, const pty_buffers* b, const pty_options* o, int32_t iters,
-                       int32_t* heatmap_valid, void* stream) {
+static int era_prepare(pty_plan* p, const pty_buffers* b, const pty_options* o, int iters) {
   PTY_TRY(validate_run(p, b, o, iters));
+  const size_t npix = (size_t)p->N0 * p->N1;
+  if (o->method >= 4 && !p->d_bgf) PTY_TRY(dalloc_t(p, &p->d_bgf, (size_t)p->n * npix));
+  return PTY_OK;
+}
+
+// The ERA loop (era.py:13-332) on stream st.  heatP_valid ends as the state of
+// the reference's P_heatmap (false where it would be None).
+static int era_body(pty_plan* p, const pty_buffers* b, const pty_options* o, int iters,
+                    bool& heatP_valid, cudaStream_t st) {
   const int upd = update_mask(o->method);
   const bool use_bg = o->method >= 4;
   const size_t nobj = (size_t)p->U * p->V, npix = (size_t)p->N0 * p->N1;
   const float alpha = (float)o->alpha;
-  if (use_bg && !p->d_bgf) PTY_TRY(dalloc_t(p, &p->d_bgf, (size_t)p->n * npix));
   float2* O = (float2*)b->O;
   float2* P = (float2*)b->P;
   float2* psi = (float2*)b->psi;
-  bool heatP_valid = false, heatO_valid = false;
+  heatP_valid = false;
+  bool heatO_valid = false;
 
-  auto body = [&](cudaStream_t st) -> int {
     for (int i = 0; i < iters; ++i) {
       if (upd & 1) PTY_TRY(copy_d2d(p->d_bakO, O, nobj * sizeof(float2), st));
       if (upd & 2) PTY_TRY(copy_d2d(p->d_bakP, P, npix * sizeof(float2), st));
@@ -479,7 +489,13 @@ extern "C" int pty_era(pty_plan* p, const pty_buffers* b, const pty_options* o, 
       PTY_TRY(copy_d2d(b->background_mean, src, npix * sizeof(float), st));
     }
     return PTY_OK;
-  };
+}
+
+extern "C" int pty_era(pty_plan* p, const pty_buffers* b, const pty_options* o, int32_t iters,
+                       int32_t* heatmap_valid, void* stream) {
+  PTY_TRY(era_prepare(p, b, o, iters));
+  bool heatP_valid = false;
+  auto body = [&](cudaStream_t st) -> int { return era_body(p, b, o, iters, heatP_valid, st); };
   int rc = run_on_stream(p, (cudaStream_t)stream, o->use_graph != 0, request_key('E', b, o, iters),
                          body, heatP_valid);
   if (heatmap_valid) *heatmap_valid = heatP_valid ? 1 : 0;
@@ -487,14 +503,10 @@ extern "C" int pty_era(pty_plan* p, const pty_buffers* b, const pty_options* o, 
 }
 
 // ------------------------------------------------------------------ DM
-extern "C" int pty_dm(pty_plan* p, const pty_buffers* b, const pty_options* o, int32_t iters,
-                      int32_t* heatmap_valid, void* stream) {
+static int dm_prepare(pty_plan* p, const pty_buffers* b, const pty_options* o, int iters) {
   PTY_TRY(validate_run(p, b, o, iters));
-  const int upd = update_mask(o->method);
-  const bool use_bg = o->method >= 4;
-  const size_t nobj = (size_t)p->U * p->V, npix = (size_t)p->N0 * p->N1;
-  const float alpha = (float)o->alpha;
-  if (o->probe_centering && upd == 3 && !p->d_psi_tmp) {
+  const size_t npix = (size_t)p->N0 * p->N1;
+  if (o->probe_centering && update_mask(o->method) == 3 && !p->d_psi_tmp) {
     cudaError_t e = cudaMalloc(&p->d_psi_tmp, (size_t)p->n * npix * sizeof(float2));
     if (e != cudaSuccess) {
       cudaGetLastError();
@@ -502,16 +514,27 @@ extern "C" int pty_dm(pty_plan* p, const pty_buffers* b, const pty_options* o, i
       return set_error(PTY_ERR_NOMEM, "DM centring scratch allocation failed");
     }
   }
+  return PTY_OK;
+}
+
+// The DM loop (dm.py:13-333) on stream st.
+static int dm_body(pty_plan* p, const pty_buffers* b, const pty_options* o, int iters,
+                   bool& heatP_valid, cudaStream_t st) {
+  const int upd = update_mask(o->method);
+  const bool use_bg = o->method >= 4;
+  const size_t nobj = (size_t)p->U * p->V, npix = (size_t)p->N0 * p->N1;
+  const float alpha = (float)o->alpha;
   float2* O = (float2*)b->O;
   float2* P = (float2*)b->P;
   float2* psi = (float2*)b->psi;
   float* bg = b->background;
-  bool heatP_valid = false, heatO_valid = false;
+  heatP_valid = false;
+  bool heatO_valid = false;
   const int n = p->n, N0 = p->N0, N1 = p->N1, U = p->U, V = p->V;
   const int* R = p->d_R;
 
-  auto body = [&](cudaStream_t st) -> int {
-    PTY_TRY(launch_make_exits(n, N0, N1, U, V, R, O, P, psi, st));  // era.py:536
+    // era.py:536: psi = P * O[R]; methods 4-6 form it inside their first Pmod_7 pass
+    if (!use_bg || iters == 0) PTY_TRY(launch_make_exits(n, N0, N1, U, V, R, O, P, psi, st));
     if (upd & 1) PTY_TRY(copy_d2d(p->d_bakO, O, nobj * sizeof(float2), st));  // dm.py:35-38
     if (upd & 2) PTY_TRY(copy_d2d(p->d_bakP, P, npix * sizeof(float2), st));
     for (int i = 0; i < iters; ++i) {
@@ -524,7 +547,13 @@ extern "C" int pty_dm(pty_plan* p, const pty_buffers* b, const pty_options* o, i
         a.bg_in = bg;
         a.bg_stride = (long long)npix;
         a.bg_out = bg;
-        PTY_TRY(frame_op(p, OP_PSI7, a, n, st));
+        if (i == 0) {  // exits straight from P * O[R] (era.py:536), same values
+          a.O = O;
+          a.P = P;
+          PTY_TRY(frame_op(p, OP_EXIT7, a, n, st));
+        } else {
+          PTY_TRY(frame_op(p, OP_PSI7, a, n, st));
+        }
       }
       // main consistency projection (dm.py:56-85)
       if (upd == 1) {
@@ -621,10 +650,90 @@ extern "C" int pty_dm(pty_plan* p, const pty_buffers* b, const pty_options* o, i
     if (use_bg && b->background_mean && iters > 0)
       PTY_TRY(copy_d2d(b->background_mean, p->d_b0, npix * sizeof(float), st));
     return PTY_OK;
-  };
+}
+
+extern "C" int pty_dm(pty_plan* p, const pty_buffers* b, const pty_options* o, int32_t iters,
+                      int32_t* heatmap_valid, void* stream) {
+  PTY_TRY(dm_prepare(p, b, o, iters));
+  bool heatP_valid = false;
+  auto body = [&](cudaStream_t st) -> int { return dm_body(p, b, o, iters, heatP_valid, st); };
   int rc = run_on_stream(p, (cudaStream_t)stream, o->use_graph != 0, request_key('D', b, o, iters),
                          body, heatP_valid);
   if (heatmap_valid) *heatmap_valid = heatP_valid ? 1 : 0;
+  return rc;
+}
+
+// ------------------------------------------------------------------ batches
+// Independent reconstructions in one CUDA graph: each plan's loop is captured
+// on that plan's own stream, forked from and joined to the first plan's
+// stream, so the graph holds one branch per reconstruction and the GPU runs
+// the branches concurrently.
+extern "C" int pty_run_batch(int32_t kind, pty_plan* const* plans, const pty_buffers* bufs,
+                             const pty_options* opts, int32_t nrec, int32_t iters,
+                             int32_t* heatmap_valid, void* stream) {
+  if (!plans || !bufs || !opts || nrec < 1) return set_error(PTY_ERR_ARG, "empty batch");
+  if (kind != 0 && kind != 1) return set_error(PTY_ERR_ARG, "kind must be 0 (ERA) or 1 (DM)");
+  for (int r = 0; r < nrec; ++r) {
+    for (int q = 0; q < r; ++q)
+      if (plans[q] == plans[r]) return set_error(PTY_ERR_ARG, "a plan appears twice in the batch");
+    PTY_TRY(kind == 0 ? era_prepare(plans[r], &bufs[r], &opts[r], iters)
+                      : dm_prepare(plans[r], &bufs[r], &opts[r], iters));
+  }
+  pty_plan* p0 = plans[0];
+  cudaStream_t master = p0->cap, user = (cudaStream_t)stream;
+  std::vector<bool> hv(nrec, false);
+  cudaEvent_t fork = nullptr;
+  PTY_CUDA(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming));
+  int rc = PTY_OK;
+  cudaGraph_t g = nullptr;
+  cudaError_t e = cudaEventRecord(p0->ev_in, user);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(master, p0->ev_in, 0);
+  if (e == cudaSuccess) e = cudaStreamBeginCapture(master, cudaStreamCaptureModeThreadLocal);
+  if (e != cudaSuccess) rc = set_cuda_error(e, "batch capture");
+  bool capturing = (rc == PTY_OK);
+  if (rc == PTY_OK) {
+    e = cudaEventRecord(fork, master);
+    if (e != cudaSuccess) rc = set_cuda_error(e, "batch fork");
+  }
+  for (int r = 0; rc == PTY_OK && r < nrec; ++r) {
+    cudaStream_t st = (r == 0) ? master : plans[r]->cap;
+    if (r > 0 && (e = cudaStreamWaitEvent(st, fork, 0)) != cudaSuccess) {
+      rc = set_cuda_error(e, "batch fork wait");
+      break;
+    }
+    bool h = false;
+    rc = kind == 0 ? era_body(plans[r], &bufs[r], &opts[r], iters, h, st)
+                   : dm_body(plans[r], &bufs[r], &opts[r], iters, h, st);
+    hv[r] = h;
+    if (rc == PTY_OK && r > 0) {
+      e = cudaEventRecord(plans[r]->ev_out, st);
+      if (e == cudaSuccess) e = cudaStreamWaitEvent(master, plans[r]->ev_out, 0);
+      if (e != cudaSuccess) rc = set_cuda_error(e, "batch join");
+    }
+  }
+  if (capturing) {
+    e = cudaStreamEndCapture(master, &g);
+    if (rc == PTY_OK && e != cudaSuccess) rc = set_cuda_error(e, "batch end capture");
+  }
+  if (rc == PTY_OK) {
+    cudaGraphExec_t ge = nullptr;
+    e = cudaGraphInstantiate(&ge, g, 0);
+    if (e == cudaSuccess) e = cudaGraphLaunch(ge, master);
+    if (e != cudaSuccess) {
+      rc = set_cuda_error(e, "batch graph launch");
+      if (ge) cudaGraphExecDestroy(ge);
+    } else {
+      // kept alive until the plan is destroyed or runs the next batch
+      if (p0->batch_exec) cudaGraphExecDestroy(p0->batch_exec);
+      p0->batch_exec = ge;
+    }
+  }
+  if (g) cudaGraphDestroy(g);
+  cudaEventRecord(p0->ev_out, master);
+  cudaStreamWaitEvent(user, p0->ev_out, 0);
+  cudaEventDestroy(fork);
+  if (heatmap_valid)
+    for (int r = 0; r < nrec; ++r) heatmap_valid[r] = hv[r] ? 1 : 0;
   return rc;
 }
 

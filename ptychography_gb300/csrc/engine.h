@@ -52,7 +52,7 @@ int prepare_cluster_frame_kernels(int N);
 int cluster_err_slots(int N);
 // error-partial slots each frame writes (one per CTA working on it)
 inline int frame_err_slots(int N0, int N1) {
-  return (N0 == N1 && (N0 == 256 || N0 == 512)) ? cluster_err_slots(N0) : 1;
+  return (N0 == N1 && cluster_frame_supported(N0)) ? cluster_err_slots(N0) : 1;
 }
 
 // error reporting (engine.cu)

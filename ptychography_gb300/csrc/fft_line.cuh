@@ -1,8 +1,9 @@
 // Register/shared-memory FFT building blocks.
 //
-// dft<R, DIR>(x): in-register DFT of R (power of two <= 32) complex values,
-// natural order in and out, DIR = -1 forward (exp(-2 pi i/R)), +1 inverse
-// (unnormalised).  Radix-4 decimation in time with compile-time twiddles.
+// dft<R, DIR>(x): in-register DFT of R complex values (R a power of two, or 3
+// times one, <= 64), natural order in and out, DIR = -1 forward
+// (exp(-2 pi i/R)), +1 inverse (unnormalised).  Radix-4 / radix-2 / radix-3
+// decimation in time with compile-time twiddles.
 //
 // Line FFT of length L = A * B (B a multiple of A), split over A threads:
 //   * thread t holds v[j] = x[t + A j], j < B            ("stride-A" layout)
@@ -56,17 +57,57 @@ PTY_DEV void bfly4(float2& a, float2& b, float2& c, float2& d) {
   d = csub(t1, j3);
 }
 
+// 3-point DFT in place: X0 = a+b+c, X1/X2 = (a - (b+c)/2) -/+ i sqrt(3)/2 (b-c) (forward)
+template <int DIR>
+PTY_DEV void bfly3(float2& a, float2& b, float2& c) {
+  constexpr float s3 = 0.86602540378443864676f;   // sqrt(3) / 2
+  const float2 t1 = cadd(b, c);
+  const float2 t2 = make_float2(a.x - 0.5f * t1.x, a.y - 0.5f * t1.y);
+  const float2 t3 = make_float2(s3 * (b.x - c.x), s3 * (b.y - c.y));
+  // -i t3 = (t3.y, -t3.x); +i t3 = (-t3.y, t3.x)
+  const float2 m = (DIR < 0) ? make_float2(t3.y, -t3.x) : make_float2(-t3.y, t3.x);
+  a = cadd(a, t1);
+  b = cadd(t2, m);
+  c = csub(t2, m);
+}
+
 template <int R, int DIR>
 PTY_DEV void dft(float2 (&x)[R]) {
-  static_assert((R & (R - 1)) == 0 && R <= 64, "power-of-two codelet");
+  static_assert(R <= 64 && ((R & (R - 1)) == 0 || (R % 3 == 0 && ((R / 3) & (R / 3 - 1)) == 0)),
+                "codelet sizes: powers of two and 3 x powers of two");
   if constexpr (R == 1) {
     return;
   } else if constexpr (R == 2) {
     float2 a = x[0], b = x[1];
     x[0] = cadd(a, b);
     x[1] = csub(a, b);
+  } else if constexpr (R == 3) {
+    bfly3<DIR>(x[0], x[1], x[2]);
   } else if constexpr (R == 4) {
     bfly4<DIR>(x[0], x[1], x[2], x[3]);
+  } else if constexpr (R % 3 == 0) {
+    // radix-3 decimation in time over three power-of-two sub-DFTs
+    constexpr int M = R / 3;
+    float2 s0[M], s1[M], s2[M];
+#pragma unroll
+    for (int m = 0; m < M; ++m) {
+      s0[m] = x[3 * m + 0];
+      s1[m] = x[3 * m + 1];
+      s2[m] = x[3 * m + 2];
+    }
+    dft<M, DIR>(s0);
+    dft<M, DIR>(s1);
+    dft<M, DIR>(s2);
+    sfor<0, M>([&](auto ik) {
+      constexpr int k = decltype(ik)::value;
+      float2 a = s0[k];
+      float2 b = tw_mul<k, R, DIR>(s1[k]);
+      float2 c = tw_mul<2 * k, R, DIR>(s2[k]);
+      bfly3<DIR>(a, b, c);
+      x[k] = a;
+      x[k + M] = b;
+      x[k + 2 * M] = c;
+    });
   } else if constexpr (R % 4 == 0) {
     constexpr int M = R / 4;
     float2 s0[M], s1[M], s2[M], s3[M];
@@ -120,6 +161,7 @@ template <> struct LineGeom<16>  { static constexpr int A = 4,  B = 4;  };
 template <> struct LineGeom<32>  { static constexpr int A = 4,  B = 8;  };
 template <> struct LineGeom<64>  { static constexpr int A = 8,  B = 8;  };
 template <> struct LineGeom<128> { static constexpr int A = 8,  B = 16; };
+template <> struct LineGeom<192> { static constexpr int A = 8,  B = 24; };
 template <> struct LineGeom<256> { static constexpr int A = 16, B = 16; };
 template <> struct LineGeom<512> { static constexpr int A = 16, B = 32; };
 

@@ -18,3 +18,22 @@ def ERA(I, R, P, O, iters, OP_iters=1, mask=1, background=None, method=None, Pmo
     """
     return _engine.run("era", I, R, P, O, iters, OP_iters, mask, background, method, Pmod_probe,
                        probe_centering, alpha, dtype, full_output)
+
+
+def ERA_batch(problems, iters, OP_iters=1, mask=1, background=None, method=None, Pmod_probe=False,
+              probe_centering=False, hardware='cpu', alpha=1.0e-10, dtype=None, full_output=True):
+    """Many independent ERA reconstructions launched together (no reference counterpart).
+
+    ``problems`` is a sequence of ``(I, R, P, O)`` tuples or of dicts holding
+    ``I``, ``R``, ``P``, ``O`` and any per-problem overrides of the keyword
+    arguments (``mask``, ``background``, ``method``, ``OP_iters``,
+    ``Pmod_probe``, ``probe_centering``, ``alpha``, ``dtype``).  All
+    reconstructions run ``iters`` iterations inside one CUDA graph, one branch
+    each, so small problems fill the GPU together.  Returns the list of what
+    ``ERA`` returns for each problem; the results equal those of separate ERA
+    calls made in the same order (NumPy's global RNG is drawn in that order).
+    """
+    defaults = dict(OP_iters=OP_iters, mask=mask, background=background, method=method,
+                    Pmod_probe=Pmod_probe, probe_centering=probe_centering, alpha=alpha,
+                    dtype=dtype, full_output=full_output)
+    return _engine.run_batch("era", problems, iters, defaults)
