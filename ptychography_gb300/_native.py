@@ -58,6 +58,10 @@ SIGNATURES = {
     "pty_psup_P_noalloc": [ctypes.POINTER(Geometry), ctypes.POINTER(c_int64), c_void_p, c_void_p,
                            c_void_p, c_int32, c_double, c_void_p, c_void_p],
     "pty_shape_supported": [c_int32, c_int32],
+    "pty_frame_tile_candidates": [c_int32, c_int32, ctypes.POINTER(c_int32), c_int32,
+                                  ctypes.POINTER(c_int32)],
+    "pty_get_frame_tile": [c_int32, c_int32, ctypes.POINTER(c_int32)],
+    "pty_set_frame_tile": [c_int32, c_int32, c_int32],
     "pty_last_error": [],
     "pty_version": [],
     "pty_launch_count": [],

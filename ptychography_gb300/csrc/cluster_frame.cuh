@@ -1,10 +1,13 @@
-// 256 x 256 and 512 x 512 frames: one frame per thread-block cluster.
+// Square frames on thread-block clusters: one frame per cluster of C CTAs.
 //
 // A 256^2 complex64 frame (512 KB) or 512^2 frame (2 MB) does not fit one SM's
-// shared memory, so the 2-D transform is distributed over a cluster of C CTAs
-// (8 for 256^2, two per SM; 16 for 512^2, one per SM), each owning N / C rows
-// and N / C columns, and the two transposes go through distributed shared
-// memory instead of HBM:
+// shared memory, so the 2-D transform is distributed over a cluster of C CTAs,
+// each owning N / C rows and N / C columns, and the two transposes go through
+// distributed shared memory instead of HBM.  The frame tiles built (N, C):
+// (128, 2), (192, 2), (256, 4), (256, 8), (512, 16); each is instantiated in
+// its own translation unit (cluster_<N>x<C>.cu) and chosen per frame size by
+// the tile autotuner (frame_tiles.cu).  Per frame (64 rows per CTA shown for
+// 256^2 on 4 CTAs):
 //
 //   1. CTA r forms its 64 rows of the input wave (exit wave, psi, or the DM
 //      combination), row-FFTs them, and stores each transformed row straight
@@ -21,6 +24,7 @@
 // HBM sees only the frame's input and output (plus the L2-resident object
 // window and probe), the same traffic as the single-CTA kernel for small frames.
 // Replaces the same reference functions as frame_kernels.cu.
+#pragma once
 #include <cooperative_groups.h>
 
 #include "engine.h"
@@ -41,8 +45,9 @@ PTY_DEV void cluster_sync_relaxed() {
 template <int N, int C>
 struct ClusterCfg {
   static constexpr int A = LineGeom<N>::A, B = LineGeom<N>::B;  // rows and columns alike
-  // 8- and 16-CTA clusters and 192^2 frames: 256 threads per CTA
-  static constexpr int NT = (C >= 8 || N == 192) ? 256 : 512;
+  // 256 threads per CTA for 8- and 16-CTA clusters and frames up to 192^2
+  // (two CTAs per SM where the shared memory allows), else 512
+  static constexpr int NT = (C >= 8 || N <= 192) ? 256 : 512;
   static constexpr int RPC = N / C;          // rows owned per CTA
   static constexpr int CPC = N / C;          // columns owned per CTA
   static constexpr int CP = CPC + 1;         // column-buffer pitch (float2), odd
@@ -186,17 +191,8 @@ __global__ void __launch_bounds__(ClusterCfg<N, C>::NT, ClusterCfg<N, C>::MINB)
   }
 }
 
-// 256 x 256 frames: 8-CTA clusters (two CTAs per SM); 512 x 512 frames:
-// 16-CTA clusters (non-portable size, one CTA per SM).
-template <int N>
-struct ClusterOf;
-template <> struct ClusterOf<192> { static constexpr int C = 2; };
-template <> struct ClusterOf<256> { static constexpr int C = 8; };
-template <> struct ClusterOf<512> { static constexpr int C = 16; };
-
-template <int N, int OP>
+template <int N, int C, int OP>
 static int set_cluster_attr() {
-  constexpr int C = ClusterOf<N>::C;
   using K = ClusterCfg<N, C>;
   auto fn = cluster_frame_kernel<N, C, OP>;
   cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)K::SMEM);
@@ -205,55 +201,50 @@ static int set_cluster_attr() {
   return PTY_OK;
 }
 
-template <int N, int OP>
-static int launch_cluster(const FrameArgs& a, int nframes, cudaStream_t st) {
-  constexpr int C = ClusterOf<N>::C;
+template <int N, int C>
+static cudaLaunchConfig_t cluster_config(int nframes, cudaStream_t st, cudaLaunchAttribute* attr) {
   using K = ClusterCfg<N, C>;
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(nframes * C);
   cfg.blockDim = dim3(K::NT);
   cfg.dynamicSmemBytes = K::SMEM;
   cfg.stream = st;
-  cudaLaunchAttribute attr[1];
   attr[0].id = cudaLaunchAttributeClusterDimension;
   attr[0].val.clusterDim.x = C;
   attr[0].val.clusterDim.y = 1;
   attr[0].val.clusterDim.z = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
+  return cfg;
+}
+
+template <int N, int C, int OP>
+static int launch_cluster(const FrameArgs& a, int nframes, cudaStream_t st) {
+  cudaLaunchAttribute attr[1];
+  cudaLaunchConfig_t cfg = cluster_config<N, C>(nframes, st, attr);
   cudaError_t e = cudaLaunchKernelEx(&cfg, cluster_frame_kernel<N, C, OP>, a);
   if (e != cudaSuccess) return set_cuda_error(e, "cluster_frame_kernel launch");
   return check_launch("cluster_frame_kernel");
 }
 
-template <int N>
-static int prepare_n() {
+// Sets the kernels' attributes and refuses the tile when no cluster of its
+// size can be resident on this GPU.
+template <int N, int C>
+static int prepare_cluster_tile() {
   int rc = PTY_OK;
-  if (!rc) rc = set_cluster_attr<N, OP_EXIT1>();
-  if (!rc) rc = set_cluster_attr<N, OP_EXIT7>();
-  if (!rc) rc = set_cluster_attr<N, OP_PSI1>();
-  if (!rc) rc = set_cluster_attr<N, OP_PSI7>();
-  if (!rc) rc = set_cluster_attr<N, OP_DM1>();
-  if (!rc) rc = set_cluster_attr<N, OP_DM7>();
-  if (!rc) rc = set_cluster_attr<N, OP_MERR>();
-  if (!rc) rc = set_cluster_attr<N, OP_INTENS>();
-  if (!rc) rc = set_cluster_attr<N, OP_MERR_PSI>();
-  if (!rc) rc = set_cluster_attr<N, OP_BP>();
+  if (!rc) rc = set_cluster_attr<N, C, OP_EXIT1>();
+  if (!rc) rc = set_cluster_attr<N, C, OP_EXIT7>();
+  if (!rc) rc = set_cluster_attr<N, C, OP_PSI1>();
+  if (!rc) rc = set_cluster_attr<N, C, OP_PSI7>();
+  if (!rc) rc = set_cluster_attr<N, C, OP_DM1>();
+  if (!rc) rc = set_cluster_attr<N, C, OP_DM7>();
+  if (!rc) rc = set_cluster_attr<N, C, OP_MERR>();
+  if (!rc) rc = set_cluster_attr<N, C, OP_INTENS>();
+  if (!rc) rc = set_cluster_attr<N, C, OP_MERR_PSI>();
+  if (!rc) rc = set_cluster_attr<N, C, OP_BP>();
   if (rc) return rc;
-  // refuse the shape when no cluster of this size can be resident on the GPU
-  constexpr int C = ClusterOf<N>::C;
-  using K = ClusterCfg<N, C>;
-  cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3(C);
-  cfg.blockDim = dim3(K::NT);
-  cfg.dynamicSmemBytes = K::SMEM;
   cudaLaunchAttribute attr[1];
-  attr[0].id = cudaLaunchAttributeClusterDimension;
-  attr[0].val.clusterDim.x = C;
-  attr[0].val.clusterDim.y = 1;
-  attr[0].val.clusterDim.z = 1;
-  cfg.attrs = attr;
-  cfg.numAttrs = 1;
+  cudaLaunchConfig_t cfg = cluster_config<N, C>(1, nullptr, attr);
   int nclusters = 0;
   cudaError_t e = cudaOccupancyMaxActiveClusters(&nclusters, cluster_frame_kernel<N, C, OP_PSI7>, &cfg);
   if (e != cudaSuccess) return set_cuda_error(e, "cudaOccupancyMaxActiveClusters");
@@ -261,41 +252,31 @@ static int prepare_n() {
   return PTY_OK;
 }
 
-template <int N>
-static int launch_n(int op, const FrameArgs& a, int nframes, cudaStream_t st) {
+template <int N, int C>
+static int launch_cluster_tile(int op, const FrameArgs& a, int nframes, cudaStream_t st) {
   switch (op) {
-    case OP_EXIT1: return launch_cluster<N, OP_EXIT1>(a, nframes, st);
-    case OP_EXIT7: return launch_cluster<N, OP_EXIT7>(a, nframes, st);
-    case OP_PSI1: return launch_cluster<N, OP_PSI1>(a, nframes, st);
-    case OP_PSI7: return launch_cluster<N, OP_PSI7>(a, nframes, st);
-    case OP_DM1: return launch_cluster<N, OP_DM1>(a, nframes, st);
-    case OP_DM7: return launch_cluster<N, OP_DM7>(a, nframes, st);
-    case OP_MERR: return launch_cluster<N, OP_MERR>(a, nframes, st);
-    case OP_INTENS: return launch_cluster<N, OP_INTENS>(a, nframes, st);
-    case OP_MERR_PSI: return launch_cluster<N, OP_MERR_PSI>(a, nframes, st);
-    case OP_BP: return launch_cluster<N, OP_BP>(a, nframes, st);
+    case OP_EXIT1: return launch_cluster<N, C, OP_EXIT1>(a, nframes, st);
+    case OP_EXIT7: return launch_cluster<N, C, OP_EXIT7>(a, nframes, st);
+    case OP_PSI1: return launch_cluster<N, C, OP_PSI1>(a, nframes, st);
+    case OP_PSI7: return launch_cluster<N, C, OP_PSI7>(a, nframes, st);
+    case OP_DM1: return launch_cluster<N, C, OP_DM1>(a, nframes, st);
+    case OP_DM7: return launch_cluster<N, C, OP_DM7>(a, nframes, st);
+    case OP_MERR: return launch_cluster<N, C, OP_MERR>(a, nframes, st);
+    case OP_INTENS: return launch_cluster<N, C, OP_INTENS>(a, nframes, st);
+    case OP_MERR_PSI: return launch_cluster<N, C, OP_MERR_PSI>(a, nframes, st);
+    case OP_BP: return launch_cluster<N, C, OP_BP>(a, nframes, st);
   }
   return set_error(PTY_ERR_ARG, "unknown frame op");
 }
 
-bool cluster_frame_supported(int N) { return N == 192 || N == 256 || N == 512; }
-
-int cluster_err_slots(int N) {
-  return N == 512 ? ClusterOf<512>::C : N == 192 ? ClusterOf<192>::C : ClusterOf<256>::C;
-}
-
-int prepare_cluster_frame_kernels(int N) {
-  if (N == 192) return prepare_n<192>();
-  if (N == 256) return prepare_n<256>();
-  if (N == 512) return prepare_n<512>();
-  return set_error(PTY_ERR_SHAPE, "no cluster kernel for this frame size");
-}
-
-int launch_cluster_frame_op(int N, int op, const FrameArgs& a, int nframes, cudaStream_t st) {
-  if (N == 192) return launch_n<192>(op, a, nframes, st);
-  if (N == 256) return launch_n<256>(op, a, nframes, st);
-  if (N == 512) return launch_n<512>(op, a, nframes, st);
-  return set_error(PTY_ERR_SHAPE, "no cluster kernel for this frame size");
-}
-
 }  // namespace pty
+
+// Defines the two entry points of one cluster tile: prepare_cluster_<N>x<C>()
+// and launch_cluster_<N>x<C>(op, args, nframes, stream).
+#define PTY_CLUSTER_TILE(N, C)                                                              \
+  namespace pty {                                                                           \
+  int prepare_cluster_##N##x##C() { return prepare_cluster_tile<N, C>(); }                  \
+  int launch_cluster_##N##x##C(int op, const FrameArgs& a, int nframes, cudaStream_t st) {  \
+    return launch_cluster_tile<N, C>(op, a, nframes, st);                                   \
+  }                                                                                         \
+  }

@@ -44,17 +44,6 @@ int check_launch(const char* where) {
 
 using namespace pty;
 
-#define PTY_TRY(x)              \
-  do {                          \
-    int _rc = (x);              \
-    if (_rc != PTY_OK) return _rc; \
-  } while (0)
-#define PTY_CUDA(x)                                          \
-  do {                                                       \
-    cudaError_t _e = (x);                                    \
-    if (_e != cudaSuccess) return set_cuda_error(_e, #x);    \
-  } while (0)
-
 struct pty_plan {
   int n = 0, N0 = 0, N1 = 0, U = 0, V = 0;
   int* d_R = nullptr;
@@ -73,7 +62,8 @@ struct pty_plan {
   int Km = 1;                    // background-mean frame chunks
   float2* d_mean_part = nullptr;
   double* d_err_part = nullptr;  // [n * eslots]
-  int eslots = 1;                // error partials per frame
+  int tile = 1;                  // CTAs per frame of the fused frame kernels
+  int eslots = 1;                // error partials per frame (one per CTA)
   int ndn = 304;                 // diffnorm blocks per array (two per SM)
   double* d_dn_part = nullptr;   // [2 arrays][ndn][2]
   int* d_shift = nullptr;
@@ -96,7 +86,12 @@ struct pty_plan {
     int heat_valid = 0;
     long long kernels = 0;
   } graphs[2];
-  cudaGraphExec_t batch_exec = nullptr;   // last batch graph launched from this plan
+  // last batch graph launched with this plan first (pty_run_batch)
+  cudaGraphExec_t batch_exec = nullptr;
+  std::string batch_key;
+  std::vector<char> batch_heat;
+  long long batch_kernels = 0;
+  long long serial = 0;          // unique per plan in the process (batch keys)
   std::vector<void*> allocs;
 };
 
@@ -116,27 +111,7 @@ static int dalloc_t(pty_plan* p, T** ptr, size_t count) {
   return dalloc(p, reinterpret_cast<void**>(ptr), count * sizeof(T));
 }
 
-static void twiddles(int L, std::vector<float2>& out) {
-  int A, B;
-  switch (L) {
-    case 16: A = 4; B = 4; break;
-    case 32: A = 4; B = 8; break;
-    case 64: A = 8; B = 8; break;
-    case 128: A = 8; B = 16; break;
-    case 192: A = 8; B = 24; break;
-    case 256: A = 16; B = 16; break;
-    default: A = 16; B = 32; break;
-  }
-  out.assign(L, make_float2(1.f, 0.f));
-  const double pi = 3.14159265358979323846;
-  for (int k1 = 0; k1 < B; ++k1)
-    for (int t = 0; t < A; ++t) {
-      const double th = -2.0 * pi * (double)((long long)t * k1 % L) / (double)L;
-      out[k1 * A + t] = make_float2((float)std::cos(th), (float)std::sin(th));
-    }
-}
 
-static int prepare_kernels(int N0, int N1);
 
 extern "C" int pty_shape_supported(int32_t N0, int32_t N1) {
   return frame_shape_supported(N0, N1) ? 1 : 0;
@@ -179,6 +154,8 @@ extern "C" int pty_plan_create(const pty_geometry* g, const int64_t* R_host, pty
   }
   pty_plan* p = new pty_plan();
   p->n = n; p->N0 = N0; p->N1 = N1; p->U = U; p->V = V;
+  static std::atomic<long long> next_serial{1};
+  p->serial = next_serial++;
   int rc = PTY_OK;
   auto fail = [&](int code) { pty_plan_destroy(p); return code; };
 
@@ -227,7 +204,8 @@ extern "C" int pty_plan_create(const pty_geometry* g, const int64_t* R_host, pty
   if ((rc = dalloc_t(p, &p->d_part_num, (size_t)p->K * npix))) return fail(rc);
   if ((rc = dalloc_t(p, &p->d_part_den, (size_t)p->K * npix))) return fail(rc);
   if ((rc = dalloc_t(p, &p->d_mean_part, (size_t)(p->Km > p->K ? p->Km : p->K) * npix))) return fail(rc);
-  p->eslots = frame_err_slots(N0, N1);
+  if ((rc = choose_frame_tile(N0, N1, &p->tile))) return fail(rc);
+  p->eslots = p->tile;
   if ((rc = dalloc_t(p, &p->d_err_part, (size_t)n * p->eslots))) return fail(rc);
   if ((rc = dalloc_t(p, &p->d_dn_part, (size_t)4 * p->ndn))) return fail(rc);
   if ((rc = dalloc_t(p, &p->d_shift, 2))) return fail(rc);
@@ -240,9 +218,9 @@ extern "C" int pty_plan_create(const pty_geometry* g, const int64_t* R_host, pty
   if ((rc = dalloc_t(p, &p->d_b0, npix))) return fail(rc);
   if ((rc = dalloc_t(p, &p->d_sum, 4))) return fail(rc);
 
-  std::vector<float2> tw0, tw1;
-  twiddles(N0, tw0);
-  twiddles(N1, tw1);
+  std::vector<float2> tw0(N0), tw1(N1);
+  make_twiddles(N0, tw0.data());
+  make_twiddles(N1, tw1.data());
   cudaError_t e = cudaSuccess;
   if (e == cudaSuccess) e = cudaMemcpy(p->d_R, R.data(), R.size() * sizeof(int), cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemcpy(p->d_tile_ptr, ptr.data(), ptr.size() * sizeof(int), cudaMemcpyHostToDevice);
@@ -255,7 +233,6 @@ extern "C" int pty_plan_create(const pty_geometry* g, const int64_t* R_host, pty
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&p->ev_out, cudaEventDisableTiming);
   if (e != cudaSuccess) return fail(set_cuda_error(e, "pty_plan_create"));
   p->tl = TileLists{TR, T, ntu, ntv, p->d_tile_ptr, p->d_tile_frames};
-  if ((rc = prepare_kernels(N0, N1))) return fail(rc);
   *out = p;
   return PTY_OK;
 }
@@ -275,7 +252,7 @@ static FrameArgs base_args(const pty_plan* p) {
 }
 
 static int frame_op(const pty_plan* p, int op, const FrameArgs& a, int nframes, cudaStream_t st) {
-  return launch_frame_op(op, p->N0, p->N1, a, nframes, st);
+  return launch_frame_op(op, p->N0, p->N1, p->tile, a, nframes, st);
 }
 
 // Pmod_P (era.py:597-610): the probe as a single frame through the Pmod_1 path
@@ -681,57 +658,76 @@ extern "C" int pty_run_batch(int32_t kind, pty_plan* const* plans, const pty_buf
   }
   pty_plan* p0 = plans[0];
   cudaStream_t master = p0->cap, user = (cudaStream_t)stream;
+  // a batch with the same plans (by serial, so a freed and re-created plan
+  // never matches), buffers, options and iteration count replays its graph
+  std::string key;
+  for (int r = 0; r < nrec; ++r) {
+    key.append(reinterpret_cast<const char*>(&plans[r]->serial), sizeof(long long));
+    key += request_key(kind == 0 ? 'E' : 'D', &bufs[r], &opts[r], iters);
+  }
   std::vector<bool> hv(nrec, false);
-  cudaEvent_t fork = nullptr;
-  PTY_CUDA(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming));
+  PTY_CUDA(cudaEventRecord(p0->ev_in, user));
+  PTY_CUDA(cudaStreamWaitEvent(master, p0->ev_in, 0));
   int rc = PTY_OK;
-  cudaGraph_t g = nullptr;
-  cudaError_t e = cudaEventRecord(p0->ev_in, user);
-  if (e == cudaSuccess) e = cudaStreamWaitEvent(master, p0->ev_in, 0);
-  if (e == cudaSuccess) e = cudaStreamBeginCapture(master, cudaStreamCaptureModeThreadLocal);
-  if (e != cudaSuccess) rc = set_cuda_error(e, "batch capture");
-  bool capturing = (rc == PTY_OK);
-  if (rc == PTY_OK) {
-    e = cudaEventRecord(fork, master);
-    if (e != cudaSuccess) rc = set_cuda_error(e, "batch fork");
-  }
-  for (int r = 0; rc == PTY_OK && r < nrec; ++r) {
-    cudaStream_t st = (r == 0) ? master : plans[r]->cap;
-    if (r > 0 && (e = cudaStreamWaitEvent(st, fork, 0)) != cudaSuccess) {
-      rc = set_cuda_error(e, "batch fork wait");
-      break;
+  if (p0->batch_exec && p0->batch_key == key) {
+    cudaError_t e = cudaGraphLaunch(p0->batch_exec, master);
+    if (e != cudaSuccess) rc = set_cuda_error(e, "batch graph replay");
+    else count_launches(p0->batch_kernels);
+    for (int r = 0; r < nrec; ++r) hv[r] = p0->batch_heat[r] != 0;
+  } else {
+    cudaEvent_t fork = nullptr;
+    PTY_CUDA(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming));
+    cudaGraph_t g = nullptr;
+    const long long before = launch_total();
+    cudaError_t e = cudaStreamBeginCapture(master, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) rc = set_cuda_error(e, "batch capture");
+    const bool capturing = (rc == PTY_OK);
+    if (rc == PTY_OK) {
+      e = cudaEventRecord(fork, master);
+      if (e != cudaSuccess) rc = set_cuda_error(e, "batch fork");
     }
-    bool h = false;
-    rc = kind == 0 ? era_body(plans[r], &bufs[r], &opts[r], iters, h, st)
-                   : dm_body(plans[r], &bufs[r], &opts[r], iters, h, st);
-    hv[r] = h;
-    if (rc == PTY_OK && r > 0) {
-      e = cudaEventRecord(plans[r]->ev_out, st);
-      if (e == cudaSuccess) e = cudaStreamWaitEvent(master, plans[r]->ev_out, 0);
-      if (e != cudaSuccess) rc = set_cuda_error(e, "batch join");
+    for (int r = 0; rc == PTY_OK && r < nrec; ++r) {
+      cudaStream_t st = (r == 0) ? master : plans[r]->cap;
+      if (r > 0 && (e = cudaStreamWaitEvent(st, fork, 0)) != cudaSuccess) {
+        rc = set_cuda_error(e, "batch fork wait");
+        break;
+      }
+      bool h = false;
+      rc = kind == 0 ? era_body(plans[r], &bufs[r], &opts[r], iters, h, st)
+                     : dm_body(plans[r], &bufs[r], &opts[r], iters, h, st);
+      hv[r] = h;
+      if (rc == PTY_OK && r > 0) {
+        e = cudaEventRecord(plans[r]->ev_out, st);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(master, plans[r]->ev_out, 0);
+        if (e != cudaSuccess) rc = set_cuda_error(e, "batch join");
+      }
     }
-  }
-  if (capturing) {
-    e = cudaStreamEndCapture(master, &g);
-    if (rc == PTY_OK && e != cudaSuccess) rc = set_cuda_error(e, "batch end capture");
-  }
-  if (rc == PTY_OK) {
-    cudaGraphExec_t ge = nullptr;
-    e = cudaGraphInstantiate(&ge, g, 0);
-    if (e == cudaSuccess) e = cudaGraphLaunch(ge, master);
-    if (e != cudaSuccess) {
-      rc = set_cuda_error(e, "batch graph launch");
-      if (ge) cudaGraphExecDestroy(ge);
-    } else {
-      // kept alive until the plan is destroyed or runs the next batch
-      if (p0->batch_exec) cudaGraphExecDestroy(p0->batch_exec);
-      p0->batch_exec = ge;
+    const long long nkern = launch_total() - before;
+    if (capturing) {
+      e = cudaStreamEndCapture(master, &g);
+      if (rc == PTY_OK && e != cudaSuccess) rc = set_cuda_error(e, "batch end capture");
     }
+    if (rc == PTY_OK) {
+      cudaGraphExec_t ge = nullptr;
+      e = cudaGraphInstantiate(&ge, g, 0);
+      if (e == cudaSuccess) e = cudaGraphLaunch(ge, master);
+      if (e != cudaSuccess) {
+        rc = set_cuda_error(e, "batch graph launch");
+        if (ge) cudaGraphExecDestroy(ge);
+      } else {
+        // kept until the plan is destroyed or launches another batch
+        if (p0->batch_exec) cudaGraphExecDestroy(p0->batch_exec);
+        p0->batch_exec = ge;
+        p0->batch_key = key;
+        p0->batch_heat.assign(hv.begin(), hv.end());
+        p0->batch_kernels = nkern;
+      }
+    }
+    if (g) cudaGraphDestroy(g);
+    cudaEventDestroy(fork);
   }
-  if (g) cudaGraphDestroy(g);
   cudaEventRecord(p0->ev_out, master);
   cudaStreamWaitEvent(user, p0->ev_out, 0);
-  cudaEventDestroy(fork);
   if (heatmap_valid)
     for (int r = 0; r < nrec; ++r) heatmap_valid[r] = hv[r] ? 1 : 0;
   return rc;
@@ -891,4 +887,3 @@ extern "C" int pty_amp_from_intensity(pty_plan* p, const void* I, int32_t is_dou
   return check_launch("amp_kernel");
 }
 
-static int prepare_kernels(int N0, int N1) { return prepare_frame_kernels(N0, N1); }

@@ -43,21 +43,43 @@ struct FrameArgs {
   const float2* tw1;         // twiddles of the row transform (length N1)
 };
 
+// Frame tiles: how many CTAs transform one frame.  Tile 1 is the single-CTA
+// kernel (frame_kernels.cu), tile C > 1 the C-CTA cluster kernel
+// (cluster_frame.cuh).  frame_tiles.cu lists the tiles built per shape and
+// picks one per shape and device (autotuned, or forced by the caller).
 bool frame_shape_supported(int N0, int N1);
-int prepare_frame_kernels(int N0, int N1);
-int launch_frame_op(int op, int N0, int N1, const FrameArgs& a, int nframes, cudaStream_t st);
-bool cluster_frame_supported(int N);
-int launch_cluster_frame_op(int N, int op, const FrameArgs& a, int nframes, cudaStream_t st);
-int prepare_cluster_frame_kernels(int N);
-int cluster_err_slots(int N);
-// error-partial slots each frame writes (one per CTA working on it)
-inline int frame_err_slots(int N0, int N1) {
-  return (N0 == N1 && cluster_frame_supported(N0)) ? cluster_err_slots(N0) : 1;
-}
+int frame_tile_candidates(int N0, int N1, int* tiles, int cap);   // returns the count
+int choose_frame_tile(int N0, int N1, int* tile);                  // prepares the kernels too
+int launch_frame_op(int op, int N0, int N1, int tile, const FrameArgs& a, int nframes,
+                    cudaStream_t st);
+void make_twiddles(int L, float2* out);   // host table tw[k1 * A + t], length L
+
+int prepare_single_cta(int N0, int N1);
+int launch_single_cta_op(int op, int N0, int N1, const FrameArgs& a, int nframes, cudaStream_t st);
+#define PTY_DECLARE_CLUSTER_TILE(N, C)                                                    \
+  int prepare_cluster_##N##x##C();                                                        \
+  int launch_cluster_##N##x##C(int op, const FrameArgs& a, int nframes, cudaStream_t st);
+PTY_DECLARE_CLUSTER_TILE(128, 2)
+PTY_DECLARE_CLUSTER_TILE(192, 2)
+PTY_DECLARE_CLUSTER_TILE(256, 4)
+PTY_DECLARE_CLUSTER_TILE(256, 8)
+PTY_DECLARE_CLUSTER_TILE(512, 16)
+#undef PTY_DECLARE_CLUSTER_TILE
 
 // error reporting (engine.cu)
 int set_error(int code, const char* msg);
 int set_cuda_error(cudaError_t e, const char* where);
+// return early with the status of a failing call
+#define PTY_TRY(x)                   \
+  do {                               \
+    int _rc = (x);                   \
+    if (_rc != PTY_OK) return _rc;   \
+  } while (0)
+#define PTY_CUDA(x)                                          \
+  do {                                                       \
+    cudaError_t _e = (x);                                    \
+    if (_e != cudaSuccess) return pty::set_cuda_error(_e, #x); \
+  } while (0)
 int check_launch(const char* where);  // also counts the launch
 void count_launches(long long k);
 long long launch_total();

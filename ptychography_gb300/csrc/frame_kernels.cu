@@ -230,29 +230,20 @@ static int prepare_shape() {
   return rc;
 }
 
-int prepare_frame_kernels(int N0, int N1) {
+int prepare_single_cta(int N0, int N1) {
   if (N0 == 32 && N1 == 32) return prepare_shape<32, 32>();
   if (N0 == 64 && N1 == 64) return prepare_shape<64, 64>();
   if (N0 == 128 && N1 == 128) return prepare_shape<128, 128>();
   if (N0 == 32 && N1 == 64) return prepare_shape<32, 64>();
-  if (N0 == N1 && cluster_frame_supported(N0)) return prepare_cluster_frame_kernels(N0);
-  return set_error(PTY_ERR_SHAPE, "frame shape not supported by the fused FFT kernels");
+  return set_error(PTY_ERR_SHAPE, "no single-CTA frame kernel for this shape");
 }
 
-bool frame_shape_supported(int N0, int N1) {
-  auto ok = [](int n) { return n == 32 || n == 64 || n == 128; };
-  if (N0 == N1 && cluster_frame_supported(N0)) return true;
-  return ok(N0) && ok(N1) && (N0 == N1 || (N0 == 32 && N1 == 64));
-}
-
-int launch_frame_op(int op, int N0, int N1, const FrameArgs& a, int nframes, cudaStream_t st) {
-  if (nframes <= 0) return PTY_OK;
+int launch_single_cta_op(int op, int N0, int N1, const FrameArgs& a, int nframes, cudaStream_t st) {
   if (N0 == 32 && N1 == 32) return launch_op<32, 32>(op, a, nframes, st);
   if (N0 == 64 && N1 == 64) return launch_op<64, 64>(op, a, nframes, st);
   if (N0 == 128 && N1 == 128) return launch_op<128, 128>(op, a, nframes, st);
   if (N0 == 32 && N1 == 64) return launch_op<32, 64>(op, a, nframes, st);
-  if (N0 == N1 && cluster_frame_supported(N0)) return launch_cluster_frame_op(N0, op, a, nframes, st);
-  return set_error(PTY_ERR_UNSUPPORTED, "frame shape not supported by the fused FFT kernels");
+  return set_error(PTY_ERR_UNSUPPORTED, "no single-CTA frame kernel for this shape");
 }
 
 }  // namespace pty

@@ -46,10 +46,23 @@ def test_struct_layouts_match_c():
 def test_version_and_shapes_without_gpu():
     lib = _native.load()
     assert lib.pty_version() >= 100
-    for n in (32, 64, 128):
+    for n in (32, 64, 128, 192, 256, 512):
         assert lib.pty_shape_supported(n, n) == 1
+    assert lib.pty_shape_supported(32, 64) == 1
     assert lib.pty_shape_supported(48, 48) == 0
     assert lib.pty_shape_supported(100, 128) == 0
+
+
+def test_frame_tile_candidates_without_gpu():
+    lib = _native.load()
+    want = {32: [1], 64: [1], 128: [1, 2], 192: [2], 256: [8, 4], 512: [16]}
+    for n, tiles in want.items():
+        buf = (ctypes.c_int32 * 4)()
+        cnt = ctypes.c_int32(0)
+        assert lib.pty_frame_tile_candidates(n, n, buf, 4, ctypes.byref(cnt)) == 0
+        assert [buf[i] for i in range(cnt.value)] == tiles
+    cnt = ctypes.c_int32(0)
+    assert lib.pty_frame_tile_candidates(48, 48, None, 0, ctypes.byref(cnt)) != 0
 
 
 def test_plan_create_rejects_bad_geometry():

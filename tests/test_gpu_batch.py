@@ -70,3 +70,47 @@ def test_batch_tuple_form_and_empty(problems):
     (o1, i1), = pty.ERA_batch([(I, R.copy(), P, None)], 2, mask=M, method=1)
     o2, i2 = pty.ERA(I, R.copy(), P, None, 2, mask=M, method=1)
     _same((o1, i1), (o2, i2))
+
+
+def test_batch_graph_replay_matches_separate_runs(problems):
+    """A repeated pty_run_batch call replays the cached graph; results stay exact."""
+    import ctypes
+    import torch
+    from ptychography_gb300 import _engine, _native
+    lib = _native.load()
+    dev = torch.device("cuda", 0)
+    sp = ctypes.c_void_p(torch.cuda.current_stream(dev).cuda_stream)
+
+    def jobs():
+        out = []
+        for I, R, P, O, M in problems[:3]:
+            np.random.seed(3)
+            out.append(_engine._Job(lib, dev, sp, "era", I, R.copy(), P * np.exp(0.2j), None, 2, 1,
+                                    M, None, 3, False, False, 1e-10, "single", True, True))
+        return out
+
+    a, b = jobs(), jobs()
+    try:
+        k = len(a)
+        plans = (ctypes.c_void_p * k)(*[j.plan.value for j in a])
+        bufs = (_native.Buffers * k)(*[j.buf for j in a])
+        opts = (_native.Options * k)(*[j.opt for j in a])
+        hv = (ctypes.c_int32 * k)()
+        before = lib.pty_launch_count()
+        _native.check(lib.pty_run_batch(0, plans, bufs, opts, k, 2, hv, sp))
+        first = lib.pty_launch_count() - before
+        _native.check(lib.pty_run_batch(0, plans, bufs, opts, k, 2, hv, sp))
+        assert lib.pty_launch_count() - before == 2 * first      # replay counted the same
+        h = ctypes.c_int32(0)
+        for j in b:
+            for _ in range(2):
+                _native.check(lib.pty_era(j.plan, ctypes.byref(j.buf), ctypes.byref(j.opt), 2,
+                                          ctypes.byref(h), sp))
+        torch.cuda.synchronize()
+        for x, y in zip(a, b):
+            np.testing.assert_array_equal(x.O_d.cpu().numpy(), y.O_d.cpu().numpy())
+            np.testing.assert_array_equal(x.P_d.cpu().numpy(), y.P_d.cpu().numpy())
+            np.testing.assert_array_equal(x.emod.cpu().numpy(), y.emod.cpu().numpy())
+    finally:
+        for j in a + b:
+            j.close()

@@ -1,0 +1,97 @@
+"""Frame tiles: every tile built for a shape gives the same exit waves.
+
+128 x 128 frames have a single-CTA kernel and a 2-CTA cluster kernel, 256 x 256
+frames 8- and 4-CTA cluster kernels.  Each tile, forced in turn, must match the
+oracle, and the exit waves, object and probe must be bit-identical across tiles
+(the same line transforms run in the same order); only the error sums, whose
+per-CTA partials are added in a different grouping, may differ in rounding.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+import torch
+
+import ptychography_gb300 as pty
+from gpu_util import Plan, ptr, rel, to_dev
+from oracle import ptycho_oracle as orc
+from ptychography_gb300 import _native
+from test_gpu_cluster192 import small_problem
+
+pytestmark = pytest.mark.gpu
+
+
+def candidates(N):
+    lib = _native.load()
+    buf = (ctypes.c_int32 * 4)()
+    cnt = ctypes.c_int32(0)
+    _native.check(lib.pty_frame_tile_candidates(N, N, buf, 4, ctypes.byref(cnt)))
+    return [buf[i] for i in range(cnt.value)]
+
+
+class forced_tile:
+    def __init__(self, N, tile):
+        self.N, self.tile, self.lib = N, tile, _native.load()
+
+    def __enter__(self):
+        _native.check(self.lib.pty_set_frame_tile(self.N, self.N, self.tile))
+
+    def __exit__(self, *a):
+        self.lib.pty_set_frame_tile(self.N, self.N, 0)
+
+
+@pytest.mark.parametrize("N", [128, 256])
+def test_tiles_listed_and_chosen(N):
+    lib = _native.load()
+    c = candidates(N)
+    assert len(c) == 2
+    t = ctypes.c_int32(0)
+    _native.check(lib.pty_get_frame_tile(N, N, ctypes.byref(t)))
+    assert t.value in c
+    assert lib.pty_set_frame_tile(N, N, 3) == 1       # PTY_ERR_ARG: tile not built
+
+
+@pytest.mark.parametrize("N", [128, 256])
+def test_pmod_7_every_tile(N):
+    rng = np.random.default_rng(N + 7)
+    n, U = 5, N + 40
+    R = np.stack([-rng.integers(0, U - N + 1, n), -rng.integers(0, U - N + 1, n)], 1)
+    ex = rng.standard_normal((n, N, N)) + 1j * rng.standard_normal((n, N, N))
+    amp = np.abs(rng.standard_normal((n, N, N))) * 50
+    bg = np.abs(rng.standard_normal((n, N, N)))
+    mask = rng.random((N, N)) > 0.05
+    ref, bref, em = orc.pmod_7(amp, bg.copy(), ex.copy(), mask, 1e-10, True)
+    outs = []
+    for tile in candidates(N):
+        with forced_tile(N, tile):
+            plan = Plan(n, N, N, U, U, R)
+            try:
+                psi = to_dev(ex, np.complex64)
+                b = to_dev(bg, np.float32)
+                # device inputs held by name until the call has synchronised
+                amp_d, mask_d = to_dev(amp, np.float32), to_dev(mask, np.uint8)
+                e = torch.zeros(1, dtype=torch.float64, device=psi.device)
+                plan.call("pty_pmod_7", ptr(amp_d), ptr(b), ptr(psi), ptr(mask_d), 1e-10, ptr(e))
+            finally:
+                plan.close()
+        p = psi.cpu().numpy()
+        assert rel(p, ref) < 3e-6, tile
+        assert rel(b.cpu().numpy(), bref) < 1e-5, tile
+        assert float(e.cpu()[0]) == pytest.approx(em, rel=1e-5)
+        outs.append((p, b.cpu().numpy()))
+    for p, b in outs[1:]:
+        np.testing.assert_array_equal(p, outs[0][0])
+        np.testing.assert_array_equal(b, outs[0][1])
+
+
+@pytest.mark.parametrize("N", [128, 256])
+def test_era_m3_every_tile(N):
+    I, R, P, O, M = small_problem(N, seed=N, side=3)
+    res = []
+    for tile in candidates(N):
+        with forced_tile(N, tile):
+            res.append(pty.ERA(I, R.copy(), P * np.exp(0.2j), None, 3, mask=M, method=3))
+    for O_t, P_t, info in res[1:]:
+        np.testing.assert_array_equal(O_t, res[0][0])
+        np.testing.assert_array_equal(P_t, res[0][1])
+        np.testing.assert_allclose(info["eMod"], res[0][2]["eMod"], rtol=1e-6)
