@@ -491,7 +491,7 @@ def peaks():
         return 6800.0, "fallback"
 
 
-def roofline_pmod7(job, torch, reps=20):
+def roofline_pmod7(job, torch, tile, reps=20):
     """Fused frame kernel (Pmod_7 form, the DM m6 modulus step) alone, event-timed.
 
     Algorithmic bytes per frame: psi read 8 N^2 + psi write 8 N^2 + amp 4 N^2 +
@@ -509,9 +509,9 @@ def roofline_pmod7(job, torch, reps=20):
     # DRAM bytes (read + write) of one launch from the ncu capture in
     # profiles/cluster_frame_kernel_psi7_256x256x256.md (410.0 MB for 256 frames),
     # scaled by frames; recorded for the 256 x 256 kernel only
-    traffic = round(410.0e6 * job.n / 256) if job.N == 256 else None
-    kname = {256: "cluster_frame_kernel<256,8,PSI7>", 512: "cluster_frame_kernel<512,16,PSI7>"}.get(
-        job.N, "frame_kernel<%d,%d,PSI7>" % (job.N, job.N))
+    traffic = round(410.0e6 * job.n / 256) if (job.N == 256 and tile == 8) else None
+    kname = ("cluster_frame_kernel<%d,%d,PSI7>" % (job.N, tile) if tile > 1
+             else "frame_kernel<%d,%d,PSI7>" % (job.N, job.N))
     pk, kind = peaks()
     gbs = bytes_ / t / 1e9
     return {"kernel": kname,
@@ -777,7 +777,12 @@ def main():
     frames = job.frames_per_step() * args.steps * world
     value = frames / t
 
-    roof = roofline_pmod7(job, torch)
+    tiles = []
+    for fam in (0, 1):                       # plain / background op families
+        t_ = ctypes.c_int32(0)
+        _native.check(lib.pty_get_frame_tile(job.N, job.N, fam, ctypes.byref(t_)))
+        tiles.append(int(t_.value))
+    roof = roofline_pmod7(job, torch, tiles[1])
     m1 = era_m1_rate(job, torch, max(args.steps, 10)) if args.workload == "c1" else None
     job.close()
     if rank != 0:
@@ -799,7 +804,8 @@ def main():
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": round(1e3 * t / args.steps, 4), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": dict(workload_config(args.workload), parallelism="replicas" if world > 1 else "1 GPU"),
+        "config": dict(workload_config(args.workload), parallelism="replicas" if world > 1 else "1 GPU",
+                       frame_tile_ctas={"plain": tiles[0], "background": tiles[1]}),
         "gpu_launches": int(launches), "clocks": clk.summary(), "roofline": roof,
         "cpu_baseline": cpu, "e2e": e2e,
     }

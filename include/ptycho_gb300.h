@@ -162,19 +162,24 @@ int pty_psup_P_noalloc(const pty_geometry* geom, const int64_t* R_host, const vo
 int pty_shape_supported(int32_t N0, int32_t N1);
 
 /* Frame tiles (no reference counterpart): the number of CTAs that transform
- * one frame, 1 = one CTA per frame, C > 1 = a cluster of C CTAs.  Shapes with
- * more than one tile built (128 x 128: 1 or 2; 256 x 256: 8 or 4) get theirs
- * from an autotuner run by the first plan created for the shape on a device
- * (disabled by PTY_AUTOTUNE=0 in the environment: first candidate).  A plan
- * keeps the tile chosen when it was created.
+ * one frame, 1 = one CTA per frame, C > 1 = a cluster of C CTAs.  Tiles are
+ * chosen per op family: family 0 = the plain forms (Pmod_1, model error,
+ * intensities, back projection), family 1 = the background forms (Pmod_7 and
+ * the DM background recursion).  Shapes with more than one tile built
+ * (128 x 128: 1 or 2; 256 x 256: 8, 4 or 16) get theirs from an autotuner run
+ * by the first plan created for the shape on a device (disabled by
+ * PTY_AUTOTUNE=0 in the environment: first candidate).  A plan keeps the
+ * tiles chosen when it was created.
  *   pty_frame_tile_candidates: the tiles built for the shape (up to cap
  *     written to tiles[], their number to *count);
- *   pty_get_frame_tile: the tile new plans get (tunes now if not yet done);
- *   pty_set_frame_tile: force a listed tile for plans created afterwards on
- *     the current device; tile 0 forgets the choice (tuned again next time). */
+ *   pty_get_frame_tile: the tile new plans get for the family (tunes now if
+ *     not yet done);
+ *   pty_set_frame_tile: force a listed tile for the family in plans created
+ *     afterwards on the current device; tile 0 forgets the choice (tuned
+ *     again next time). */
 int pty_frame_tile_candidates(int32_t N0, int32_t N1, int32_t* tiles, int32_t cap, int32_t* count);
-int pty_get_frame_tile(int32_t N0, int32_t N1, int32_t* tile);
-int pty_set_frame_tile(int32_t N0, int32_t N1, int32_t tile);
+int pty_get_frame_tile(int32_t N0, int32_t N1, int32_t family, int32_t* tile);
+int pty_set_frame_tile(int32_t N0, int32_t N1, int32_t family, int32_t tile);
 const char* pty_last_error(void);
 int pty_version(void);
 /* Kernels this library has launched in the process so far (direct launches

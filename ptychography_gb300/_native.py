@@ -60,8 +60,8 @@ SIGNATURES = {
     "pty_shape_supported": [c_int32, c_int32],
     "pty_frame_tile_candidates": [c_int32, c_int32, ctypes.POINTER(c_int32), c_int32,
                                   ctypes.POINTER(c_int32)],
-    "pty_get_frame_tile": [c_int32, c_int32, ctypes.POINTER(c_int32)],
-    "pty_set_frame_tile": [c_int32, c_int32, c_int32],
+    "pty_get_frame_tile": [c_int32, c_int32, c_int32, ctypes.POINTER(c_int32)],
+    "pty_set_frame_tile": [c_int32, c_int32, c_int32, c_int32],
     "pty_last_error": [],
     "pty_version": [],
     "pty_launch_count": [],

@@ -47,7 +47,8 @@ struct ClusterCfg {
   static constexpr int A = LineGeom<N>::A, B = LineGeom<N>::B;  // rows and columns alike
   // 256 threads per CTA for 8- and 16-CTA clusters and frames up to 192^2
   // (two CTAs per SM where the shared memory allows), else 512
-  static constexpr int NT = (C >= 8 || N <= 192) ? 256 : 512;
+  // 128 threads for 256^2 frames on 16 CTAs (four clusters' CTAs per SM)
+  static constexpr int NT = (N == 256 && C == 16) ? 128 : (C >= 8 || N <= 192) ? 256 : 512;
   static constexpr int RPC = N / C;          // rows owned per CTA
   static constexpr int CPC = N / C;          // columns owned per CTA
   static constexpr int CP = CPC + 1;         // column-buffer pitch (float2), odd
@@ -58,11 +59,13 @@ struct ClusterCfg {
   static constexpr size_t CBUF = (size_t)N * CP + N / A;  // + one skew slot per A rows
   static constexpr size_t RSCR = (size_t)RF * ROWLEN;
   static constexpr size_t SMEM = (CBUF + RSCR + N) * sizeof(float2) + 32 * sizeof(double);
-  static_assert(RPC % RF == 0 && CPC % CW == 0 && CPC % A == 0 && CW >= 16, "cluster split");
+  static_assert(RPC % RF == 0 && CPC % CW == 0 && CPC % A == 0 && CW >= 8, "cluster split");
   static_assert(SMEM <= 227 * 1024, "shared memory budget");
   // the column pass exchanges through the (then idle) row scratch
   static_assert((size_t)N * CW <= RSCR, "column exchange fits the row scratch");
-  static constexpr int MINB = SMEM <= 113 * 1024 ? 2 : 1;   // CTAs per SM the budget allows
+  // CTAs per SM the shared-memory budget allows (1 KB per CTA reserved by the system)
+  static constexpr int MINB_SMEM = (int)((228 * 1024) / (SMEM + 1024));
+  static constexpr int MINB = MINB_SMEM > 4 ? 4 : (MINB_SMEM < 1 ? 1 : MINB_SMEM);
 };
 
 template <int N, int C, int OP>
@@ -187,7 +190,12 @@ __global__ void __launch_bounds__(ClusterCfg<N, C>::NT, ClusterCfg<N, C>::MINB)
 
   if (g.err_part) {
     const double sum = block_sum_d(ff_to_double(err), red);
-    if (tid == 0) g.err_part[(size_t)f * C + rank] = sum;
+    if (tid == 0) {
+      double* ep = g.err_part + (size_t)f * g.err_stride;
+      ep[rank] = sum;
+      if (rank == 0)
+        for (int k = C; k < g.err_stride; ++k) ep[k] = 0.0;   // slots of larger tiles
+    }
   }
 }
 

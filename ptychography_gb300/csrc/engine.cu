@@ -62,8 +62,8 @@ struct pty_plan {
   int Km = 1;                    // background-mean frame chunks
   float2* d_mean_part = nullptr;
   double* d_err_part = nullptr;  // [n * eslots]
-  int tile = 1;                  // CTAs per frame of the fused frame kernels
-  int eslots = 1;                // error partials per frame (one per CTA)
+  int tile[2] = {1, 1};          // CTAs per frame of the fused frame kernels, per op family
+  int eslots = 1;                // error-partial slots per frame (the largest tile built)
   int ndn = 304;                 // diffnorm blocks per array (two per SM)
   double* d_dn_part = nullptr;   // [2 arrays][ndn][2]
   int* d_shift = nullptr;
@@ -204,8 +204,9 @@ extern "C" int pty_plan_create(const pty_geometry* g, const int64_t* R_host, pty
   if ((rc = dalloc_t(p, &p->d_part_num, (size_t)p->K * npix))) return fail(rc);
   if ((rc = dalloc_t(p, &p->d_part_den, (size_t)p->K * npix))) return fail(rc);
   if ((rc = dalloc_t(p, &p->d_mean_part, (size_t)(p->Km > p->K ? p->Km : p->K) * npix))) return fail(rc);
-  if ((rc = choose_frame_tile(N0, N1, &p->tile))) return fail(rc);
-  p->eslots = p->tile;
+  if ((rc = choose_frame_tile(N0, N1, FAM_PLAIN, &p->tile[FAM_PLAIN]))) return fail(rc);
+  if ((rc = choose_frame_tile(N0, N1, FAM_BG, &p->tile[FAM_BG]))) return fail(rc);
+  p->eslots = max_frame_tile(N0, N1);
   if ((rc = dalloc_t(p, &p->d_err_part, (size_t)n * p->eslots))) return fail(rc);
   if ((rc = dalloc_t(p, &p->d_dn_part, (size_t)4 * p->ndn))) return fail(rc);
   if ((rc = dalloc_t(p, &p->d_shift, 2))) return fail(rc);
@@ -248,11 +249,12 @@ static FrameArgs base_args(const pty_plan* p) {
   a.amp_stride = (long long)p->N0 * p->N1;
   a.N0h = p->N0 / 2;
   a.N1h = p->N1 / 2;
+  a.err_stride = p->eslots;
   return a;
 }
 
 static int frame_op(const pty_plan* p, int op, const FrameArgs& a, int nframes, cudaStream_t st) {
-  return launch_frame_op(op, p->N0, p->N1, p->tile, a, nframes, st);
+  return launch_frame_op(op, p->N0, p->N1, p->tile[frame_family(op)], a, nframes, st);
 }
 
 // Pmod_P (era.py:597-610): the probe as a single frame through the Pmod_1 path

@@ -36,7 +36,8 @@ struct FrameArgs {
   float* bg_out;             // [n][N0][N1] per-frame background written (or DM state)
   const float* b0;           // [N0][N1] mean background (DM m4-6, model error)
   float* out_real;           // [n][N0][N1] intensities (OP_INTENS)
-  double* err_part;          // [n] per-frame error partials, or nullptr
+  double* err_part;          // [n][err_stride] per-frame error partials, or nullptr
+  int err_stride;            // partial slots per frame (>= CTAs per frame; the rest zeroed)
   float alpha;
   int N0h, N1h;              // N0 / 2, N1 / 2 (back-projection index roll)
   const float2* tw0;         // twiddles of the column transform (length N0)
@@ -47,9 +48,16 @@ struct FrameArgs {
 // kernel (frame_kernels.cu), tile C > 1 the C-CTA cluster kernel
 // (cluster_frame.cuh).  frame_tiles.cu lists the tiles built per shape and
 // picks one per shape and device (autotuned, or forced by the caller).
+// Op families tuned separately: the background forms (Pmod_7: EXIT7, PSI7,
+// DM7) move 28 N^2 bytes per frame and hold more registers than the rest.
+enum FrameFamily { FAM_PLAIN = 0, FAM_BG = 1 };
+inline int frame_family(int op) {
+  return (op == OP_EXIT7 || op == OP_PSI7 || op == OP_DM7) ? FAM_BG : FAM_PLAIN;
+}
 bool frame_shape_supported(int N0, int N1);
 int frame_tile_candidates(int N0, int N1, int* tiles, int cap);   // returns the count
-int choose_frame_tile(int N0, int N1, int* tile);                  // prepares the kernels too
+int max_frame_tile(int N0, int N1);
+int choose_frame_tile(int N0, int N1, int family, int* tile);      // prepares the kernels too
 int launch_frame_op(int op, int N0, int N1, int tile, const FrameArgs& a, int nframes,
                     cudaStream_t st);
 void make_twiddles(int L, float2* out);   // host table tw[k1 * A + t], length L
@@ -63,6 +71,7 @@ PTY_DECLARE_CLUSTER_TILE(128, 2)
 PTY_DECLARE_CLUSTER_TILE(192, 2)
 PTY_DECLARE_CLUSTER_TILE(256, 4)
 PTY_DECLARE_CLUSTER_TILE(256, 8)
+PTY_DECLARE_CLUSTER_TILE(256, 16)
 PTY_DECLARE_CLUSTER_TILE(512, 16)
 #undef PTY_DECLARE_CLUSTER_TILE
 

@@ -177,7 +177,11 @@ __global__ void __launch_bounds__(FrameCfg<N0, N1>::NT, 1) frame_kernel(FrameArg
 
   if (g.err_part) {
     const double s = block_sum_d(ff_to_double(err), red);
-    if (tid == 0) g.err_part[f] = s;
+    if (tid == 0) {
+      double* ep = g.err_part + (size_t)f * g.err_stride;
+      ep[0] = s;
+      for (int k = 1; k < g.err_stride; ++k) ep[k] = 0.0;   // slots of cluster tiles
+    }
   }
 }
 

@@ -7,16 +7,22 @@
 // depends on the GPU's shared memory, register file and cluster scheduling:
 //
 //   128^2: 1 CTA of 512 threads (one per SM) or 2-CTA clusters of 256 (two per SM)
-//   256^2: 8-CTA clusters of 256 threads (two per SM) or 4-CTA clusters of 512
+//   256^2: 8-CTA clusters of 256 threads (two CTAs per SM), 4-CTA clusters of
+//          512 (one per SM) or 16-CTA clusters of 128 (four per SM)
 //
-// The first plan created for a shape on a device times every candidate on a
-// scratch batch of frames (OP_PSI1, the plain modulus projection, three timed
-// launches each after a warm-up, fastest kept) and keeps the winner for the
-// process.  PTY_AUTOTUNE=0 in the environment skips the timing and takes the
-// first candidate listed; pty_set_frame_tile forces a tile.  Every tile runs
-// the same line transforms in the same order, so the exit waves, object and
-// probe do not depend on the choice; only the summation order of the
-// per-frame error partials (one per CTA) does.
+// Tiles are chosen per op family: the background (Pmod_7) forms move more
+// bytes and hold more registers than the plain ones, and the fastest tile
+// differs between them.  The first plan created for a shape on a device times
+// every candidate on a scratch batch of frames (about 256 MiB of waves) --
+// OP_PSI1 for the plain family, OP_PSI7 for the background family; five timed
+// launches each after a warm-up, fastest kept -- and keeps the winners for the
+// process; a candidate replaces the first-listed default only when at least
+// 3 % faster.
+// PTY_AUTOTUNE=0 in the environment skips the timing and takes the first
+// candidate listed; pty_set_frame_tile forces a tile.  Every tile runs the
+// same line transforms in the same order, so the exit waves, object and probe
+// do not depend on the choice; only the summation order of the per-frame
+// error partials (one per CTA) does.
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
@@ -34,13 +40,13 @@ namespace {
 
 struct ShapeTiles {
   int N0, N1, count;
-  int tiles[3];   // first = default without autotuning
+  int tiles[4];   // first = default without autotuning
 };
 
 constexpr ShapeTiles kShapes[] = {
-    {32, 32, 1, {1, 0, 0}},     {64, 64, 1, {1, 0, 0}},   {32, 64, 1, {1, 0, 0}},
-    {128, 128, 2, {1, 2, 0}},   {192, 192, 1, {2, 0, 0}}, {256, 256, 2, {8, 4, 0}},
-    {512, 512, 1, {16, 0, 0}},
+    {32, 32, 1, {1, 0, 0, 0}},   {64, 64, 1, {1, 0, 0, 0}},   {32, 64, 1, {1, 0, 0, 0}},
+    {128, 128, 2, {1, 2, 0, 0}}, {192, 192, 1, {2, 0, 0, 0}}, {256, 256, 3, {8, 4, 16, 0}},
+    {512, 512, 1, {16, 0, 0, 0}},
 };
 
 const ShapeTiles* find_shape(int N0, int N1) {
@@ -61,11 +67,12 @@ int prepare_tile(int N0, int N1, int tile) {
   if (N0 == 192 && N1 == 192 && tile == 2) return prepare_cluster_192x2();
   if (N0 == 256 && N1 == 256 && tile == 4) return prepare_cluster_256x4();
   if (N0 == 256 && N1 == 256 && tile == 8) return prepare_cluster_256x8();
+  if (N0 == 256 && N1 == 256 && tile == 16) return prepare_cluster_256x16();
   if (N0 == 512 && N1 == 512 && tile == 16) return prepare_cluster_512x16();
   return set_error(PTY_ERR_UNSUPPORTED, "frame tile not built for this shape");
 }
 
-using Key = std::tuple<int, int, int>;   // device, N0, N1
+using Key = std::tuple<int, int, int, int>;   // device, N0, N1, family
 std::mutex g_mu;
 std::map<Key, int> g_tile;               // chosen tile per device and shape
 
@@ -74,22 +81,25 @@ bool autotune_enabled() {
   return !(v && std::strcmp(v, "0") == 0);
 }
 
-// Times OP_PSI1 with each candidate tile on F scratch frames; *best = fastest.
-int tune(const ShapeTiles* s, int* best) {
+// Times the family's op (OP_PSI1 / OP_PSI7) with each candidate tile on F
+// scratch frames; *best = fastest.
+int tune(const ShapeTiles* s, int family, int* best) {
   const int N0 = s->N0, N1 = s->N1;
   const size_t npix = (size_t)N0 * N1;
-  // about 64 MiB of exit waves: larger than one wave of CTAs, small next to HBM
-  size_t F = ((size_t)64 << 20) / (npix * sizeof(float2));
+  // about 256 MiB of exit waves: several waves of CTAs, larger than L2
+  size_t F = ((size_t)256 << 20) / (npix * sizeof(float2));
   if (F < 64) F = 64;
-  if (F > 2048) F = 2048;
+  if (F > 8192) F = 8192;
   float2 *psi = nullptr, *tw0 = nullptr, *tw1 = nullptr;
-  float* amp = nullptr;
+  float *amp = nullptr, *bg = nullptr;
   double* err = nullptr;
+  const int op = family == FAM_BG ? OP_PSI7 : OP_PSI1;
   cudaStream_t st = nullptr;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   int rc = PTY_OK;
   cudaError_t e = cudaMalloc(&psi, F * npix * sizeof(float2));
   if (e == cudaSuccess) e = cudaMalloc(&amp, F * npix * sizeof(float));
+  if (e == cudaSuccess && family == FAM_BG) e = cudaMalloc(&bg, F * npix * sizeof(float));
   if (e == cudaSuccess) e = cudaMalloc(&err, F * 16 * sizeof(double));
   if (e == cudaSuccess) e = cudaMalloc(&tw0, N0 * sizeof(float2));
   if (e == cudaSuccess) e = cudaMalloc(&tw1, N1 * sizeof(float2));
@@ -105,6 +115,7 @@ int tune(const ShapeTiles* s, int* best) {
     // finite positive values (every byte 0x3c) in the waves and amplitudes
     if (e == cudaSuccess) e = cudaMemsetAsync(psi, 0x3c, F * npix * sizeof(float2), st);
     if (e == cudaSuccess) e = cudaMemsetAsync(amp, 0x3c, F * npix * sizeof(float), st);
+    if (e == cudaSuccess && bg) e = cudaMemsetAsync(bg, 0x3c, F * npix * sizeof(float), st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   }
   if (e != cudaSuccess) rc = set_cuda_error(e, "frame tile autotuner set-up");
@@ -117,17 +128,21 @@ int tune(const ShapeTiles* s, int* best) {
     a.amp = amp;
     a.amp_stride = (long long)npix;
     a.err_part = err;
+    a.err_stride = 16;
+    a.bg_in = bg;
+    a.bg_out = bg;
+    a.bg_stride = (long long)npix;
     a.alpha = 1e-10f;
     a.tw0 = tw0;
     a.tw1 = tw1;
     a.N0h = N0 / 2;
     a.N1h = N1 / 2;
     if ((rc = prepare_tile(N0, N1, tile))) break;
-    if ((rc = launch_frame_op(OP_PSI1, N0, N1, tile, a, (int)F, st))) break;
+    if ((rc = launch_frame_op(op, N0, N1, tile, a, (int)F, st))) break;
     float ms_min = INFINITY;
-    for (int r = 0; r < 3 && rc == PTY_OK; ++r) {
+    for (int r = 0; r < 5 && rc == PTY_OK; ++r) {
       e = cudaEventRecord(e0, st);
-      if (e == cudaSuccess && (rc = launch_frame_op(OP_PSI1, N0, N1, tile, a, (int)F, st))) break;
+      if (e == cudaSuccess && (rc = launch_frame_op(op, N0, N1, tile, a, (int)F, st))) break;
       if (e == cudaSuccess) e = cudaEventRecord(e1, st);
       if (e == cudaSuccess) e = cudaEventSynchronize(e1);
       float ms = 0.f;
@@ -135,7 +150,9 @@ int tune(const ShapeTiles* s, int* best) {
       if (e != cudaSuccess) rc = set_cuda_error(e, "frame tile autotuner timing");
       else if (ms < ms_min) ms_min = ms;
     }
-    if (rc == PTY_OK && ms_min < best_ms) {
+    // another tile replaces the default only when at least 3 % faster, so
+    // timing noise between near-equal tiles does not flip the choice
+    if (rc == PTY_OK && (i == 0 || ms_min < 0.97f * best_ms)) {
       best_ms = ms_min;
       *best = tile;
     }
@@ -146,6 +163,7 @@ int tune(const ShapeTiles* s, int* best) {
   if (st) cudaStreamDestroy(st);
   cudaFree(psi);
   cudaFree(amp);
+  cudaFree(bg);
   cudaFree(err);
   cudaFree(tw0);
   cudaFree(tw1);
@@ -169,19 +187,27 @@ int frame_tile_candidates(int N0, int N1, int* tiles, int cap) {
   return s->count;
 }
 
-int choose_frame_tile(int N0, int N1, int* tile) {
+int max_frame_tile(int N0, int N1) {
+  const ShapeTiles* s = find_shape(N0, N1);
+  int m = 1;
+  for (int i = 0; s && i < s->count; ++i) m = s->tiles[i] > m ? s->tiles[i] : m;
+  return m;
+}
+
+int choose_frame_tile(int N0, int N1, int family, int* tile) {
   const ShapeTiles* s = find_shape(N0, N1);
   if (!s) return set_error(PTY_ERR_SHAPE, "frame shape not supported by the fused FFT kernels");
+  if (family != FAM_PLAIN && family != FAM_BG) return set_error(PTY_ERR_ARG, "unknown op family");
   int dev = 0;
   PTY_TRY(current_device(&dev));
   std::lock_guard<std::mutex> lock(g_mu);
-  const Key key{dev, N0, N1};
+  const Key key{dev, N0, N1, family};
   auto it = g_tile.find(key);
   int t = s->tiles[0];
   if (it != g_tile.end()) {
     t = it->second;
   } else {
-    if (s->count > 1 && autotune_enabled()) PTY_TRY(tune(s, &t));
+    if (s->count > 1 && autotune_enabled()) PTY_TRY(tune(s, family, &t));
     g_tile[key] = t;
   }
   PTY_TRY(prepare_tile(N0, N1, t));
@@ -198,6 +224,7 @@ int launch_frame_op(int op, int N0, int N1, int tile, const FrameArgs& a, int nf
     if (N0 == 192 && tile == 2) return launch_cluster_192x2(op, a, nframes, st);
     if (N0 == 256 && tile == 4) return launch_cluster_256x4(op, a, nframes, st);
     if (N0 == 256 && tile == 8) return launch_cluster_256x8(op, a, nframes, st);
+    if (N0 == 256 && tile == 16) return launch_cluster_256x16(op, a, nframes, st);
     if (N0 == 512 && tile == 16) return launch_cluster_512x16(op, a, nframes, st);
   }
   return set_error(PTY_ERR_UNSUPPORTED, "frame tile not built for this shape");
@@ -233,31 +260,32 @@ using namespace pty;
 extern "C" int pty_frame_tile_candidates(int32_t N0, int32_t N1, int32_t* tiles, int32_t cap,
                                          int32_t* count) {
   if (!count || (cap > 0 && !tiles)) return set_error(PTY_ERR_ARG, "null argument");
-  int buf[3] = {0, 0, 0};
-  const int n = frame_tile_candidates(N0, N1, buf, 3);
+  int buf[4] = {0, 0, 0, 0};
+  const int n = frame_tile_candidates(N0, N1, buf, 4);
   if (n == 0) return set_error(PTY_ERR_SHAPE, "frame shape not supported by the fused FFT kernels");
   for (int i = 0; i < n && i < cap; ++i) tiles[i] = buf[i];
   *count = n;
   return PTY_OK;
 }
 
-extern "C" int pty_get_frame_tile(int32_t N0, int32_t N1, int32_t* tile) {
+extern "C" int pty_get_frame_tile(int32_t N0, int32_t N1, int32_t family, int32_t* tile) {
   if (!tile) return set_error(PTY_ERR_ARG, "null argument");
   int t = 0;
-  PTY_TRY(choose_frame_tile(N0, N1, &t));
+  PTY_TRY(choose_frame_tile(N0, N1, family, &t));
   *tile = t;
   return PTY_OK;
 }
 
-extern "C" int pty_set_frame_tile(int32_t N0, int32_t N1, int32_t tile) {
+extern "C" int pty_set_frame_tile(int32_t N0, int32_t N1, int32_t family, int32_t tile) {
   const ShapeTiles* s = find_shape(N0, N1);
   if (!s) return set_error(PTY_ERR_SHAPE, "frame shape not supported by the fused FFT kernels");
+  if (family != FAM_PLAIN && family != FAM_BG) return set_error(PTY_ERR_ARG, "unknown op family");
   if (tile != 0 && !tile_listed(s, tile))
     return set_error(PTY_ERR_ARG, "tile not built for this frame shape");
   int dev = 0;
   PTY_TRY(current_device(&dev));
   std::lock_guard<std::mutex> lock(g_mu);
-  const Key key{dev, (int)N0, (int)N1};
+  const Key key{dev, (int)N0, (int)N1, (int)family};
   if (tile == 0) {
     g_tile.erase(key);
     return PTY_OK;

@@ -1,7 +1,7 @@
 """Frame tiles: every tile built for a shape gives the same exit waves.
 
 128 x 128 frames have a single-CTA kernel and a 2-CTA cluster kernel, 256 x 256
-frames 8- and 4-CTA cluster kernels.  Each tile, forced in turn, must match the
+frames 8-, 4- and 16-CTA cluster kernels.  Each tile, forced in turn, must match the
 oracle, and the exit waves, object and probe must be bit-identical across tiles
 (the same line transforms run in the same order); only the error sums, whose
 per-CTA partials are added in a different grouping, may differ in rounding.
@@ -34,21 +34,46 @@ class forced_tile:
         self.N, self.tile, self.lib = N, tile, _native.load()
 
     def __enter__(self):
-        _native.check(self.lib.pty_set_frame_tile(self.N, self.N, self.tile))
+        for fam in (0, 1):       # plain and background op families
+            _native.check(self.lib.pty_set_frame_tile(self.N, self.N, fam, self.tile))
 
     def __exit__(self, *a):
-        self.lib.pty_set_frame_tile(self.N, self.N, 0)
+        for fam in (0, 1):
+            self.lib.pty_set_frame_tile(self.N, self.N, fam, 0)
 
 
 @pytest.mark.parametrize("N", [128, 256])
 def test_tiles_listed_and_chosen(N):
     lib = _native.load()
     c = candidates(N)
-    assert len(c) == 2
-    t = ctypes.c_int32(0)
-    _native.check(lib.pty_get_frame_tile(N, N, ctypes.byref(t)))
-    assert t.value in c
-    assert lib.pty_set_frame_tile(N, N, 3) == 1       # PTY_ERR_ARG: tile not built
+    assert len(c) == {128: 2, 256: 3}[N]
+    for fam in (0, 1):
+        t = ctypes.c_int32(0)
+        _native.check(lib.pty_get_frame_tile(N, N, fam, ctypes.byref(t)))
+        assert t.value in c
+    assert lib.pty_set_frame_tile(N, N, 0, 3) == 1    # PTY_ERR_ARG: tile not built
+    assert lib.pty_set_frame_tile(N, N, 2, c[0]) == 1  # no such family
+
+
+def test_mixed_family_tiles_keep_error_sums():
+    """Plain and background ops on different tiles in one run: eMod unchanged."""
+    N = 256
+    I, R, P, O, M = small_problem(N, seed=5, side=3)
+    np.random.seed(4)
+    b = np.full((N, N), 0.3, np.float32)
+    ref = pty.ERA(I, R.copy(), P * np.exp(0.2j), None, 2, mask=M, method=6, background=b)
+    lib = _native.load()
+    try:
+        _native.check(lib.pty_set_frame_tile(N, N, 0, 16))
+        _native.check(lib.pty_set_frame_tile(N, N, 1, 4))
+        np.random.seed(4)
+        got = pty.ERA(I, R.copy(), P * np.exp(0.2j), None, 2, mask=M, method=6, background=b)
+    finally:
+        for fam in (0, 1):
+            lib.pty_set_frame_tile(N, N, fam, 0)
+    np.testing.assert_array_equal(got[0], ref[0])
+    np.testing.assert_array_equal(got[1], ref[1])
+    np.testing.assert_allclose(got[2]["eMod"], ref[2]["eMod"], rtol=1e-6)
 
 
 @pytest.mark.parametrize("N", [128, 256])
