@@ -41,6 +41,10 @@ namespace pty {
 PTY_DEV void cluster_sync_relaxed() {
   asm volatile("barrier.cluster.arrive.relaxed.aligned;\n\tbarrier.cluster.wait.aligned;" ::: "memory");
 }
+// The two halves of a cluster barrier with release / acquire ordering, so that
+// independent work (global loads) can be issued between arrival and wait.
+PTY_DEV void cluster_arrive_release() { asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory"); }
+PTY_DEV void cluster_wait_acquire() { asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory"); }
 
 template <int N, int C>
 struct ClusterCfg {
@@ -126,7 +130,13 @@ __global__ void __launch_bounds__(ClusterCfg<N, C>::NT, ClusterCfg<N, C>::MINB)
 #pragma unroll
     for (int j = 0; j < B; ++j) rc(j / JPC)[cidx(a, t + A * (j % JPC))] = v[j];
   }
-  cluster.sync();
+  // the modulus inputs of the first column sub-pass are loaded while the
+  // cluster barrier completes
+  ModIn<OP, B> m;
+  cluster_arrive_release();
+  if constexpr (ModIn<OP, B>::EARLY)
+    modulus_load<N, N, OP, A, B>(g, f, fbase, tid / CW, rank * CPC + tid % CW, m);
+  cluster_wait_acquire();
 
   // ---------------- 3. column pass on the owned columns
   // Lanes of a warp run along a row (coalesced amp / mask / background
@@ -141,6 +151,8 @@ __global__ void __launch_bounds__(ClusterCfg<N, C>::NT, ClusterCfg<N, C>::MINB)
     const int cw = tid % CW, tc = tid / CW;
     const int cl = s * CW + cw;
     const int kc = rank * CPC + cl;
+    // this sub-pass's amp / mask / background, in flight during the forward FFT
+    if (ModIn<OP, B>::EARLY && s > 0) modulus_load<N, N, OP, A, B>(g, f, fbase, tc, kc, m);
     float2 v[B];
 #pragma unroll
     for (int j = 0; j < B; ++j) v[j] = cbuf[cidx(tc + A * j, cl)];
@@ -150,7 +162,8 @@ __global__ void __launch_bounds__(ClusterCfg<N, C>::NT, ClusterCfg<N, C>::MINB)
     for (int k1 = 0; k1 < B; ++k1) xb[(k1 * A + tc) * CW + cw] = v[k1];
     __syncthreads();
     line_stage2<N, OpTraits<OP>::FIRST_DIR>(v, tc, [&](int tt, int k1) { return xb[(k1 * A + tt) * CW + cw]; });
-    frame_modulus_line<N, N, OP, A, B>(g, f, fbase, tc, kc, v, err);
+    if constexpr (!ModIn<OP, B>::EARLY) modulus_load<N, N, OP, A, B>(g, f, fbase, tc, kc, m);
+    modulus_apply<N, N, OP, A, B>(g, fbase, tc, kc, v, m, err);
     if constexpr (INVERSE) {
       line_stage1<N, +1>(v, tc, tw);
       __syncthreads();

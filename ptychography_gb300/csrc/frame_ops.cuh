@@ -49,13 +49,46 @@ PTY_DEV float2 frame_input(const FrameArgs& g, int f, int r0, int r1, const floa
   }
 }
 
-// The modulus constraint on one column line: v[j] = F[t + A j][kc].  All
-// global loads of the line are issued before any store, so their latencies
-// overlap (the output pointers may alias the inputs, which would otherwise
-// serialise every load behind the previous element's store).
+// The modulus constraint on one column line: v[j] = F[t + A j][kc], in two
+// halves so a kernel can issue the line's global loads early and overlap
+// their latency with the forward transform:
+//   modulus_load  -- amp, mask and background of the line into registers
+//   modulus_apply -- the constraint on v, the error sum, the background store
+// All loads of a line precede its stores (the output pointers may alias the
+// inputs, which would otherwise serialise every load behind the previous
+// element's store).
+template <int OP, int B>
+struct ModIn {
+  static constexpr bool BG_IN = (OP == OP_EXIT7 || OP == OP_PSI7 || OP == OP_MERR || OP == OP_MERR_PSI);
+  static constexpr bool BG_OUT = (OP == OP_EXIT7 || OP == OP_PSI7 || OP == OP_DM7);
+  static constexpr bool NEEDS = !(OP == OP_INTENS || OP == OP_BP);
+  // issued ahead of the forward transform, except for DM7 whose four input
+  // arrays would not fit the register budget alongside the transform
+  static constexpr bool EARLY = (OP != OP_DM7);
+  float am[B], mk[B], bb[B], b0v[B];
+};
+
 template <int N0, int N1, int OP, int A, int B>
-PTY_DEV void frame_modulus_line(const FrameArgs& g, int f, size_t fbase, int t, int kc,
-                                float2 (&v)[B], ff& err) {
+PTY_DEV void modulus_load(const FrameArgs& g, int f, size_t fbase, int t, int kc, ModIn<OP, B>& m) {
+  if constexpr (ModIn<OP, B>::NEEDS) {
+    const float* amp = g.amp + (size_t)g.amp_stride * f;
+#pragma unroll
+    for (int j = 0; j < B; ++j) {
+      const int pix = (t + A * j) * N1 + kc;
+      m.am[j] = __ldg(&amp[pix]);
+      m.mk[j] = g.mask ? (float)__ldg(&g.mask[pix]) : 1.0f;
+      if constexpr (ModIn<OP, B>::BG_IN) m.bb[j] = g.bg_in ? g.bg_in[(size_t)g.bg_stride * f + pix] : 0.0f;
+      if constexpr (OP == OP_DM7) {
+        m.bb[j] = g.bg_out[fbase + pix];
+        m.b0v[j] = __ldg(&g.b0[pix]);
+      }
+    }
+  }
+}
+
+template <int N0, int N1, int OP, int A, int B>
+PTY_DEV void modulus_apply(const FrameArgs& g, size_t fbase, int t, int kc, float2 (&v)[B],
+                           ModIn<OP, B>& m, ff& err) {
   if constexpr (OP == OP_INTENS) {
     const int sc = (kc + N1 / 2) % N1;   // fftshift, era.py:295
 #pragma unroll
@@ -71,64 +104,58 @@ PTY_DEV void frame_modulus_line(const FrameArgs& g, int f, size_t fbase, int t, 
     for (int j = 0; j < B; ++j) g.psi[fbase + (size_t)(t + A * j) * N1 + kc] = cscale(v[j], kInv);
     return;
   } else {
-    constexpr bool BG_IN = (OP == OP_EXIT7 || OP == OP_PSI7 || OP == OP_MERR || OP == OP_MERR_PSI);
-    constexpr bool BG_OUT = (OP == OP_EXIT7 || OP == OP_PSI7 || OP == OP_DM7);
-    float am[B], mk[B], bb[B], b0v[B];
     float line_err = 0.f;   // FP32 over one line (B terms), folded into err once
-    const float* amp = g.amp + (size_t)g.amp_stride * f;
-#pragma unroll
-    for (int j = 0; j < B; ++j) {
-      const int pix = (t + A * j) * N1 + kc;
-      am[j] = __ldg(&amp[pix]);
-      mk[j] = g.mask ? (float)__ldg(&g.mask[pix]) : 1.0f;
-      if constexpr (BG_IN) bb[j] = g.bg_in ? g.bg_in[(size_t)g.bg_stride * f + pix] : 0.0f;
-      if constexpr (OP == OP_DM7) {
-        bb[j] = g.bg_out[fbase + pix];
-        b0v[j] = __ldg(&g.b0[pix]);
-      }
-    }
 #pragma unroll
     for (int j = 0; j < B; ++j) {
       const float2 F = v[j];
+      const float am = m.am[j], mk = m.mk[j];
       // square roots and quotients use the hardware reciprocal square root
       // (a few ulp; the engine's tolerances are 1e-5 relative)
       if constexpr (OP == OP_EXIT1 || OP == OP_PSI1 || OP == OP_DM1) {
         // era.py:561-571: |F| + alpha, masked pixels keep F
         const float x2 = cabs2(F);
         const float mag = (x2 > 0.f ? x2 * rsqrtf(x2) : 0.f) + g.alpha;
-        const float d = mag - am[j];
-        line_err += d * d * mk[j];
-        const float fac = (mk[j] != 0.f) ? __fdividef(am[j], mag) : 1.0f;
+        const float d = mag - am;
+        line_err += d * d * mk;
+        const float fac = (mk != 0.f) ? __fdividef(am, mag) : 1.0f;
         v[j] = cscale(F, fac);
       } else if constexpr (OP == OP_EXIT7 || OP == OP_PSI7) {
         // era.py:584-594: sqrt(|F|^2 + b^2 + alpha), masked pixels zeroed
-        const float x2 = cabs2(F) + bb[j] * bb[j] + g.alpha;
+        const float x2 = cabs2(F) + m.bb[j] * m.bb[j] + g.alpha;
         const float rs = rsqrtf(x2);
-        const float d = x2 * rs - am[j];
-        line_err += d * d * mk[j];
-        const float fac = mk[j] * am[j] * rs;
+        const float d = x2 * rs - am;
+        line_err += d * d * mk;
+        const float fac = mk * am * rs;
         v[j] = cscale(F, fac);
-        bb[j] *= fac;
+        m.bb[j] *= fac;
       } else if constexpr (OP == OP_DM7) {
         // dm.py:219-224 on the background: g1 = g - b0 ; tb = b0 - g1 ; g = g1 + Pmod7(tb)
-        const float g1 = bb[j] - b0v[j];
-        const float tb = b0v[j] - g1;
-        const float fac = mk[j] * am[j] * rsqrtf(cabs2(F) + tb * tb + g.alpha);
+        const float g1 = m.bb[j] - m.b0v[j];
+        const float tb = m.b0v[j] - g1;
+        const float fac = mk * am * rsqrtf(cabs2(F) + tb * tb + g.alpha);
         v[j] = cscale(F, fac);
-        bb[j] = g1 + tb * fac;
+        m.bb[j] = g1 + tb * fac;
       } else if constexpr (OP == OP_MERR || OP == OP_MERR_PSI) {
         // dm.py:338-340, no alpha
-        const float x2 = cabs2(F) + bb[j] * bb[j];
-        const float d = (x2 > 0.f ? x2 * rsqrtf(x2) : 0.f) - am[j];
-        line_err += mk[j] * (d * d);
+        const float x2 = cabs2(F) + m.bb[j] * m.bb[j];
+        const float d = (x2 > 0.f ? x2 * rsqrtf(x2) : 0.f) - am;
+        line_err += mk * (d * d);
       }
     }
     err = ff_add(err, line_err);
-    if constexpr (BG_OUT) {
+    if constexpr (ModIn<OP, B>::BG_OUT) {
 #pragma unroll
-      for (int j = 0; j < B; ++j) g.bg_out[fbase + (size_t)(t + A * j) * N1 + kc] = bb[j];
+      for (int j = 0; j < B; ++j) g.bg_out[fbase + (size_t)(t + A * j) * N1 + kc] = m.bb[j];
     }
   }
+}
+
+template <int N0, int N1, int OP, int A, int B>
+PTY_DEV void frame_modulus_line(const FrameArgs& g, int f, size_t fbase, int t, int kc,
+                                float2 (&v)[B], ff& err) {
+  ModIn<OP, B> m;
+  modulus_load<N0, N1, OP, A, B>(g, f, fbase, t, kc, m);
+  modulus_apply<N0, N1, OP, A, B>(g, fbase, t, kc, v, m, err);
 }
 
 // The result of the inverse transform for one row line (v[j] at column
