@@ -491,7 +491,7 @@ def peaks():
         return 6800.0, "fallback"
 
 
-def roofline_pmod7(job, torch, tile, reps=20):
+def roofline_pmod7(job, torch, tile, sm_max_mhz, reps=20):
     """Fused frame kernel (Pmod_7 form, the DM m6 modulus step) alone, event-timed.
 
     Algorithmic bytes per frame: psi read 8 N^2 + psi write 8 N^2 + amp 4 N^2 +
@@ -506,18 +506,28 @@ def roofline_pmod7(job, torch, tile, reps=20):
         fn()
     t = event_time(torch, fn, reps) / reps
     bytes_ = 28.0 * job.N * job.N * job.n
-    # DRAM bytes (read + write) of one launch from the ncu capture in
-    # profiles/cluster_frame_kernel_psi7_256x256x256.md (410.0 MB for 256 frames),
-    # scaled by frames; recorded for the 256 x 256 kernel only
-    traffic = round(410.0e6 * job.n / 256) if (job.N == 256 and tile == 8) else None
+    # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one ncu
+    # capture of this kernel (256^2 frames, 8-CTA tile): 880.7 MB for 512
+    # frames, scaled by frames; recorded for that kernel only
+    traffic = round(880.7e6 * job.n / 512) if (job.N == 256 and tile == 8) else None
     kname = ("cluster_frame_kernel<%d,%d,PSI7>" % (job.N, tile) if tile > 1
              else "frame_kernel<%d,%d,PSI7>" % (job.N, job.N))
     pk, kind = peaks()
     gbs = bytes_ / t / 1e9
+    # FP32 side: 5 N^2 log2(N^2) flops per 2-D transform, forward + inverse,
+    # against 2 flops x 128 FP32 lanes x SMs x the SM clock
+    flops = 10.0 * job.N * job.N * math.log2(job.N * job.N) * job.n
+    props = torch.cuda.get_device_properties(job.dev)
+    fp32_peak = 2 * 128 * props.multi_processor_count * sm_max_mhz * 1e6
     return {"kernel": kname,
             "bound": "hbm", "achieved": round(gbs, 1), "peak": pk, "unit": "GB/s",
             "frac": round(gbs / pk, 4), "peak_kind": kind, "traffic": traffic,
-            "launch_ms": round(t * 1e3, 4), "algorithmic_bytes": bytes_}
+            "launch_ms": round(t * 1e3, 4), "algorithmic_bytes": bytes_,
+            "fp32": {"flops_per_launch": flops, "achieved_tflops": round(flops / t / 1e12, 2),
+                     "peak_tflops": round(fp32_peak / 1e12, 1),
+                     "frac": round(flops / t / fp32_peak, 4),
+                     "peak_kind": "nominal: 2 x 128 lanes x %d SMs x %d MHz"
+                                  % (props.multi_processor_count, sm_max_mhz)}}
 
 
 def era_m1_rate(job, torch, K):
@@ -782,7 +792,7 @@ def main():
         t_ = ctypes.c_int32(0)
         _native.check(lib.pty_get_frame_tile(job.N, job.N, fam, ctypes.byref(t_)))
         tiles.append(int(t_.value))
-    roof = roofline_pmod7(job, torch, tiles[1])
+    roof = roofline_pmod7(job, torch, tiles[1], clk.summary()["sm_max_mhz"] or 2070)
     m1 = era_m1_rate(job, torch, max(args.steps, 10)) if args.workload == "c1" else None
     job.close()
     if rank != 0:

@@ -63,7 +63,7 @@ struct pty_plan {
   float2* d_mean_part = nullptr;
   double* d_err_part = nullptr;  // [n * eslots]
   int tile[2] = {1, 1};          // CTAs per frame of the fused frame kernels, per op family
-  int eslots = 1;                // error-partial slots per frame (the largest tile built)
+  int eslots = 1;                // error-partial slots per frame (the larger family tile)
   int ndn = 304;                 // diffnorm blocks per array (two per SM)
   double* d_dn_part = nullptr;   // [2 arrays][ndn][2]
   int* d_shift = nullptr;
@@ -206,7 +206,7 @@ extern "C" int pty_plan_create(const pty_geometry* g, const int64_t* R_host, pty
   if ((rc = dalloc_t(p, &p->d_mean_part, (size_t)(p->Km > p->K ? p->Km : p->K) * npix))) return fail(rc);
   if ((rc = choose_frame_tile(N0, N1, FAM_PLAIN, &p->tile[FAM_PLAIN]))) return fail(rc);
   if ((rc = choose_frame_tile(N0, N1, FAM_BG, &p->tile[FAM_BG]))) return fail(rc);
-  p->eslots = max_frame_tile(N0, N1);
+  p->eslots = p->tile[0] > p->tile[1] ? p->tile[0] : p->tile[1];
   if ((rc = dalloc_t(p, &p->d_err_part, (size_t)n * p->eslots))) return fail(rc);
   if ((rc = dalloc_t(p, &p->d_dn_part, (size_t)4 * p->ndn))) return fail(rc);
   if ((rc = dalloc_t(p, &p->d_shift, 2))) return fail(rc);

@@ -359,8 +359,17 @@ __global__ void finalize_kernel(const double* __restrict__ err_part, int n,
                                 const double* __restrict__ dn_part, int ndn, double I_norm,
                                 double* hist_emod, double* hist_econ, int it) {
   __shared__ double red[32];
-  double e = 0.0, d = 0.0, c = 0.0;
-  for (int i = threadIdx.x; i < n; i += blockDim.x) e += err_part[i];
+  double d = 0.0, c = 0.0;
+  // four independent running sums per thread keep four loads in flight
+  double e4[4] = {0.0, 0.0, 0.0, 0.0};
+  const int stride = 4 * blockDim.x;
+  int i0 = threadIdx.x;
+  for (; i0 + 3 * (int)blockDim.x < n; i0 += stride)
+#pragma unroll
+    for (int k = 0; k < 4; ++k) e4[k] += err_part[i0 + k * blockDim.x];
+  for (int k = 0; k < 4; ++k)
+    if (i0 + k * (int)blockDim.x < n) e4[k] += err_part[i0 + k * blockDim.x];
+  double e = (e4[0] + e4[1]) + (e4[2] + e4[3]);
   for (int i = threadIdx.x; i < ndn; i += blockDim.x) {
     d += dn_part[2 * i];
     c += dn_part[2 * i + 1];
@@ -376,7 +385,7 @@ __global__ void finalize_kernel(const double* __restrict__ err_part, int n,
 
 int launch_finalize(const double* err_part, int n, const double* dn_part, int ndn, double I_norm,
                     double* hist_emod, double* hist_econ, int it, cudaStream_t st) {
-  finalize_kernel<<<1, 256, 0, st>>>(err_part, n, dn_part, ndn, I_norm, hist_emod, hist_econ, it);
+  finalize_kernel<<<1, 1024, 0, st>>>(err_part, n, dn_part, ndn, I_norm, hist_emod, hist_econ, it);
   return check_launch("finalize_kernel");
 }
 
