@@ -1,5 +1,5 @@
 // Per-pixel pieces of the fused frame kernels, shared by the one-CTA-per-frame
-// kernel (frame_kernels.cu) and the cluster-per-frame kernel (cluster_kernels.cu):
+// kernel (frame_kernels.cu) and the cluster-per-frame kernel (cluster_frame.cuh):
 //   frame_input   -- the wave entering the forward FFT at detector pixel (a, b)
 //   frame_modulus -- the constraint applied to F at frequency (kr, kc)
 //   frame_output  -- what is written back after the inverse FFT
