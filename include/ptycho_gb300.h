@@ -139,6 +139,13 @@ int pty_background_mean(pty_plan* plan, const float* background, float* mean_out
  * I is float32 (is_double = 0) or float64 (is_double = 1), centred order. */
 int pty_amp_from_intensity(pty_plan* plan, const void* I, int32_t is_double, float* amp,
                            void* stream);
+/* pty_amp_from_intensity plus I_norm = sum(mask * I) over all frames
+ * (era.py:495) into the device double *norm, summed in double in a fixed
+ * order (a deterministic value, within rounding of the reference's sum in I's
+ * dtype).  mask: the device uint8 mask in unshifted order (as pty_era takes
+ * it), or NULL for all pixels. */
+int pty_amp_and_norm(pty_plan* plan, const void* I, int32_t is_double, const uint8_t* mask,
+                     float* amp, double* norm, void* stream);
 /* Probe update for callers that cannot allocate device memory.  No
  * counterpart in the reference: it computes what pty_psup_P computes
  * (psup_P, era.py:371-400) without a plan, for code that must not call
@@ -158,6 +165,18 @@ int pty_amp_from_intensity(pty_plan* plan, const void* I, int32_t is_double, flo
 int pty_psup_P_noalloc(const pty_geometry* geom, const int64_t* R_host, const void* psi,
                        const void* O, double* O_heatmap, int32_t recompute_heatmap, double alpha,
                        void* P_out, void* stream);
+/* The random initial background of methods 4-6 (era.py:539-540:
+ * np.random.random((n, N0, N1)).astype(dtype) + 0.1) drawn on the device from
+ * NumPy's legacy global generator.  key[624] / pos: the MT19937 state as
+ * np.random.get_state() returns it (host memory); count doubles are drawn
+ * (n * N0 * N1), out[i] = float32(dtype(u_i) + 0.1) with dtype float64 when
+ * rdt_double, else float32 (device memory); key_out[624] / *pos_out: the state
+ * after the draw, to be handed back with np.random.set_state.  Synchronises
+ * the stream. */
+int pty_legacy_random_background(const uint32_t* key, int32_t pos, int64_t count,
+                                 int32_t rdt_double, float* out, uint32_t* key_out,
+                                 int32_t* pos_out, void* stream);
+
 /* 1 if the frame shape N0 x N1 has a fused FFT kernel. */
 int pty_shape_supported(int32_t N0, int32_t N1);
 

@@ -3,11 +3,14 @@ one C-ABI call for the whole loop, and the reference's return values.
 
 Host work mirrors ``preamble`` (ptychography/era.py:435-548): the method and
 update choice, the dtype rule, the default object of ones, the random initial
-probe and background drawn from NumPy's global RNG in the reference's order,
-``I_norm``, and the in-place shift of ``R``.  Everything else (amplitudes,
-exit waves, FFTs, projections, metrics) runs on the GPU in libptycho_gb300.
-Bulk arithmetic is complex64; ``dtype='double'`` only sets the dtype of the
-returned arrays.
+probe drawn from NumPy's global RNG, and the in-place shift of ``R``.  The
+random initial background (era.py:539-540) is the next draw of that same
+generator; on the public path it is drawn on the GPU from the generator's state
+(``device_random_background``), which is then advanced exactly as the host
+draw would have advanced it.  ``I_norm`` (era.py:495) is summed on the GPU in
+the pass that forms the amplitudes.  Everything else (exit waves, FFTs,
+projections, metrics) runs on the GPU in libptycho_gb300.  Bulk arithmetic is
+complex64; ``dtype='double'`` only sets the dtype of the returned arrays.
 """
 import ctypes
 import math
@@ -57,7 +60,8 @@ def pmod_probe_count(Pmod_probe, iters):
 class Preamble:
     """Host set-up shared by ERA and DM (era.py:435-548), without exit waves."""
 
-    def __init__(self, I, R, P, O, OP_iters, mask, background, method, dtype):
+    def __init__(self, I, R, P, O, OP_iters, mask, background, method, dtype,
+                 host_background_draw=True, host_norm=True):
         I = np.asarray(I)
         if I.ndim != 3:
             raise ValueError("I must be (n_frames, N0, N1)")
@@ -86,14 +90,21 @@ class Preamble:
         if self.P.shape != (N0, N1):
             raise ValueError("P must have the frame shape %s" % ((N0, N1),))
         scalar_mask = np.ndim(mask) == 0
+        # I_norm (era.py:495); with host_norm=False and a 0/1 mask it is left to
+        # the device (None here, norm_scale the scalar mask's value)
+        self.norm_scale = 1.0
         if scalar_mask:
             mask_arr = None
-            self.I_norm = float(np.sum(mask * I, dtype=np.float64))
+            if host_norm:
+                self.I_norm = float(np.sum(mask * I, dtype=np.float64))
+            else:
+                self.I_norm, self.norm_scale = None, float(mask)
         else:
             mask = np.asarray(mask)
             if mask.shape != (N0, N1):
                 raise ValueError("mask must have the frame shape %s" % ((N0, N1),))
-            self.I_norm = float(np.sum(mask * I))
+            binary = mask.dtype == np.bool_ or bool(np.all((mask == 0) | (mask == 1)))
+            self.I_norm = None if (binary and not host_norm) else float(np.sum(mask * I))
             mask_arr = np.ascontiguousarray(np.fft.ifftshift(mask) != 0).astype(np.uint8)
         self.mask = mask_arr
         self.I = I
@@ -102,13 +113,23 @@ class Preamble:
         self.R = R
         self.n, self.N0, self.N1 = n, N0, N1
         self.background = None
+        self.background_pattern = None
+        self.random_background = False
         if self.method in (4, 5, 6):                              # era.py:539-544
-            if background is None:
+            if background is None and not host_background_draw:
+                # drawn later on the device from the same generator state
+                # (device_random_background), the next draw of the global RNG
+                self.random_background = True
+            elif background is None:
                 self.background = (np.random.random((n, N0, N1)).astype(self.rdt) + 0.1).astype(np.float32)
             else:
                 b = np.sqrt(np.fft.ifftshift(np.asarray(background, dtype=np.float64)))
-                self.background = np.ascontiguousarray(
-                    np.broadcast_to(b.astype(np.float32), (n, N0, N1)))
+                if host_background_draw:
+                    self.background = np.ascontiguousarray(
+                        np.broadcast_to(b.astype(np.float32), (n, N0, N1)))
+                else:
+                    # one frame's pattern; copied to every frame on the device
+                    self.background_pattern = np.ascontiguousarray(b.astype(np.float32))
         self.user_background = background
         Pamp = np.fft.fftn(self.P, axes=(-2, -1))                 # era.py:546-547
         self.Pamp = np.sqrt((Pamp.conj() * Pamp).real).astype(np.float32)
@@ -118,6 +139,23 @@ def _ptr(t):
     return ctypes.c_void_p(t.data_ptr()) if t is not None else None
 
 
+def device_random_background(lib, out, rdt, sp):
+    """np.random.random(out.shape).astype(rdt) + 0.1 (as float32) into the
+    device tensor `out`, drawn on the GPU from NumPy's global legacy generator,
+    which is then advanced exactly as the host draw would have advanced it."""
+    st = np.random.get_state()
+    if st[0] != "MT19937":
+        raise RuntimeError("NumPy's global generator is not MT19937")
+    key = np.ascontiguousarray(st[1], dtype=np.uint32)
+    key_out = np.empty(624, dtype=np.uint32)
+    pos_out = ctypes.c_int32(0)
+    u32p = ctypes.POINTER(ctypes.c_uint32)
+    _native.check(lib.pty_legacy_random_background(
+        key.ctypes.data_as(u32p), int(st[2]), int(out.numel()), int(rdt == np.float64),
+        _ptr(out), key_out.ctypes.data_as(u32p), ctypes.byref(pos_out), sp))
+    np.random.set_state((st[0], key_out, int(pos_out.value), st[3], st[4]))
+
+
 class _Job:
     """One reconstruction's plan and device buffers (era.py:435-548 set-up on the GPU)."""
 
@@ -125,7 +163,8 @@ class _Job:
                  Pmod_probe, probe_centering, alpha, dtype, full_output, use_graph):
         torch = _torch()
         self.lib, self.kind, self.full_output = lib, kind, full_output
-        pre = self.pre = Preamble(I, R, P, O, OP_iters, mask, background, method, dtype)
+        pre = self.pre = Preamble(I, R, P, O, OP_iters, mask, background, method, dtype,
+                                  host_background_draw=False, host_norm=False)
         self.iters = iters = int(iters)
         n, N0, N1 = pre.n, pre.N0, pre.N1
         U, V = pre.O.shape
@@ -141,14 +180,26 @@ class _Job:
                 Iin = Iin.astype(np.float64)
             I_d = torch.from_numpy(np.ascontiguousarray(Iin)).to(dev, non_blocking=False)
             amp = torch.empty((n, N0, N1), dtype=torch.float32, device=dev)
-            _native.check(lib.pty_amp_from_intensity(self.plan, _ptr(I_d),
-                                                     int(Iin.dtype == np.float64), _ptr(amp), sp))
+            mask_d = torch.from_numpy(pre.mask).to(dev) if pre.mask is not None else None
+            if pre.I_norm is None:
+                # amplitudes and I_norm = sum(mask * I) in one pass over I
+                norm_d = torch.zeros(1, dtype=torch.float64, device=dev)
+                _native.check(lib.pty_amp_and_norm(self.plan, _ptr(I_d), int(Iin.dtype == np.float64),
+                                                   _ptr(mask_d), _ptr(amp), _ptr(norm_d), sp))
+                pre.I_norm = float(norm_d.cpu()[0]) * pre.norm_scale
+            else:
+                _native.check(lib.pty_amp_from_intensity(self.plan, _ptr(I_d),
+                                                         int(Iin.dtype == np.float64), _ptr(amp), sp))
             del I_d
             self.O_d = torch.from_numpy(np.ascontiguousarray(pre.O.astype(np.complex64))).to(dev)
             self.P_d = torch.from_numpy(np.ascontiguousarray(pre.P.astype(np.complex64))).to(dev)
             psi = torch.empty((n, N0, N1), dtype=torch.complex64, device=dev)
-            mask_d = torch.from_numpy(pre.mask).to(dev) if pre.mask is not None else None
             bg_d = torch.from_numpy(pre.background).to(dev) if pre.background is not None else None
+            if pre.background_pattern is not None:
+                bg_d = torch.from_numpy(pre.background_pattern).to(dev).expand(n, N0, N1).contiguous()
+            if pre.random_background:                               # era.py:539-540
+                bg_d = torch.empty((n, N0, N1), dtype=torch.float32, device=dev)
+                device_random_background(lib, bg_d, pre.rdt, sp)
             npm = pmod_probe_count(Pmod_probe, iters)
             Pamp_d = torch.from_numpy(pre.Pamp).to(dev) if npm > 0 else None
             self.bmean = (torch.zeros((N0, N1), dtype=torch.float32, device=dev)
@@ -175,14 +226,15 @@ class _Job:
     def outputs(self):
         """The reference's return value (era.py:300-332 / dm.py:300-333)."""
         pre, kind, iters = self.pre, self.kind, self.iters
-        O_out = self.O_d.cpu().numpy().astype(pre.cdt)
-        P_out = self.P_d.cpu().numpy().astype(pre.cdt)
+        # astype(copy=False): no host copy when the dtype already matches
+        O_out = self.O_d.cpu().numpy().astype(pre.cdt, copy=False)
+        P_out = self.P_d.cpu().numpy().astype(pre.cdt, copy=False)
         upd = pre.update
         if not self.full_output:
             return O_out if upd == "O" else P_out if upd == "P" else (O_out, P_out)
         rt = pre.rdt
         info = {
-            "I": self.inten.cpu().numpy().astype(rt) if self.inten is not None else None,
+            "I": self.inten.cpu().numpy().astype(rt, copy=False) if self.inten is not None else None,
             "eMod": [rt(x) for x in self.emod.cpu().numpy()[:iters]],
             "eCon": [rt(x) for x in self.econ.cpu().numpy()[:iters]],
             "heatmap": (self.heat.cpu().numpy().astype(rt)

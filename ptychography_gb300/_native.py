@@ -54,9 +54,13 @@ SIGNATURES = {
     "pty_intensities": [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p],
     "pty_background_mean": [c_void_p, c_void_p, c_void_p, c_void_p],
     "pty_back_project": [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p],
+    "pty_amp_and_norm": [c_void_p, c_void_p, c_int32, c_void_p, c_void_p, c_void_p, c_void_p],
     "pty_amp_from_intensity": [c_void_p, c_void_p, c_int32, c_void_p, c_void_p],
     "pty_psup_P_noalloc": [ctypes.POINTER(Geometry), ctypes.POINTER(c_int64), c_void_p, c_void_p,
                            c_void_p, c_int32, c_double, c_void_p, c_void_p],
+    "pty_legacy_random_background": [ctypes.POINTER(ctypes.c_uint32), c_int32, ctypes.c_int64,
+                                     c_int32, c_void_p, ctypes.POINTER(ctypes.c_uint32),
+                                     ctypes.POINTER(c_int32), c_void_p],
     "pty_shape_supported": [c_int32, c_int32],
     "pty_frame_tile_candidates": [c_int32, c_int32, ctypes.POINTER(c_int32), c_int32,
                                   ctypes.POINTER(c_int32)],

@@ -879,6 +879,58 @@ static __global__ void amp_kernel(const void* I, int is_double, int n, int N0, i
   }
 }
 
+// amp as above, plus per-block partial sums of mask * I (era.py:495, I_norm)
+// in double; the mask is in unshifted order, like amp.
+static __global__ void amp_norm_kernel(const void* I, int is_double, int n, int N0, int N1,
+                                       const uint8_t* mask, float* amp, double* part) {
+  __shared__ double red[32];
+  const long long tot = (long long)n * N0 * N1;
+  double acc = 0.0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < tot;
+       i += (long long)gridDim.x * blockDim.x) {
+    const long long f = i / ((long long)N0 * N1);
+    const int k0 = (int)((i / N1) % N0), k1 = (int)(i % N1);
+    const long long src = f * N0 * N1 + (long long)((k0 + N0 / 2) % N0) * N1 + (k1 + N1 / 2) % N1;
+    const double m = mask ? (double)mask[(long long)k0 * N1 + k1] : 1.0;
+    if (is_double) {
+      const double v = ((const double*)I)[src];
+      amp[i] = (float)sqrt(v);
+      acc += m * v;
+    } else {
+      const float v = ((const float*)I)[src];
+      amp[i] = sqrtf(v);
+      acc += m * (double)v;
+    }
+  }
+  acc = block_sum_d(acc, red);
+  if (threadIdx.x == 0) part[blockIdx.x] = acc;
+}
+
+static __global__ void sum_parts_kernel(const double* part, int nparts, double* out) {
+  __shared__ double red[32];
+  double s = 0.0;
+  for (int i = threadIdx.x; i < nparts; i += blockDim.x) s += part[i];
+  s = block_sum_d(s, red);
+  if (threadIdx.x == 0) *out = s;
+}
+
+extern "C" int pty_amp_and_norm(pty_plan* p, const void* I, int32_t is_double, const uint8_t* mask,
+                                float* amp, double* norm, void* stream) {
+  if (!p || !I || !amp || !norm) return set_error(PTY_ERR_ARG, "null argument");
+  cudaStream_t st = (cudaStream_t)stream;
+  constexpr int kBlocks = 152 * 8;
+  double* part = nullptr;
+  PTY_CUDA(cudaMallocAsync(&part, kBlocks * sizeof(double), st));
+  amp_norm_kernel<<<kBlocks, 256, 0, st>>>(I, is_double, p->n, p->N0, p->N1, mask, amp, part);
+  int rc = check_launch("amp_norm_kernel");
+  if (rc == PTY_OK) {
+    sum_parts_kernel<<<1, 256, 0, st>>>(part, kBlocks, norm);
+    rc = check_launch("sum_parts_kernel");
+  }
+  cudaFreeAsync(part, st);
+  return rc;
+}
+
 extern "C" int pty_amp_from_intensity(pty_plan* p, const void* I, int32_t is_double, float* amp,
                                       void* stream) {
   if (!p || !I || !amp) return set_error(PTY_ERR_ARG, "null argument");
