@@ -134,8 +134,7 @@ __global__ void __launch_bounds__(ClusterCfg<N, C>::NT, ClusterCfg<N, C>::MINB)
   // cluster barrier completes
   ModIn<OP, B> m;
   cluster_arrive_release();
-  if constexpr (ModIn<OP, B>::EARLY)
-    modulus_load<N, N, OP, A, B>(g, f, fbase, tid / CW, rank * CPC + tid % CW, m);
+  modulus_load<N, N, OP, A, B>(g, f, fbase, tid / CW, rank * CPC + tid % CW, m);
   cluster_wait_acquire();
 
   // ---------------- 3. column pass on the owned columns
@@ -152,7 +151,7 @@ __global__ void __launch_bounds__(ClusterCfg<N, C>::NT, ClusterCfg<N, C>::MINB)
     const int cl = s * CW + cw;
     const int kc = rank * CPC + cl;
     // this sub-pass's amp / mask / background, in flight during the forward FFT
-    if (ModIn<OP, B>::EARLY && s > 0) modulus_load<N, N, OP, A, B>(g, f, fbase, tc, kc, m);
+    if (s > 0) modulus_load<N, N, OP, A, B>(g, f, fbase, tc, kc, m);
     float2 v[B];
 #pragma unroll
     for (int j = 0; j < B; ++j) v[j] = cbuf[cidx(tc + A * j, cl)];
@@ -162,7 +161,7 @@ __global__ void __launch_bounds__(ClusterCfg<N, C>::NT, ClusterCfg<N, C>::MINB)
     for (int k1 = 0; k1 < B; ++k1) xb[(k1 * A + tc) * CW + cw] = v[k1];
     __syncthreads();
     line_stage2<N, OpTraits<OP>::FIRST_DIR>(v, tc, [&](int tt, int k1) { return xb[(k1 * A + tt) * CW + cw]; });
-    if constexpr (!ModIn<OP, B>::EARLY) modulus_load<N, N, OP, A, B>(g, f, fbase, tc, kc, m);
+    modulus_load_late<N, N, OP, A, B>(g, fbase, tc, kc, m);
     modulus_apply<N, N, OP, A, B>(g, fbase, tc, kc, v, m, err);
     if constexpr (INVERSE) {
       line_stage1<N, +1>(v, tc, tw);

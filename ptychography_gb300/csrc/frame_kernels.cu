@@ -118,7 +118,7 @@ __global__ void __launch_bounds__(FrameCfg<N0, N1>::NT, 1) frame_kernel(FrameArg
   constexpr int CW = C::CW;
   // the modulus inputs of the first column pass are loaded across the barrier
   ModIn<OP, B0> m;
-  if constexpr (ModIn<OP, B0>::EARLY) modulus_load<N0, N1, OP, A0, B0>(g, f, fbase, tid / CW, tid % CW, m);
+  modulus_load<N0, N1, OP, A0, B0>(g, f, fbase, tid / CW, tid % CW, m);
   __syncthreads();
 
   // ---------------- column pass: forward FFT, modulus constraint, inverse FFT
@@ -136,7 +136,7 @@ __global__ void __launch_bounds__(FrameCfg<N0, N1>::NT, 1) frame_kernel(FrameArg
     const int cp = padpos(c, A1);
     auto at = [&](int r) -> float2& { return fr[rbase(r) + cp]; };
     // this pass's amp / mask / background, in flight during the forward FFT
-    if (ModIn<OP, B0>::EARLY && c0 > 0) modulus_load<N0, N1, OP, A0, B0>(g, f, fbase, t, c, m);
+    if (c0 > 0) modulus_load<N0, N1, OP, A0, B0>(g, f, fbase, t, c, m);
     float2 v[B0];
 #pragma unroll
     for (int j = 0; j < B0; ++j) v[j] = at(t + A0 * j);
@@ -146,7 +146,7 @@ __global__ void __launch_bounds__(FrameCfg<N0, N1>::NT, 1) frame_kernel(FrameArg
     for (int k1 = 0; k1 < B0; ++k1) xb[(k1 * A0 + t) * CW + cw] = v[k1];
     __syncthreads();
     line_stage2<N0, OpTraits<OP>::FIRST_DIR>(v, t, [&](int tt, int k1) { return xb[(k1 * A0 + tt) * CW + cw]; });
-    if constexpr (!ModIn<OP, B0>::EARLY) modulus_load<N0, N1, OP, A0, B0>(g, f, fbase, t, c, m);
+    modulus_load_late<N0, N1, OP, A0, B0>(g, fbase, t, c, m);
     modulus_apply<N0, N1, OP, A0, B0>(g, fbase, t, c, v, m, err);
     if constexpr (INVERSE) {
       line_stage1<N0, +1>(v, t, tw0);

@@ -50,10 +50,11 @@ PTY_DEV float2 frame_input(const FrameArgs& g, int f, int r0, int r1, const floa
 }
 
 // The modulus constraint on one column line: v[j] = F[t + A j][kc], in two
-// halves so a kernel can issue the line's global loads early and overlap
+// parts so a kernel can issue the line's global loads early and overlap
 // their latency with the forward transform:
-//   modulus_load  -- amp, mask and background of the line into registers
-//   modulus_apply -- the constraint on v, the error sum, the background store
+//   modulus_load      -- amp, mask and background of the line into registers
+//   modulus_load_late -- DM7's background state and mean, just before use
+//   modulus_apply     -- the constraint on v, the error sum, the background store
 // All loads of a line precede its stores (the output pointers may alias the
 // inputs, which would otherwise serialise every load behind the previous
 // element's store).
@@ -62,9 +63,6 @@ struct ModIn {
   static constexpr bool BG_IN = (OP == OP_EXIT7 || OP == OP_PSI7 || OP == OP_MERR || OP == OP_MERR_PSI);
   static constexpr bool BG_OUT = (OP == OP_EXIT7 || OP == OP_PSI7 || OP == OP_DM7);
   static constexpr bool NEEDS = !(OP == OP_INTENS || OP == OP_BP);
-  // issued ahead of the forward transform, except for DM7 whose four input
-  // arrays would not fit the register budget alongside the transform
-  static constexpr bool EARLY = (OP != OP_DM7);
   float am[B], mk[B], bb[B], b0v[B];
 };
 
@@ -78,10 +76,21 @@ PTY_DEV void modulus_load(const FrameArgs& g, int f, size_t fbase, int t, int kc
       m.am[j] = __ldg(&amp[pix]);
       m.mk[j] = g.mask ? (float)__ldg(&g.mask[pix]) : 1.0f;
       if constexpr (ModIn<OP, B>::BG_IN) m.bb[j] = g.bg_in ? g.bg_in[(size_t)g.bg_stride * f + pix] : 0.0f;
-      if constexpr (OP == OP_DM7) {
-        m.bb[j] = g.bg_out[fbase + pix];
-        m.b0v[j] = __ldg(&g.b0[pix]);
-      }
+    }
+  }
+}
+
+// The DM7 background state and mean, loaded just before the constraint: with
+// amp and mask already in flight, two more arrays across the forward
+// transform would not fit the register budget.
+template <int N0, int N1, int OP, int A, int B>
+PTY_DEV void modulus_load_late(const FrameArgs& g, size_t fbase, int t, int kc, ModIn<OP, B>& m) {
+  if constexpr (OP == OP_DM7) {
+#pragma unroll
+    for (int j = 0; j < B; ++j) {
+      const int pix = (t + A * j) * N1 + kc;
+      m.bb[j] = g.bg_out[fbase + pix];
+      m.b0v[j] = __ldg(&g.b0[pix]);
     }
   }
 }
@@ -155,6 +164,7 @@ PTY_DEV void frame_modulus_line(const FrameArgs& g, int f, size_t fbase, int t, 
                                 float2 (&v)[B], ff& err) {
   ModIn<OP, B> m;
   modulus_load<N0, N1, OP, A, B>(g, f, fbase, t, kc, m);
+  modulus_load_late<N0, N1, OP, A, B>(g, fbase, t, kc, m);
   modulus_apply<N0, N1, OP, A, B>(g, fbase, t, kc, v, m, err);
 }
 
