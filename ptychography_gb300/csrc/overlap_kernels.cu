@@ -12,7 +12,14 @@ namespace pty {
 constexpr int kTile = 32;      // tile width (columns) of the object / probe gathers
 constexpr int kTileRows = 16;  // tile height (rows)
 constexpr int kGatherNT = 256; // threads per tile: 32 columns x 8 rows, 2 pixels each
-constexpr int kPrefetch = 4;   // frames whose loads are issued together
+constexpr int kPrefetch = 4;   // frames whose loads are issued together (object gather)
+constexpr int kPrefetchP = 4;  // the same for the probe gather
+
+// acc += conj(p) x as four FMAs
+PTY_DEV void cmac_conj(float2& acc, float2 x, float2 p) {
+  acc.x = fmaf(p.x, x.x, fmaf(p.y, x.y, acc.x));
+  acc.y = fmaf(p.x, x.y, fmaf(-p.y, x.x, acc.y));
+}
 
 // ------------------------------------------------------------------ psup_O
 // era.py:336-369: O = sum_i psi_i * conj(P) placed at window i, / (heat + alpha),
@@ -52,25 +59,34 @@ __global__ void __launch_bounds__(kGatherNT) psup_O_kernel(
       p[k] = ok ? P[a * N1 + b] : make_float2(0.f, 0.f);
     }
   };
-  auto accumulate = [&](const float2 (&x)[2], const float2 (&p)[2]) {
-#pragma unroll
-    for (int k = 0; k < 2; ++k) {
-      acc[k] = cadd(acc[k], cmulc(x[k], p[k]));
-      if (HEAT) h[k] = ff_add(h[k], cabs2(p[k]));
-    }
-  };
+  // The heat terms of a prefetch group are summed in FP32 (at most kPrefetch
+  // terms of one sign, relative error < 2e-7) and the group sum is added to
+  // the float-float total, so the total's error does not grow with the frame
+  // count; the numerators accumulate with fused multiply-adds.
   int e = beg;
   for (; e + kPrefetch <= end; e += kPrefetch) {
     float2 x[kPrefetch][2], p[kPrefetch][2];
 #pragma unroll
     for (int q = 0; q < kPrefetch; ++q) fetch(e + q, x[q], p[q]);
 #pragma unroll
-    for (int q = 0; q < kPrefetch; ++q) accumulate(x[q], p[q]);
+    for (int k = 0; k < 2; ++k) {
+      float hs = 0.f;
+#pragma unroll
+      for (int q = 0; q < kPrefetch; ++q) {
+        cmac_conj(acc[k], x[q][k], p[q][k]);
+        if (HEAT) hs += cabs2(p[q][k]);
+      }
+      if (HEAT) h[k] = ff_add(h[k], hs);
+    }
   }
   for (; e < end; ++e) {
     float2 x[2], p[2];
     fetch(e, x, p);
-    accumulate(x, p);
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+      cmac_conj(acc[k], x[k], p[k]);
+      if (HEAT) h[k] = ff_add(h[k], cabs2(p[k]));
+    }
   }
   if (v < V) {
 #pragma unroll
@@ -104,16 +120,30 @@ __global__ void __launch_bounds__(kGatherNT) heat_P_kernel(
 #pragma unroll
   for (int k = 0; k < 2; ++k) acc[k] = ff_zero();
   const int beg = tl.ptr[tile], end = tl.ptr[tile + 1];
-  for (int e = beg; e < end; ++e) {
+  // |P|^2 at window pixel of list entry e, or an exact zero outside the window
+  auto term = [&](int e, int k) -> float {
     const int f = tl.frames[e];
     const int r0 = R[2 * f], r1 = R[2 * f + 1];
-    const int b = v + r1;
-    if (b < 0 || b >= N1) continue;
+    const int b = v + r1, a = tu * kTileRows + ty + 8 * k + r0;
+    return (b >= 0 && b < N1 && a >= 0 && a < N0) ? cabs2(__ldg(&P[a * N1 + b])) : 0.f;
+  };
+  // the same grouping as psup_O_kernel<true>: FP32 sums of kPrefetch entries,
+  // each added to the float-float total, then the remaining entries one by one
+  // (adding an exact zero leaves a normalised pair unchanged), so both kernels
+  // produce the same bits
+  int e = beg;
+  for (; e + kPrefetch <= end; e += kPrefetch) {
 #pragma unroll
     for (int k = 0; k < 2; ++k) {
-      const int a = tu * kTileRows + ty + 8 * k + r0;
-      if (a >= 0 && a < N0) acc[k] = ff_add(acc[k], cabs2(__ldg(&P[a * N1 + b])));
+      float hs = 0.f;
+#pragma unroll
+      for (int q = 0; q < kPrefetch; ++q) hs += term(e + q, k);
+      acc[k] = ff_add(acc[k], hs);
     }
+  }
+  for (; e < end; ++e) {
+#pragma unroll
+    for (int k = 0; k < 2; ++k) acc[k] = ff_add(acc[k], term(e, k));
   }
   if (v < V) {
 #pragma unroll
@@ -180,25 +210,31 @@ __global__ void __launch_bounds__(kGatherNT) psup_P_partial_kernel(
         }
       }
     };
-    auto accumulate = [&](const float2 (&x)[2], const float2 (&o)[2]) {
+    // as in psup_O: FMA numerators, |O|^2 group sums added to a float-float total
+    int f = f0;
+    for (; f + kPrefetchP <= f1; f += kPrefetchP) {
+      float2 x[kPrefetchP][2], o[kPrefetchP][2];
+#pragma unroll
+      for (int j = 0; j < kPrefetchP; ++j) fetch(f + j, x[j], o[j]);
 #pragma unroll
       for (int q = 0; q < 2; ++q) {
-        num[q] = cadd(num[q], cmulc(x[q], o[q]));
-        if (want_den) den[q] = ff_add(den[q], cabs2(o[q]));
+        float ds = 0.f;
+#pragma unroll
+        for (int j = 0; j < kPrefetchP; ++j) {
+          cmac_conj(num[q], x[j][q], o[j][q]);
+          ds += cabs2(o[j][q]);
+        }
+        if (want_den) den[q] = ff_add(den[q], ds);
       }
-    };
-    int f = f0;
-    for (; f + kPrefetch <= f1; f += kPrefetch) {
-      float2 x[kPrefetch][2], o[kPrefetch][2];
-#pragma unroll
-      for (int q = 0; q < kPrefetch; ++q) fetch(f + q, x[q], o[q]);
-#pragma unroll
-      for (int q = 0; q < kPrefetch; ++q) accumulate(x[q], o[q]);
     }
     for (; f < f1; ++f) {
       float2 x[2], o[2];
       fetch(f, x, o);
-      accumulate(x, o);
+#pragma unroll
+      for (int q = 0; q < 2; ++q) {
+        cmac_conj(num[q], x[q], o[q]);
+        if (want_den) den[q] = ff_add(den[q], cabs2(o[q]));
+      }
     }
 #pragma unroll
     for (int q = 0; q < 2; ++q) {
