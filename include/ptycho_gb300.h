@@ -185,7 +185,7 @@ int pty_shape_supported(int32_t N0, int32_t N1);
  * chosen per op family: family 0 = the plain forms (Pmod_1, model error,
  * intensities, back projection), family 1 = the background forms (Pmod_7 and
  * the DM background recursion).  Shapes with more than one tile built
- * (128 x 128: 1 or 2; 256 x 256: 8, 4 or 16) get theirs from an autotuner run
+ * (128 x 128: 1 or 2; 256 x 256: 8 or 4) get theirs from an autotuner run
  * by the first plan created for the shape on a device (disabled by
  * PTY_AUTOTUNE=0 in the environment: first candidate).  A plan keeps the
  * tiles chosen when it was created.

@@ -51,8 +51,7 @@ struct ClusterCfg {
   static constexpr int A = LineGeom<N>::A, B = LineGeom<N>::B;  // rows and columns alike
   // 256 threads per CTA for 8- and 16-CTA clusters and frames up to 192^2
   // (two CTAs per SM where the shared memory allows), else 512
-  // 128 threads for 256^2 frames on 16 CTAs (four clusters' CTAs per SM)
-  static constexpr int NT = (N == 256 && C == 16) ? 128 : (C >= 8 || N <= 192) ? 256 : 512;
+  static constexpr int NT = (C >= 8 || N <= 192) ? 256 : 512;
   static constexpr int RPC = N / C;          // rows owned per CTA
   static constexpr int CPC = N / C;          // columns owned per CTA
   static constexpr int CP = CPC + 1;         // column-buffer pitch (float2), odd

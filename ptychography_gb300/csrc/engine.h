@@ -71,7 +71,6 @@ PTY_DECLARE_CLUSTER_TILE(128, 2)
 PTY_DECLARE_CLUSTER_TILE(192, 2)
 PTY_DECLARE_CLUSTER_TILE(256, 4)
 PTY_DECLARE_CLUSTER_TILE(256, 8)
-PTY_DECLARE_CLUSTER_TILE(256, 16)
 PTY_DECLARE_CLUSTER_TILE(512, 16)
 #undef PTY_DECLARE_CLUSTER_TILE
 

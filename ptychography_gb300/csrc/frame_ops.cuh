@@ -95,6 +95,9 @@ PTY_DEV void modulus_load_late(const FrameArgs& g, size_t fbase, int t, int kc, 
   }
 }
 
+template <int OP, int B>
+PTY_DEV void modulus_compute(const FrameArgs& g, float2 (&v)[B], ModIn<OP, B>& m, ff& err);
+
 template <int N0, int N1, int OP, int A, int B>
 PTY_DEV void modulus_apply(const FrameArgs& g, size_t fbase, int t, int kc, float2 (&v)[B],
                            ModIn<OP, B>& m, ff& err) {
@@ -113,6 +116,19 @@ PTY_DEV void modulus_apply(const FrameArgs& g, size_t fbase, int t, int kc, floa
     for (int j = 0; j < B; ++j) g.psi[fbase + (size_t)(t + A * j) * N1 + kc] = cscale(v[j], kInv);
     return;
   } else {
+    modulus_compute<OP, B>(g, v, m, err);
+    if constexpr (ModIn<OP, B>::BG_OUT) {
+#pragma unroll
+      for (int j = 0; j < B; ++j) g.bg_out[fbase + (size_t)(t + A * j) * N1 + kc] = m.bb[j];
+    }
+  }
+}
+
+// The constraint itself (EXIT / PSI / DM / MERR forms): updates v and, for the
+// background forms, m.bb; adds the line's error terms to err.
+template <int OP, int B>
+PTY_DEV void modulus_compute(const FrameArgs& g, float2 (&v)[B], ModIn<OP, B>& m, ff& err) {
+  {
     float line_err = 0.f;   // FP32 over one line (B terms), folded into err once
 #pragma unroll
     for (int j = 0; j < B; ++j) {
@@ -152,10 +168,6 @@ PTY_DEV void modulus_apply(const FrameArgs& g, size_t fbase, int t, int kc, floa
       }
     }
     err = ff_add(err, line_err);
-    if constexpr (ModIn<OP, B>::BG_OUT) {
-#pragma unroll
-      for (int j = 0; j < B; ++j) g.bg_out[fbase + (size_t)(t + A * j) * N1 + kc] = m.bb[j];
-    }
   }
 }
 

@@ -7,8 +7,8 @@
 // depends on the GPU's shared memory, register file and cluster scheduling:
 //
 //   128^2: 1 CTA of 512 threads (one per SM) or 2-CTA clusters of 256 (two per SM)
-//   256^2: 8-CTA clusters of 256 threads (two CTAs per SM), 4-CTA clusters of
-//          512 (one per SM) or 16-CTA clusters of 128 (four per SM)
+//   256^2: 8-CTA clusters of 256 threads (two CTAs per SM) or 4-CTA clusters
+//          of 512 (one per SM)
 //
 // Tiles are chosen per op family: the background (Pmod_7) forms move more
 // bytes and hold more registers than the plain ones, and the fastest tile
@@ -45,7 +45,7 @@ struct ShapeTiles {
 
 constexpr ShapeTiles kShapes[] = {
     {32, 32, 1, {1, 0, 0, 0}},   {64, 64, 1, {1, 0, 0, 0}},   {32, 64, 1, {1, 0, 0, 0}},
-    {128, 128, 2, {1, 2, 0, 0}}, {192, 192, 1, {2, 0, 0, 0}}, {256, 256, 3, {8, 4, 16, 0}},
+    {128, 128, 2, {1, 2, 0, 0}}, {192, 192, 1, {2, 0, 0, 0}}, {256, 256, 2, {8, 4, 0, 0}},
     {512, 512, 1, {16, 0, 0, 0}},
 };
 
@@ -67,7 +67,6 @@ int prepare_tile(int N0, int N1, int tile) {
   if (N0 == 192 && N1 == 192 && tile == 2) return prepare_cluster_192x2();
   if (N0 == 256 && N1 == 256 && tile == 4) return prepare_cluster_256x4();
   if (N0 == 256 && N1 == 256 && tile == 8) return prepare_cluster_256x8();
-  if (N0 == 256 && N1 == 256 && tile == 16) return prepare_cluster_256x16();
   if (N0 == 512 && N1 == 512 && tile == 16) return prepare_cluster_512x16();
   return set_error(PTY_ERR_UNSUPPORTED, "frame tile not built for this shape");
 }
@@ -224,7 +223,6 @@ int launch_frame_op(int op, int N0, int N1, int tile, const FrameArgs& a, int nf
     if (N0 == 192 && tile == 2) return launch_cluster_192x2(op, a, nframes, st);
     if (N0 == 256 && tile == 4) return launch_cluster_256x4(op, a, nframes, st);
     if (N0 == 256 && tile == 8) return launch_cluster_256x8(op, a, nframes, st);
-    if (N0 == 256 && tile == 16) return launch_cluster_256x16(op, a, nframes, st);
     if (N0 == 512 && tile == 16) return launch_cluster_512x16(op, a, nframes, st);
   }
   return set_error(PTY_ERR_UNSUPPORTED, "frame tile not built for this shape");
