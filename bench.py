@@ -663,6 +663,21 @@ def cpu_oracle_rate(method, shard_frames, cores, pool=None):
 
 
 # --------------------------------------------------------------------------- main
+def max_over_ranks(torch, t, world, dev):
+    """The slowest rank's time (every rank gets it); t itself for one rank."""
+    if world <= 1:
+        return t
+    tt = torch.tensor([t], dtype=torch.float64, device=dev)
+    torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+    return float(tt.item())
+
+
+def job_rate(frames_per_step, steps, world, t):
+    """Whole-job frame-iterations per second: every rank runs its own replica
+    of the workload (weak scaling), so the job does world x the frames."""
+    return frames_per_step * steps * world / t
+
+
 def dist_env():
     return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), \
         int(os.environ.get("LOCAL_RANK", 0))
@@ -779,13 +794,8 @@ def main():
         torch.cuda.synchronize()
     barrier()
     launches = lib.pty_launch_count() - launches0
-    t = s.elapsed_time(e) / 1e3
-    if world > 1:
-        tt = torch.tensor([t], device=dev)
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        t = float(tt.item())
-    frames = job.frames_per_step() * args.steps * world
-    value = frames / t
+    t = max_over_ranks(torch, s.elapsed_time(e) / 1e3, world, dev)
+    value = job_rate(job.frames_per_step(), args.steps, world, t)
 
     tiles = []
     for fam in (0, 1):                       # plain / background op families
