@@ -170,12 +170,15 @@ int pty_psup_P_noalloc(const pty_geometry* geom, const int64_t* R_host, const vo
  * NumPy's legacy global generator.  key[624] / pos: the MT19937 state as
  * np.random.get_state() returns it (host memory); count doubles are drawn
  * (n * N0 * N1), out[i] = float32(dtype(u_i) + 0.1) with dtype float64 when
- * rdt_double, else float32 (device memory); key_out[624] / *pos_out: the state
- * after the draw, to be handed back with np.random.set_state.  Synchronises
- * the stream. */
+ * rdt_double, else float32 (device memory); scratch: device memory of
+ * pty_legacy_random_scratch_words(pos, count) uint32 words, or NULL to have
+ * the call allocate it; key_out[624] / *pos_out: the state after the draw, to
+ * be handed back with np.random.set_state.  Synchronises the stream. */
 int pty_legacy_random_background(const uint32_t* key, int32_t pos, int64_t count,
-                                 int32_t rdt_double, float* out, uint32_t* key_out,
-                                 int32_t* pos_out, void* stream);
+                                 int32_t rdt_double, float* out, uint32_t* scratch,
+                                 uint32_t* key_out, int32_t* pos_out, void* stream);
+/* Scratch words pty_legacy_random_background needs (-1 for invalid input). */
+int64_t pty_legacy_random_scratch_words(int32_t pos, int64_t count);
 
 /* 1 if the frame shape N0 x N1 has a fused FFT kernel. */
 int pty_shape_supported(int32_t N0, int32_t N1);

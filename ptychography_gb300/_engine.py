@@ -150,9 +150,12 @@ def device_random_background(lib, out, rdt, sp):
     key_out = np.empty(624, dtype=np.uint32)
     pos_out = ctypes.c_int32(0)
     u32p = ctypes.POINTER(ctypes.c_uint32)
+    # scratch (2 words per double) from the library's stream-ordered pool: a
+    # block this large from torch's caching allocator would displace the
+    # blocks the run's own large buffers reuse
     _native.check(lib.pty_legacy_random_background(
         key.ctypes.data_as(u32p), int(st[2]), int(out.numel()), int(rdt == np.float64),
-        _ptr(out), key_out.ctypes.data_as(u32p), ctypes.byref(pos_out), sp))
+        _ptr(out), None, key_out.ctypes.data_as(u32p), ctypes.byref(pos_out), sp))
     np.random.set_state((st[0], key_out, int(pos_out.value), st[3], st[4]))
 
 

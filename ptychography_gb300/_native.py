@@ -59,8 +59,9 @@ SIGNATURES = {
     "pty_psup_P_noalloc": [ctypes.POINTER(Geometry), ctypes.POINTER(c_int64), c_void_p, c_void_p,
                            c_void_p, c_int32, c_double, c_void_p, c_void_p],
     "pty_legacy_random_background": [ctypes.POINTER(ctypes.c_uint32), c_int32, ctypes.c_int64,
-                                     c_int32, c_void_p, ctypes.POINTER(ctypes.c_uint32),
+                                     c_int32, c_void_p, c_void_p, ctypes.POINTER(ctypes.c_uint32),
                                      ctypes.POINTER(c_int32), c_void_p],
+    "pty_legacy_random_scratch_words": [c_int32, ctypes.c_int64],
     "pty_shape_supported": [c_int32, c_int32],
     "pty_frame_tile_candidates": [c_int32, c_int32, ctypes.POINTER(c_int32), c_int32,
                                   ctypes.POINTER(c_int32)],
@@ -70,7 +71,8 @@ SIGNATURES = {
     "pty_version": [],
     "pty_launch_count": [],
 }
-_RESTYPES = {"pty_last_error": ctypes.c_char_p, "pty_launch_count": ctypes.c_int64}
+_RESTYPES = {"pty_last_error": ctypes.c_char_p, "pty_launch_count": ctypes.c_int64,
+             "pty_legacy_random_scratch_words": ctypes.c_int64}
 
 
 class PtyError(RuntimeError):

@@ -16,10 +16,10 @@
 //   x[m] = x[m - 227] ^ ((y >> 1) ^ (y & 1 ? 0x9908b0df : 0)),
 //   y    = (x[m - 624] & 0x80000000) | (x[m - 623] & 0x7fffffff),   m >= 624,
 // and the k-th output is temper(x[pos + k]).  Each word depends on words at
-// least 227 back, so one CTA computes 227 words per step from a ring of the
-// last 1024 and writes them out (the only serial part, ~0.6 M steps at
-// 1024 x 256^2); a second, fully parallel kernel tempers them and forms the
-// doubles: a double takes two consecutive outputs a, b,
+// least 227 back, so one CTA computes 227 words per step and writes them out
+// (the only serial part, ~0.6 M steps at 1024 x 256^2); a second, fully
+// parallel kernel tempers them and forms the doubles: a double takes two
+// consecutive outputs a, b,
 // ((a >> 5) 2^26 + (b >> 6)) 2^-53 (53 random bits, NumPy's legacy conversion).
 #include <cuda_runtime.h>
 
@@ -34,7 +34,6 @@ namespace {
 
 constexpr int kMtN = 624;
 constexpr int kMtLag = 227;          // 624 - 397
-constexpr int kRing = 1024;          // > 624 + 227 + 1 words kept
 constexpr int kThreads = 256;
 
 struct MtState {
@@ -56,30 +55,38 @@ __device__ __forceinline__ uint32_t mt_next_word(uint32_t lag, uint32_t lo, uint
 
 // Words x[0, total) of the sequence into x (x[0..623] = the state array); the
 // last 624 computed words, the state after the draw, into key_out.  One CTA:
-// each step computes 227 independent words from a shared ring of the last
-// 1024 (word m sits in slot m % 1024), one barrier per step.
+// step s computes words m = 624 + 227 s + t (thread t < 227).  Word m needs
+// x[m - 227] -- the same thread's word of step s - 1, kept in a register --
+// and x[m - 624], x[m - 623], words of steps s - 2 and s - 3 read from a
+// shared ring of the last 2048 words.  So one barrier after every second
+// step makes every read word visible, and a slot is overwritten only ~9 steps
+// after it was written, long after its last reader passed a barrier.
 __global__ void __launch_bounds__(kThreads, 1)
     legacy_words_kernel(MtState st, long long total, uint32_t* x, uint32_t* key_out) {
-  __shared__ uint32_t ring[kRing];
+  constexpr int kRingW = 2048;
+  __shared__ uint32_t ring[kRingW];
   const int tid = threadIdx.x;
   for (int i = tid; i < kMtN; i += kThreads) {
     ring[i] = st.key[i];
     x[i] = st.key[i];
   }
   __syncthreads();
-  for (long long m0 = kMtN; m0 < total; m0 += kMtLag) {
+  uint32_t prev = tid < kMtLag ? ring[kMtN - kMtLag + tid] : 0u;   // x[m - 227] of step 0
+  int step = 0;
+  for (long long m0 = kMtN; m0 < total; m0 += kMtLag, ++step) {
     if (tid < kMtLag && m0 + tid < total) {
-      const int s = (int)((m0 + tid) & (kRing - 1));
-      const uint32_t v = mt_next_word(ring[(s - kMtLag) & (kRing - 1)],
-                                      ring[(s - kMtN) & (kRing - 1)],
-                                      ring[(s - kMtN + 1) & (kRing - 1)]);
+      const int s = (int)((m0 + tid) & (kRingW - 1));
+      const uint32_t v = mt_next_word(prev, ring[(s - kMtN) & (kRingW - 1)],
+                                      ring[(s - kMtN + 1) & (kRingW - 1)]);
       ring[s] = v;
       x[m0 + tid] = v;
+      prev = v;
     }
-    __syncthreads();
+    if (step & 1) __syncthreads();
   }
+  __syncthreads();
   for (int i = tid; i < kMtN; i += kThreads)
-    key_out[i] = ring[(int)((total - kMtN + i) & (kRing - 1))];
+    key_out[i] = ring[(int)((total - kMtN + i) & (kRingW - 1))];
 }
 
 // out[i] = float32(dtype(u_i) + 0.1), u_i the double from outputs pos + 2 i and
@@ -109,9 +116,15 @@ __global__ void legacy_uniform_kernel(const uint32_t* __restrict__ x, int pos, l
 
 using namespace pty;
 
+extern "C" int64_t pty_legacy_random_scratch_words(int32_t pos, int64_t count) {
+  if (pos < 0 || pos > kMtN || count < 1) return -1;
+  const long long end = (long long)pos + 2 * (long long)count;
+  return ((end - 1) / kMtN + 1) * kMtN + kMtN;
+}
+
 extern "C" int pty_legacy_random_background(const uint32_t* key, int32_t pos, int64_t count,
-                                            int32_t rdt_double, float* out, uint32_t* key_out,
-                                            int32_t* pos_out, void* stream) {
+                                            int32_t rdt_double, float* out, uint32_t* scratch,
+                                            uint32_t* key_out, int32_t* pos_out, void* stream) {
   if (!key || !out || !key_out || !pos_out) return set_error(PTY_ERR_ARG, "null argument");
   if (pos < 0 || pos > kMtN) return set_error(PTY_ERR_ARG, "generator position outside 0..624");
   if (count < 1) return set_error(PTY_ERR_ARG, "count must be positive");
@@ -120,12 +133,15 @@ extern "C" int pty_legacy_random_background(const uint32_t* key, int32_t pos, in
   std::memcpy(s.key, key, sizeof(s.key));
   const long long end = (long long)pos + 2 * (long long)count;   // one past the last word drawn
   const long long total = ((end - 1) / kMtN + 1) * kMtN;          // through the block holding it
-  // raw words plus the final state, stream-ordered scratch
-  uint32_t* d_x = nullptr;
-  cudaError_t e = cudaMallocAsync(&d_x, (size_t)(total + kMtN) * sizeof(uint32_t), st);
-  if (e != cudaSuccess) {
-    cudaGetLastError();
-    return set_error(PTY_ERR_NOMEM, "generator scratch allocation failed");
+  // raw words plus the final state: the caller's scratch, else stream-ordered
+  uint32_t* d_x = scratch;
+  cudaError_t e = cudaSuccess;
+  if (!d_x) {
+    e = cudaMallocAsync(&d_x, (size_t)(total + kMtN) * sizeof(uint32_t), st);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      return set_error(PTY_ERR_NOMEM, "generator scratch allocation failed");
+    }
   }
   uint32_t* d_key = d_x + total;
   legacy_words_kernel<<<1, kThreads, 0, st>>>(s, total, d_x, d_key);
@@ -138,7 +154,7 @@ extern "C" int pty_legacy_random_background(const uint32_t* key, int32_t pos, in
     e = cudaMemcpyAsync(key_out, d_key, kMtN * sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
     if (e != cudaSuccess) rc = set_cuda_error(e, "generator state copy");
   }
-  cudaFreeAsync(d_x, st);
+  if (!scratch) cudaFreeAsync(d_x, st);
   if (rc == PTY_OK) {
     e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) rc = set_cuda_error(e, "generator state copy");

@@ -42,3 +42,30 @@ def test_next_draw_continues_stream():
     out = torch.empty((2, 48, 48), dtype=torch.float32, device=dev())
     _engine.device_random_background(lib, out, np.float32, stream())
     np.testing.assert_array_equal(np.random.random(10), want)
+
+
+def test_caller_scratch_matches_internal():
+    lib = _native.load()
+    shape = (3, 64, 64)
+    np.random.seed(44)
+    st0 = np.random.get_state()
+    a = torch.empty(shape, dtype=torch.float32, device=dev())
+    _engine.device_random_background(lib, a, np.float32, stream())
+    after = np.random.get_state()
+    np.random.set_state(st0)
+    import ctypes
+    key = np.ascontiguousarray(st0[1], dtype=np.uint32)
+    words = lib.pty_legacy_random_scratch_words(int(st0[2]), a.numel())
+    scratch = torch.empty(int(words), dtype=torch.int32, device=dev())
+    b = torch.empty_like(a)
+    key_out = np.empty(624, dtype=np.uint32)
+    pos = ctypes.c_int32(0)
+    u32p = ctypes.POINTER(ctypes.c_uint32)
+    _native.check(lib.pty_legacy_random_background(
+        key.ctypes.data_as(u32p), int(st0[2]), a.numel(), 0, ctypes.c_void_p(b.data_ptr()),
+        ctypes.c_void_p(scratch.data_ptr()), key_out.ctypes.data_as(u32p), ctypes.byref(pos),
+        stream()))
+    np.testing.assert_array_equal(a.cpu().numpy(), b.cpu().numpy())
+    np.testing.assert_array_equal(key_out, after[1])
+    assert pos.value == after[2]
+    assert lib.pty_legacy_random_scratch_words(625, 1) == -1
