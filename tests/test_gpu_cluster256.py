@@ -1,4 +1,4 @@
-"""256x256 frames: the 4-CTA cluster kernel against the oracle.
+"""256x256 frames: the cluster frame kernels (the autotuned tile) against the oracle.
 
 Operators are compared on random data (FP32 rounding of a 256^2 FFT round
 trip: 3e-6 relative); ERA / DM one-step errors on a small 256^2 problem with
@@ -122,3 +122,20 @@ def test_dm_m6_one_step_256(c1s):
     O_g, P_g, ig = pty.DM(I, R.copy(), P_k, O_k, 1, mask=M, method=6, background=b, dtype="double")
     assert rel(O_g, O_o) < 1e-5 and rel(P_g, P_o) < 1e-5
     assert ig["eMod"][0] == pytest.approx(io["eMod"][0], rel=1e-5)
+
+
+@pytest.mark.parametrize("kind,method", [("era", 1), ("era", 3), ("dm", 1), ("dm", 3)])
+def test_plain_methods_one_step_256(c1s, kind, method):
+    """The EXIT1 / DM1 frame ops and the object / probe gathers at 256^2: one
+    iteration from the oracle's FP64 state within 1e-5 relative."""
+    I, R, P, O, M = c1s
+    np.random.seed(9)
+    O_k, P_k, _ = orc.ERA(I, R.copy(), P * np.exp(0.1j), None, 2, mask=M, method=3, dtype="double")
+    fo, fg = (orc.ERA, pty.ERA) if kind == "era" else (orc.DM, pty.DM)
+    P_in = P_k if method == 3 else P
+    res_o = fo(I, R.copy(), P_in, O_k, 1, mask=M, method=method, dtype="double")
+    res_g = fg(I, R.copy(), P_in, O_k, 1, mask=M, method=method, dtype="double")
+    assert rel(res_g[0], res_o[0]) < 1e-5
+    if method == 3:
+        assert rel(res_g[1], res_o[1]) < 1e-5
+    assert res_g[-1]["eMod"][0] == pytest.approx(res_o[-1]["eMod"][0], rel=1e-5)
