@@ -126,3 +126,32 @@ def test_engine_fails_loudly_without_gpu():
     with pytest.raises(RuntimeError, match="CUDA GPU"):
         _engine.run("era", I, R, np.ones((32, 32)), None, 1, 1, 1, None, 1, False, False, 1e-10,
                     None, True)
+
+
+def test_preamble_rejects_malformed_inputs():
+    """Inputs the reference would fail on with broadcast / unbound-name errors
+    raise ValueError here (before any device work)."""
+    I = np.ones((3, 32, 32))
+    R = np.zeros((3, 2), dtype=np.int64)
+    P = np.ones((32, 32))
+    args = dict(OP_iters=1, mask=1, background=None, method=1, dtype=None)
+
+    def pre(**kw):
+        a = dict(I=I, R=R.copy(), P=P, O=None, **args)
+        a.update(kw)
+        return _engine.Preamble(a["I"], a["R"], a["P"], a["O"], a["OP_iters"], a["mask"],
+                                a["background"], a["method"], a["dtype"])
+
+    pre()                                                # well formed
+    with pytest.raises(ValueError):
+        pre(I=np.ones((32, 32)))                         # not a frame stack
+    with pytest.raises(ValueError):
+        pre(R=np.zeros((2, 2), dtype=np.int64))          # one offset per frame
+    with pytest.raises(ValueError):
+        pre(P=np.ones((16, 32)))                         # probe of another shape
+    with pytest.raises(ValueError):
+        pre(mask=np.ones((16, 16)))                      # mask of another shape
+    with pytest.raises(ValueError):
+        pre(dtype="half")
+    with pytest.raises(ValueError):
+        pre(method=0)
