@@ -188,7 +188,7 @@ extern "C" int pty_plan_create(const pty_geometry* g, const int64_t* R_host, pty
   if ((rc = dalloc_t(p, &p->d_heatO2, npix))) return fail(rc);
   {
     // enough frame chunks for about four waves of probe-gather blocks
-    const int ntiles = ((N0 + 15) / 16) * ((N1 + 31) / 32);
+    const int ntiles = psup_P_tiles(N0, N1);
     int K = (2432 + ntiles - 1) / ntiles;
     if (K > 64) K = 64;
     if (K > n) K = n;

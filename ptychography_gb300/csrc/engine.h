@@ -108,6 +108,8 @@ int launch_psup_O(const TileLists& tl, int n, int N0, int N1, int U, int V, cons
 int launch_heat_P(const TileLists& tl, int n, int N0, int N1, int U, int V, const int* R,
                   const float2* P, double* heat, cudaStream_t st);
 // P = sum conj(O_i) psi_i / (sum |O_i|^2 + alpha) (era.py:371-400, 412-417)
+// blocks per frame chunk of the probe gather (sets the plan's chunk count)
+int psup_P_tiles(int N0, int N1);
 int launch_psup_P(int n, int N0, int N1, int U, int V, const int* R, const float2* psi,
                   const float2* O, float2* part_num, float2* part_den, int K, double* heatO,
                   bool recompute_heat, float alpha, float2* P, cudaStream_t st);

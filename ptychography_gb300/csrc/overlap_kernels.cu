@@ -275,12 +275,98 @@ __global__ void psup_P_reduce_kernel(int npix, int K, const float2* __restrict__
   P[i] = make_float2(nr.hi / den, ni.hi / den);
 }
 
+// The same partial sums for frames whose rows are a multiple of 256 wide: a
+// block takes whole frame rows -- 1024 / N1 rows x N1 columns, 4 pixels per
+// thread (CPT columns of 1024 / (256 CPT) rows) -- so each psi load of a warp
+// reads a contiguous row segment and a block's reads of one frame are
+// consecutive rows (better DRAM page locality than 16 x 32 tiles).
+template <int CPT>
+__global__ void __launch_bounds__(kGatherNT) psup_P_rows_kernel(
+    int n, int N0, int N1, int U, int V, const int* __restrict__ R, const float2* __restrict__ psi,
+    const float2* __restrict__ O, int K, bool want_den, float2* __restrict__ part_num,
+    float2* __restrict__ part_den) {
+  constexpr int TR = 4 / CPT;               // rows per block
+  constexpr int PF = 2;                     // frames whose loads are issued together
+  const int k = blockIdx.y;
+  const int a0 = blockIdx.x * TR;
+  const int f0 = (int)(((long long)n * k) / K), f1 = (int)(((long long)n * (k + 1)) / K);
+  int pa[4], pc[4];
+#pragma unroll
+  for (int p = 0; p < 4; ++p) {
+    pa[p] = a0 + p / CPT;
+    pc[p] = threadIdx.x + kGatherNT * (p % CPT);
+  }
+  float2 num[4];
+  ff den[4];
+#pragma unroll
+  for (int p = 0; p < 4; ++p) {
+    num[p] = make_float2(0.f, 0.f);
+    den[p] = ff_zero();
+  }
+  auto fetch = [&](int f, float2 (&x)[4], float2 (&o)[4]) {
+    const int r0 = R[2 * f], r1 = R[2 * f + 1];
+    const float2* pf = psi + (size_t)f * N0 * N1;
+#pragma unroll
+    for (int p = 0; p < 4; ++p) {
+      x[p] = pf[pa[p] * N1 + pc[p]];
+      o[p] = __ldg(&O[(size_t)(pa[p] - r0) * V + (pc[p] - r1)]);
+    }
+  };
+  int f = f0;
+  for (; f + PF <= f1; f += PF) {
+    float2 x[PF][4], o[PF][4];
+#pragma unroll
+    for (int j = 0; j < PF; ++j) fetch(f + j, x[j], o[j]);
+#pragma unroll
+    for (int p = 0; p < 4; ++p) {
+      float ds = 0.f;
+#pragma unroll
+      for (int j = 0; j < PF; ++j) {
+        cmac_conj(num[p], x[j][p], o[j][p]);
+        ds += cabs2(o[j][p]);
+      }
+      if (want_den) den[p] = ff_add(den[p], ds);
+    }
+  }
+  for (; f < f1; ++f) {
+    float2 x[4], o[4];
+    fetch(f, x, o);
+#pragma unroll
+    for (int p = 0; p < 4; ++p) {
+      cmac_conj(num[p], x[p], o[p]);
+      if (want_den) den[p] = ff_add(den[p], cabs2(o[p]));
+    }
+  }
+#pragma unroll
+  for (int p = 0; p < 4; ++p) {
+    const size_t idx = (size_t)k * N0 * N1 + (size_t)pa[p] * N1 + pc[p];
+    part_num[idx] = num[p];
+    if (want_den) part_den[idx] = make_float2(den[p].hi, den[p].lo);
+  }
+}
+
+bool psup_P_by_rows(int N0, int N1) {
+  return (N1 == 256 && N0 % 4 == 0) || (N1 == 512 && N0 % 2 == 0);
+}
+
+int psup_P_tiles(int N0, int N1) {
+  if (psup_P_by_rows(N0, N1)) return N0 / (1024 / N1);
+  return ((N0 + kTileRows - 1) / kTileRows) * ((N1 + kTile - 1) / kTile);
+}
+
 int launch_psup_P(int n, int N0, int N1, int U, int V, const int* R, const float2* psi,
                   const float2* O, float2* part_num, float2* part_den, int K, double* heatO,
                   bool recompute_heat, float alpha, float2* P, cudaStream_t st) {
-  const int ntiles = ((N0 + kTileRows - 1) / kTileRows) * ((N1 + kTile - 1) / kTile);
-  psup_P_partial_kernel<<<dim3(ntiles, K), kGatherNT, 0, st>>>(n, N0, N1, U, V, R, psi, O, K,
-                                                               recompute_heat, part_num, part_den);
+  const int ntiles = psup_P_tiles(N0, N1);
+  if (N1 == 256 && psup_P_by_rows(N0, N1))
+    psup_P_rows_kernel<1><<<dim3(ntiles, K), kGatherNT, 0, st>>>(n, N0, N1, U, V, R, psi, O, K,
+                                                                 recompute_heat, part_num, part_den);
+  else if (N1 == 512 && psup_P_by_rows(N0, N1))
+    psup_P_rows_kernel<2><<<dim3(ntiles, K), kGatherNT, 0, st>>>(n, N0, N1, U, V, R, psi, O, K,
+                                                                 recompute_heat, part_num, part_den);
+  else
+    psup_P_partial_kernel<<<dim3(ntiles, K), kGatherNT, 0, st>>>(n, N0, N1, U, V, R, psi, O, K,
+                                                                 recompute_heat, part_num, part_den);
   int rc = check_launch("psup_P_partial_kernel");
   if (rc) return rc;
   const int npix = N0 * N1;
