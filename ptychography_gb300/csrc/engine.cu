@@ -159,8 +159,8 @@ extern "C" int pty_plan_create(const pty_geometry* g, const int64_t* R_host, pty
   int rc = PTY_OK;
   auto fail = [&](int code) { pty_plan_destroy(p); return code; };
 
-  // per-tile ascending frame lists for the object gathers (16-row x 32-column tiles)
-  const int T = 32, TR = 16;
+  // per-tile ascending frame lists for the object gathers
+  const int T = kGatherTileCols, TR = kGatherTileRows;
   const int ntu = (U + TR - 1) / TR, ntv = (V + T - 1) / T;
   std::vector<int> ptr((size_t)ntu * ntv + 1, 0), frames;
   {

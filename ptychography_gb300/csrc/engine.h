@@ -93,6 +93,12 @@ void count_launches(long long k);
 long long launch_total();
 
 // ------------------------------------------------------------ overlap kernels
+// object / probe gather tiles: kGatherTileRows x kGatherTileCols pixels, one
+// block of 256 threads (two pixels each) per tile.  (8 x 64 tiles, with wider
+// contiguous row segments, measured slower: more frames overlap a tile only
+// partially.)
+constexpr int kGatherTileRows = 16;
+constexpr int kGatherTileCols = 32;
 struct TileLists {
   int TU, TV, ntu, ntv;      // object tiles
   const int* ptr;            // [ntu*ntv + 1]

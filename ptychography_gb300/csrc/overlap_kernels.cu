@@ -9,9 +9,11 @@
 
 namespace pty {
 
-constexpr int kTile = 32;      // tile width (columns) of the object / probe gathers
-constexpr int kTileRows = 16;  // tile height (rows)
-constexpr int kGatherNT = 256; // threads per tile: 32 columns x 8 rows, 2 pixels each
+constexpr int kTile = kGatherTileCols;      // tile width (columns) of the object / probe gathers
+constexpr int kTileRows = kGatherTileRows;  // tile height (rows)
+constexpr int kRowStep = kTileRows / 2;     // a thread's two pixels are kRowStep rows apart
+constexpr int kGatherNT = 256; // threads per tile, 2 pixels each
+static_assert(kGatherNT * 2 == kTile * kTileRows && kTileRows % 2 == 0, "gather tile split");
 constexpr int kPrefetch = 4;   // frames whose loads are issued together (object gather)
 constexpr int kPrefetchP = 4;  // the same for the probe gather
 
@@ -24,7 +26,7 @@ PTY_DEV void cmac_conj(float2& acc, float2 x, float2 p) {
 // ------------------------------------------------------------------ psup_O
 // era.py:336-369: O = sum_i psi_i * conj(P) placed at window i, / (heat + alpha),
 // with heat = sum_i |P|^2 (era.py:402-410) recomputed in the same pass when HEAT.
-// A thread owns 2 pixels (rows ty, ty + 8) of a 16 x 32 object tile; the tile's
+// A thread owns 2 pixels (rows ty, ty + kRowStep) of an object tile; the tile's
 // frames are visited in ascending order, kPrefetch at a time with all their
 // loads issued first.  Out-of-window pixels contribute an exact zero.
 template <bool HEAT>
@@ -34,7 +36,7 @@ __global__ void __launch_bounds__(kGatherNT) psup_O_kernel(
     float alpha, float2* __restrict__ O) {
   const int tile = blockIdx.x;
   const int tu = tile / tl.ntv, tv = tile % tl.ntv;
-  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  const int tx = threadIdx.x % kTile, ty = threadIdx.x / kTile;
   const int v = tv * kTile + tx;
   const int u0 = tu * kTileRows + ty;
   float2 acc[2];
@@ -53,7 +55,7 @@ __global__ void __launch_bounds__(kGatherNT) psup_O_kernel(
     const float2* pf = psi + (size_t)f * N0 * N1;
 #pragma unroll
     for (int k = 0; k < 2; ++k) {
-      const int a = u0 + 8 * k + r0;
+      const int a = u0 + kRowStep * k + r0;
       const bool ok = bok && a >= 0 && a < N0;
       x[k] = ok ? pf[a * N1 + b] : make_float2(0.f, 0.f);
       p[k] = ok ? P[a * N1 + b] : make_float2(0.f, 0.f);
@@ -91,7 +93,7 @@ __global__ void __launch_bounds__(kGatherNT) psup_O_kernel(
   if (v < V) {
 #pragma unroll
     for (int k = 0; k < 2; ++k) {
-      const int uu = u0 + 8 * k;
+      const int uu = u0 + kRowStep * k;
       if (uu < U) {
         const size_t o = (size_t)uu * V + v;
         double hd;
@@ -114,7 +116,7 @@ __global__ void __launch_bounds__(kGatherNT) heat_P_kernel(
     const float2* __restrict__ P, double* __restrict__ heat) {
   const int tile = blockIdx.x;
   const int tu = tile / tl.ntv, tv = tile % tl.ntv;
-  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  const int tx = threadIdx.x % kTile, ty = threadIdx.x / kTile;
   const int v = tv * kTile + tx;
   ff acc[2];
 #pragma unroll
@@ -124,7 +126,7 @@ __global__ void __launch_bounds__(kGatherNT) heat_P_kernel(
   auto term = [&](int e, int k) -> float {
     const int f = tl.frames[e];
     const int r0 = R[2 * f], r1 = R[2 * f + 1];
-    const int b = v + r1, a = tu * kTileRows + ty + 8 * k + r0;
+    const int b = v + r1, a = tu * kTileRows + ty + kRowStep * k + r0;
     return (b >= 0 && b < N1 && a >= 0 && a < N0) ? cabs2(__ldg(&P[a * N1 + b])) : 0.f;
   };
   // the same grouping as psup_O_kernel<true>: FP32 sums of kPrefetch entries,
@@ -148,7 +150,7 @@ __global__ void __launch_bounds__(kGatherNT) heat_P_kernel(
   if (v < V) {
 #pragma unroll
     for (int k = 0; k < 2; ++k) {
-      const int uu = tu * kTileRows + ty + 8 * k;
+      const int uu = tu * kTileRows + ty + kRowStep * k;
       if (uu < U) heat[(size_t)uu * V + v] = ff_to_double(acc[k]);
     }
   }
@@ -174,8 +176,8 @@ int launch_heat_P(const TileLists& tl, int n, int N0, int N1, int U, int V, cons
 
 // ------------------------------------------------------------------ psup_P
 // era.py:371-400 (+ make_O_heatmap era.py:412-417): per probe pixel, sum over
-// frames of psi_i * conj(O_i) and |O_i|^2.  Grid: 16 x 32 probe tiles x K frame
-// chunks; a thread owns 2 pixels (rows ty, ty + 8) and issues the loads of
+// frames of psi_i * conj(O_i) and |O_i|^2.  Grid: kTileRows x kTile probe tiles x K
+// frame chunks; a thread owns 2 pixels (rows ty, ty + kRowStep) and issues the loads of
 // kPrefetch frames together.
 __global__ void __launch_bounds__(kGatherNT) psup_P_partial_kernel(
     int n, int N0, int N1, int U, int V, const int* __restrict__ R, const float2* __restrict__ psi,
@@ -184,7 +186,7 @@ __global__ void __launch_bounds__(kGatherNT) psup_P_partial_kernel(
   const int ntv = (N1 + kTile - 1) / kTile;
   const int tile = blockIdx.x, k = blockIdx.y;
   const int tu = tile / ntv, tv = tile % ntv;
-  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  const int tx = threadIdx.x % kTile, ty = threadIdx.x / kTile;
   const int b = tv * kTile + tx;
   const int f0 = (int)(((long long)n * k) / K), f1 = (int)(((long long)n * (k + 1)) / K);
   float2 num[2];
@@ -201,7 +203,7 @@ __global__ void __launch_bounds__(kGatherNT) psup_P_partial_kernel(
       const int vv = b - r1;
 #pragma unroll
       for (int q = 0; q < 2; ++q) {
-        const int a = tu * kTileRows + ty + 8 * q;
+        const int a = tu * kTileRows + ty + kRowStep * q;
         if (a < N0) {
           o[q] = __ldg(&O[(size_t)(a - r0) * V + vv]);
           x[q] = pf[a * N1 + b];
@@ -238,7 +240,7 @@ __global__ void __launch_bounds__(kGatherNT) psup_P_partial_kernel(
     }
 #pragma unroll
     for (int q = 0; q < 2; ++q) {
-      const int a = tu * kTileRows + ty + 8 * q;
+      const int a = tu * kTileRows + ty + kRowStep * q;
       if (a < N0) {
         const size_t o = (size_t)k * N0 * N1 + (size_t)a * N1 + b;
         part_num[o] = num[q];
@@ -279,7 +281,7 @@ __global__ void psup_P_reduce_kernel(int npix, int K, const float2* __restrict__
 // block takes whole frame rows -- 1024 / N1 rows x N1 columns, 4 pixels per
 // thread (CPT columns of 1024 / (256 CPT) rows) -- so each psi load of a warp
 // reads a contiguous row segment and a block's reads of one frame are
-// consecutive rows (better DRAM page locality than 16 x 32 tiles).
+// consecutive rows (better DRAM page locality than small 2-D tiles).
 template <int CPT>
 __global__ void __launch_bounds__(kGatherNT) psup_P_rows_kernel(
     int n, int N0, int N1, int U, int V, const int* __restrict__ R, const float2* __restrict__ psi,
