@@ -96,7 +96,7 @@ def load(build_if_missing=True):
     if build_if_missing:
         path = _build.build()
     if not os.path.exists(path):
-        raise RuntimeError("libptycho_gb300.so is not built: run __graft_entry__.build()")
+        raise RuntimeError("libptycho_gb300.so is not built: run python -m ptychography_gb300._build")
     lib = ctypes.CDLL(path)
     for name, args in SIGNATURES.items():
         fn = getattr(lib, name)
