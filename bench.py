@@ -608,10 +608,13 @@ def e2e_public_api(w, K):
     n, N = w.I.shape[0], w.I.shape[1]
     U = w.U
     calls = 2 if w.method == 6 else 1
-    # per call: I (float32), background stack (float32), O, P, mask up; O, P,
-    # info['I'] (float32), heatmap (float64), histories and mean background down
-    h2d = calls * (n * N * N * 4 + (n * N * N * 4 if w.method >= 4 else 0) + U * U * 8 + N * N * 9)
-    d2h = calls * (U * U * 8 + N * N * 8 + n * N * N * 4 + U * U * 8 + 16 * K + N * N * 4)
+    # per call up: I (float32), O (complex64), P (complex64), mask (uint8); the DM
+    # call also one background pattern (float32; ERA's random background is drawn
+    # on the device).  Down: O, P, info['I'] (float32), heatmap (float64), the
+    # eMod / eCon histories and, for methods 4-6, the mean background.
+    h2d = calls * (n * N * N * 4 + U * U * 8 + N * N * 9) + (N * N * 4 if w.method >= 4 else 0)
+    d2h = calls * (U * U * 8 + N * N * 8 + n * N * N * 4 + U * U * 8 + 16 * K
+                   + (N * N * 4 if w.method >= 4 else 0))
     frames = n * K * calls
     return {"value": round(frames / dt, 1), "unit": "frame-iters/s",
             "h2d_bytes_per_step": int(h2d / K), "d2h_bytes_per_step": int(d2h / K),
