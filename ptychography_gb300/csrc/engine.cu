@@ -52,6 +52,7 @@ struct pty_plan {
   TileLists tl{};
   float2* d_tw0 = nullptr;
   float2* d_tw1 = nullptr;
+  float2* d_twf = nullptr;       // W_N1^e, e < N1
   double* d_heatP = nullptr;     // P_heatmap cache
   double* d_heatP2 = nullptr;    // DM metric-branch heatmap
   double* d_heatO = nullptr;     // O_heatmap cache
@@ -182,6 +183,7 @@ extern "C" int pty_plan_create(const pty_geometry* g, const int64_t* R_host, pty
   if ((rc = dalloc_t(p, &p->d_tile_frames, frames.size() + 1))) return fail(rc);
   if ((rc = dalloc_t(p, &p->d_tw0, (size_t)N0))) return fail(rc);
   if ((rc = dalloc_t(p, &p->d_tw1, (size_t)N1))) return fail(rc);
+  if ((rc = dalloc_t(p, &p->d_twf, (size_t)N1))) return fail(rc);
   if ((rc = dalloc_t(p, &p->d_heatP, nobj))) return fail(rc);
   if ((rc = dalloc_t(p, &p->d_heatP2, nobj))) return fail(rc);
   if ((rc = dalloc_t(p, &p->d_heatO, npix))) return fail(rc);
@@ -206,7 +208,8 @@ extern "C" int pty_plan_create(const pty_geometry* g, const int64_t* R_host, pty
   if ((rc = dalloc_t(p, &p->d_mean_part, (size_t)(p->Km > p->K ? p->Km : p->K) * npix))) return fail(rc);
   if ((rc = choose_frame_tile(N0, N1, FAM_PLAIN, &p->tile[FAM_PLAIN]))) return fail(rc);
   if ((rc = choose_frame_tile(N0, N1, FAM_BG, &p->tile[FAM_BG]))) return fail(rc);
-  p->eslots = p->tile[0] > p->tile[1] ? p->tile[0] : p->tile[1];
+  p->eslots = tile_ctas(p->tile[0]) > tile_ctas(p->tile[1]) ? tile_ctas(p->tile[0])
+                                                             : tile_ctas(p->tile[1]);
   if ((rc = dalloc_t(p, &p->d_err_part, (size_t)n * p->eslots))) return fail(rc);
   if ((rc = dalloc_t(p, &p->d_dn_part, (size_t)4 * p->ndn))) return fail(rc);
   if ((rc = dalloc_t(p, &p->d_shift, 2))) return fail(rc);
@@ -229,6 +232,11 @@ extern "C" int pty_plan_create(const pty_geometry* g, const int64_t* R_host, pty
     e = cudaMemcpy(p->d_tile_frames, frames.data(), frames.size() * sizeof(int), cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemcpy(p->d_tw0, tw0.data(), N0 * sizeof(float2), cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemcpy(p->d_tw1, tw1.data(), N1 * sizeof(float2), cudaMemcpyHostToDevice);
+  {
+    std::vector<float2> twf(N1);
+    make_full_twiddles(N1, twf.data());
+    if (e == cudaSuccess) e = cudaMemcpy(p->d_twf, twf.data(), N1 * sizeof(float2), cudaMemcpyHostToDevice);
+  }
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&p->cap, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&p->ev_in, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&p->ev_out, cudaEventDisableTiming);
@@ -246,6 +254,7 @@ static FrameArgs base_args(const pty_plan* p) {
   a.R = p->d_R;
   a.tw0 = p->d_tw0;
   a.tw1 = p->d_tw1;
+  a.twf = p->d_twf;
   a.amp_stride = (long long)p->N0 * p->N1;
   a.N0h = p->N0 / 2;
   a.N1h = p->N1 / 2;

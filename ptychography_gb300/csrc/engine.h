@@ -42,6 +42,7 @@ struct FrameArgs {
   int N0h, N1h;              // N0 / 2, N1 / 2 (back-projection index roll)
   const float2* tw0;         // twiddles of the column transform (length N0)
   const float2* tw1;         // twiddles of the row transform (length N1)
+  const float2* twf;         // W_N1^e, e < N1 (three-stage line transforms)
 };
 
 // Frame tiles: how many CTAs transform one frame.  Tile 1 is the single-CTA
@@ -54,6 +55,9 @@ enum FrameFamily { FAM_PLAIN = 0, FAM_BG = 1 };
 inline int frame_family(int op) {
   return (op == OP_EXIT7 || op == OP_PSI7 || op == OP_DM7) ? FAM_BG : FAM_PLAIN;
 }
+// Tile ids: C = C CTAs per frame with the two-stage line transforms;
+// 100 + C = C CTAs with three-stage transforms (32 threads x 8 values per line).
+inline int tile_ctas(int tile) { return tile % 100; }
 bool frame_shape_supported(int N0, int N1);
 int frame_tile_candidates(int N0, int N1, int* tiles, int cap);   // returns the count
 int max_frame_tile(int N0, int N1);
@@ -61,6 +65,7 @@ int choose_frame_tile(int N0, int N1, int family, int* tile);      // prepares t
 int launch_frame_op(int op, int N0, int N1, int tile, const FrameArgs& a, int nframes,
                     cudaStream_t st);
 void make_twiddles(int L, float2* out);   // host table tw[k1 * A + t], length L
+void make_full_twiddles(int L, float2* out);   // host table W_L^e, e < L
 
 int prepare_single_cta(int N0, int N1);
 int launch_single_cta_op(int op, int N0, int N1, const FrameArgs& a, int nframes, cudaStream_t st);
@@ -71,6 +76,8 @@ PTY_DECLARE_CLUSTER_TILE(128, 2)
 PTY_DECLARE_CLUSTER_TILE(192, 2)
 PTY_DECLARE_CLUSTER_TILE(256, 4)
 PTY_DECLARE_CLUSTER_TILE(256, 8)
+int prepare_cluster_256x8l();
+int launch_cluster_256x8l(int op, const FrameArgs& a, int nframes, cudaStream_t st);
 PTY_DECLARE_CLUSTER_TILE(512, 16)
 #undef PTY_DECLARE_CLUSTER_TILE
 

@@ -7,8 +7,9 @@
 // depends on the GPU's shared memory, register file and cluster scheduling:
 //
 //   128^2: 1 CTA of 512 threads (one per SM) or 2-CTA clusters of 256 (two per SM)
-//   256^2: 8-CTA clusters of 256 threads (two CTAs per SM) or 4-CTA clusters
-//          of 512 (one per SM)
+//   256^2: 8-CTA clusters of 256 threads (two CTAs per SM), 4-CTA clusters
+//          of 512 (one per SM), or (tile id 108) 8-CTA clusters of 512 threads
+//          with three-stage line transforms (two CTAs, 32 warps per SM)
 //
 // Tiles are chosen per op family: the background (Pmod_7) forms move more
 // bytes and hold more registers than the plain ones, and the fastest tile
@@ -45,7 +46,7 @@ struct ShapeTiles {
 
 constexpr ShapeTiles kShapes[] = {
     {32, 32, 1, {1, 0, 0, 0}},   {64, 64, 1, {1, 0, 0, 0}},   {32, 64, 1, {1, 0, 0, 0}},
-    {128, 128, 2, {1, 2, 0, 0}}, {192, 192, 1, {2, 0, 0, 0}}, {256, 256, 2, {8, 4, 0, 0}},
+    {128, 128, 2, {1, 2, 0, 0}}, {192, 192, 1, {2, 0, 0, 0}}, {256, 256, 3, {8, 4, 108, 0}},
     {512, 512, 1, {16, 0, 0, 0}},
 };
 
@@ -67,6 +68,7 @@ int prepare_tile(int N0, int N1, int tile) {
   if (N0 == 192 && N1 == 192 && tile == 2) return prepare_cluster_192x2();
   if (N0 == 256 && N1 == 256 && tile == 4) return prepare_cluster_256x4();
   if (N0 == 256 && N1 == 256 && tile == 8) return prepare_cluster_256x8();
+  if (N0 == 256 && N1 == 256 && tile == 108) return prepare_cluster_256x8l();
   if (N0 == 512 && N1 == 512 && tile == 16) return prepare_cluster_512x16();
   return set_error(PTY_ERR_UNSUPPORTED, "frame tile not built for this shape");
 }
@@ -89,7 +91,7 @@ int tune(const ShapeTiles* s, int family, int* best) {
   size_t F = ((size_t)256 << 20) / (npix * sizeof(float2));
   if (F < 64) F = 64;
   if (F > 8192) F = 8192;
-  float2 *psi = nullptr, *tw0 = nullptr, *tw1 = nullptr;
+  float2 *psi = nullptr, *tw0 = nullptr, *tw1 = nullptr, *twf = nullptr;
   float *amp = nullptr, *bg = nullptr;
   double* err = nullptr;
   const int op = family == FAM_BG ? OP_PSI7 : OP_PSI1;
@@ -102,15 +104,18 @@ int tune(const ShapeTiles* s, int family, int* best) {
   if (e == cudaSuccess) e = cudaMalloc(&err, F * 16 * sizeof(double));
   if (e == cudaSuccess) e = cudaMalloc(&tw0, N0 * sizeof(float2));
   if (e == cudaSuccess) e = cudaMalloc(&tw1, N1 * sizeof(float2));
+  if (e == cudaSuccess) e = cudaMalloc(&twf, N1 * sizeof(float2));
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaEventCreate(&e0);
   if (e == cudaSuccess) e = cudaEventCreate(&e1);
   if (e == cudaSuccess) {
-    std::vector<float2> h0(N0), h1(N1);
+    std::vector<float2> h0(N0), h1(N1), hf(N1);
     make_twiddles(N0, h0.data());
     make_twiddles(N1, h1.data());
+    make_full_twiddles(N1, hf.data());
     e = cudaMemcpyAsync(tw0, h0.data(), N0 * sizeof(float2), cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(tw1, h1.data(), N1 * sizeof(float2), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(twf, hf.data(), N1 * sizeof(float2), cudaMemcpyHostToDevice, st);
     // finite positive values (every byte 0x3c) in the waves and amplitudes
     if (e == cudaSuccess) e = cudaMemsetAsync(psi, 0x3c, F * npix * sizeof(float2), st);
     if (e == cudaSuccess) e = cudaMemsetAsync(amp, 0x3c, F * npix * sizeof(float), st);
@@ -134,6 +139,7 @@ int tune(const ShapeTiles* s, int family, int* best) {
     a.alpha = 1e-10f;
     a.tw0 = tw0;
     a.tw1 = tw1;
+    a.twf = twf;
     a.N0h = N0 / 2;
     a.N1h = N1 / 2;
     if ((rc = prepare_tile(N0, N1, tile))) break;
@@ -166,6 +172,7 @@ int tune(const ShapeTiles* s, int family, int* best) {
   cudaFree(err);
   cudaFree(tw0);
   cudaFree(tw1);
+  cudaFree(twf);
   return rc;
 }
 
@@ -189,7 +196,7 @@ int frame_tile_candidates(int N0, int N1, int* tiles, int cap) {
 int max_frame_tile(int N0, int N1) {
   const ShapeTiles* s = find_shape(N0, N1);
   int m = 1;
-  for (int i = 0; s && i < s->count; ++i) m = s->tiles[i] > m ? s->tiles[i] : m;
+  for (int i = 0; s && i < s->count; ++i) m = tile_ctas(s->tiles[i]) > m ? tile_ctas(s->tiles[i]) : m;
   return m;
 }
 
@@ -223,6 +230,7 @@ int launch_frame_op(int op, int N0, int N1, int tile, const FrameArgs& a, int nf
     if (N0 == 192 && tile == 2) return launch_cluster_192x2(op, a, nframes, st);
     if (N0 == 256 && tile == 4) return launch_cluster_256x4(op, a, nframes, st);
     if (N0 == 256 && tile == 8) return launch_cluster_256x8(op, a, nframes, st);
+    if (N0 == 256 && tile == 108) return launch_cluster_256x8l(op, a, nframes, st);
     if (N0 == 512 && tile == 16) return launch_cluster_512x16(op, a, nframes, st);
   }
   return set_error(PTY_ERR_UNSUPPORTED, "frame tile not built for this shape");
@@ -249,6 +257,15 @@ void make_twiddles(int L, float2* out) {
       const double th = -2.0 * pi * (double)((long long)t * k1 % L) / (double)L;
       out[k1 * A + t] = make_float2((float)std::cos(th), (float)std::sin(th));
     }
+}
+
+// twf[e] = exp(-2 pi i e / L), e < L, evaluated in double and rounded once.
+void make_full_twiddles(int L, float2* out) {
+  const double pi = 3.14159265358979323846;
+  for (int e = 0; e < L; ++e) {
+    const double th = -2.0 * pi * (double)e / (double)L;
+    out[e] = make_float2((float)std::cos(th), (float)std::sin(th));
+  }
 }
 
 }  // namespace pty

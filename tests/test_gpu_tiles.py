@@ -1,7 +1,8 @@
 """Frame tiles: every tile built for a shape gives the same exit waves.
 
 128 x 128 frames have a single-CTA kernel and a 2-CTA cluster kernel, 256 x 256
-frames 8- and 4-CTA cluster kernels.  Each tile, forced in turn, must match the
+frames 8- and 4-CTA cluster kernels (16 x 16 line transforms) and an 8-CTA
+kernel with three-stage 8 x 8 x 4 line transforms (tile 108).  Each tile, forced in turn, must match the
 oracle, and the exit waves, object and probe must be bit-identical across tiles
 (the same line transforms run in the same order); only the error sums, whose
 per-CTA partials are added in a different grouping, may differ in rounding.
@@ -19,6 +20,14 @@ from ptychography_gb300 import _native
 from test_gpu_cluster192 import small_problem
 
 pytestmark = pytest.mark.gpu
+
+
+# tiles sharing a line decomposition (bit-identical results), per frame size
+SAME_LINES = {128: [(1, 2)], 256: [(8, 4), (108,)]}
+
+
+def same_lines(N, t0, t1):
+    return any(t0 in grp and t1 in grp for grp in SAME_LINES[N])
 
 
 def candidates(N):
@@ -46,7 +55,7 @@ class forced_tile:
 def test_tiles_listed_and_chosen(N):
     lib = _native.load()
     c = candidates(N)
-    assert len(c) == 2
+    assert len(c) == {128: 2, 256: 3}[N]
     for fam in (0, 1):
         t = ctypes.c_int32(0)
         _native.check(lib.pty_get_frame_tile(N, N, fam, ctypes.byref(t)))
@@ -105,20 +114,31 @@ def test_pmod_7_every_tile(N):
         assert rel(p, ref) < 3e-6, tile
         assert rel(b.cpu().numpy(), bref) < 1e-5, tile
         assert float(e.cpu()[0]) == pytest.approx(em, rel=1e-5)
-        outs.append((p, b.cpu().numpy()))
-    for p, b in outs[1:]:
-        np.testing.assert_array_equal(p, outs[0][0])
-        np.testing.assert_array_equal(b, outs[0][1])
+        outs.append((tile, p, b.cpu().numpy()))
+    t0, p0, b0 = outs[0]
+    for t, p, b in outs[1:]:
+        if same_lines(N, t0, t):
+            np.testing.assert_array_equal(p, p0)
+            np.testing.assert_array_equal(b, b0)
+        else:   # other line transforms: agreement to FP32 rounding
+            assert rel(p, p0) < 3e-6 and rel(b, b0) < 1e-5
 
 
 @pytest.mark.parametrize("N", [128, 256])
 def test_era_m3_every_tile(N):
     I, R, P, O, M = small_problem(N, seed=N, side=3)
     res = []
-    for tile in candidates(N):
+    tiles = candidates(N)
+    for tile in tiles:
         with forced_tile(N, tile):
             res.append(pty.ERA(I, R.copy(), P * np.exp(0.2j), None, 3, mask=M, method=3))
-    for O_t, P_t, info in res[1:]:
-        np.testing.assert_array_equal(O_t, res[0][0])
-        np.testing.assert_array_equal(P_t, res[0][1])
-        np.testing.assert_allclose(info["eMod"], res[0][2]["eMod"], rtol=1e-6)
+    for t, (O_t, P_t, info) in zip(tiles[1:], res[1:]):
+        if same_lines(N, tiles[0], t):
+            np.testing.assert_array_equal(O_t, res[0][0])
+            np.testing.assert_array_equal(P_t, res[0][1])
+            np.testing.assert_allclose(info["eMod"], res[0][2]["eMod"], rtol=1e-6)
+        else:
+            # two FP32 rounding paths through three iterations on noisy data
+            # (each operator agrees with the FP64 oracle to 3e-6)
+            assert rel(O_t, res[0][0]) < 5e-5 and rel(P_t, res[0][1]) < 5e-5
+            np.testing.assert_allclose(info["eMod"], res[0][2]["eMod"], rtol=2e-5)
