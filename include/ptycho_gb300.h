@@ -196,11 +196,12 @@ int pty_shape_supported(int32_t N0, int32_t N1);
  * tiles chosen when it was created.
  *   pty_frame_tile_candidates: the tiles built for the shape (up to cap
  *     written to tiles[], their number to *count);
- *   pty_get_frame_tile: the tile new plans get for the family (tunes now if
- *     not yet done);
+ *   pty_get_frame_tile: the tile new plans with at least one frame per SM
+ *     get for the family (tunes now if not yet done); plans with fewer frames
+ *     are tuned on their own frame count;
  *   pty_set_frame_tile: force a listed tile for the family in plans created
- *     afterwards on the current device; tile 0 forgets the choice (tuned
- *     again next time). */
+ *     afterwards on the current device, whatever their frame count; tile 0
+ *     forgets forced and tuned choices (tuned again next time). */
 int pty_frame_tile_candidates(int32_t N0, int32_t N1, int32_t* tiles, int32_t cap, int32_t* count);
 int pty_get_frame_tile(int32_t N0, int32_t N1, int32_t family, int32_t* tile);
 int pty_set_frame_tile(int32_t N0, int32_t N1, int32_t family, int32_t tile);

@@ -206,8 +206,8 @@ extern "C" int pty_plan_create(const pty_geometry* g, const int64_t* R_host, pty
   if ((rc = dalloc_t(p, &p->d_part_num, (size_t)p->K * npix))) return fail(rc);
   if ((rc = dalloc_t(p, &p->d_part_den, (size_t)p->K * npix))) return fail(rc);
   if ((rc = dalloc_t(p, &p->d_mean_part, (size_t)(p->Km > p->K ? p->Km : p->K) * npix))) return fail(rc);
-  if ((rc = choose_frame_tile(N0, N1, FAM_PLAIN, &p->tile[FAM_PLAIN]))) return fail(rc);
-  if ((rc = choose_frame_tile(N0, N1, FAM_BG, &p->tile[FAM_BG]))) return fail(rc);
+  if ((rc = choose_frame_tile(N0, N1, FAM_PLAIN, n, &p->tile[FAM_PLAIN]))) return fail(rc);
+  if ((rc = choose_frame_tile(N0, N1, FAM_BG, n, &p->tile[FAM_BG]))) return fail(rc);
   p->eslots = tile_ctas(p->tile[0]) > tile_ctas(p->tile[1]) ? tile_ctas(p->tile[0])
                                                              : tile_ctas(p->tile[1]);
   if ((rc = dalloc_t(p, &p->d_err_part, (size_t)n * p->eslots))) return fail(rc);

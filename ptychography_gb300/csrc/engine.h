@@ -61,7 +61,8 @@ inline int tile_ctas(int tile) { return tile % 100; }
 bool frame_shape_supported(int N0, int N1);
 int frame_tile_candidates(int N0, int N1, int* tiles, int cap);   // returns the count
 int max_frame_tile(int N0, int N1);
-int choose_frame_tile(int N0, int N1, int family, int* tile);      // prepares the kernels too
+// nframes: the plan's frame count (0: a large launch); prepares the kernels too
+int choose_frame_tile(int N0, int N1, int family, int nframes, int* tile);
 int launch_frame_op(int op, int N0, int N1, int tile, const FrameArgs& a, int nframes,
                     cudaStream_t st);
 void make_twiddles(int L, float2* out);   // host table tw[k1 * A + t], length L

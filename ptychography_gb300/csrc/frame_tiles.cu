@@ -18,12 +18,15 @@
 // OP_PSI1 for the plain family, OP_PSI7 for the background family; five timed
 // launches each after a warm-up, fastest kept -- and keeps the winners for the
 // process; a candidate replaces the first-listed default only when at least
-// 3 % faster.
+// 3 % faster.  A plan with fewer frames than the GPU has SMs launches less
+// than one wave, where per-frame latency rather than throughput decides; such
+// frame counts are tuned on exactly that many frames, each count once.
 // PTY_AUTOTUNE=0 in the environment skips the timing and takes the first
-// candidate listed; pty_set_frame_tile forces a tile.  Every tile runs the
-// same line transforms in the same order, so the exit waves, object and probe
-// do not depend on the choice; only the summation order of the per-frame
-// error partials (one per CTA) does.
+// candidate listed; pty_set_frame_tile forces a tile for every frame count.
+// Tiles with the same line transforms give the same exit waves, object and
+// probe; only the summation order of the per-frame error partials (one per
+// CTA) differs.  Tile 108's three-stage transforms agree with the others to
+// FP32 rounding.
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
@@ -73,9 +76,10 @@ int prepare_tile(int N0, int N1, int tile) {
   return set_error(PTY_ERR_UNSUPPORTED, "frame tile not built for this shape");
 }
 
-using Key = std::tuple<int, int, int, int>;   // device, N0, N1, family
+using Key = std::tuple<int, int, int, int, int>;   // device, N0, N1, family, frames class
 std::mutex g_mu;
-std::map<Key, int> g_tile;               // chosen tile per device and shape
+std::map<Key, int> g_tile;               // tuned tile per device, shape, family, frames class
+std::map<Key, int> g_forced;             // tiles forced by pty_set_frame_tile
 
 bool autotune_enabled() {
   const char* v = std::getenv("PTY_AUTOTUNE");
@@ -84,13 +88,16 @@ bool autotune_enabled() {
 
 // Times the family's op (OP_PSI1 / OP_PSI7) with each candidate tile on F
 // scratch frames; *best = fastest.
-int tune(const ShapeTiles* s, int family, int* best) {
+int tune(const ShapeTiles* s, int family, int small_frames, int* best) {
   const int N0 = s->N0, N1 = s->N1;
   const size_t npix = (size_t)N0 * N1;
-  // about 256 MiB of exit waves: several waves of CTAs, larger than L2
+  // about 256 MiB of exit waves (several waves of CTAs, larger than L2), or the
+  // plan's own frame count for launches too small to fill the GPU, where the
+  // per-frame latency decides
   size_t F = ((size_t)256 << 20) / (npix * sizeof(float2));
   if (F < 64) F = 64;
   if (F > 8192) F = 8192;
+  if (small_frames > 0) F = (size_t)small_frames;
   float2 *psi = nullptr, *tw0 = nullptr, *tw1 = nullptr, *twf = nullptr;
   float *amp = nullptr, *bg = nullptr;
   double* err = nullptr;
@@ -200,20 +207,34 @@ int max_frame_tile(int N0, int N1) {
   return m;
 }
 
-int choose_frame_tile(int N0, int N1, int family, int* tile) {
+// Frame counts below this many per SM form their own tuning class, tuned on
+// exactly that many frames (one class per count, the counts being small).
+constexpr int kSmallFramesPerSM = 1;
+
+int choose_frame_tile(int N0, int N1, int family, int nframes, int* tile) {
   const ShapeTiles* s = find_shape(N0, N1);
   if (!s) return set_error(PTY_ERR_SHAPE, "frame shape not supported by the fused FFT kernels");
   if (family != FAM_PLAIN && family != FAM_BG) return set_error(PTY_ERR_ARG, "unknown op family");
   int dev = 0;
   PTY_TRY(current_device(&dev));
+  int sms = 0;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+    cudaGetLastError();
+    sms = 0;
+  }
+  const int small = (nframes > 0 && nframes < kSmallFramesPerSM * sms) ? nframes : 0;
   std::lock_guard<std::mutex> lock(g_mu);
-  const Key key{dev, N0, N1, family};
+  // a forced tile (pty_set_frame_tile, class 0) applies to every frame count
+  auto forced = g_forced.find(Key{dev, N0, N1, family, 0});
+  const Key key{dev, N0, N1, family, small};
   auto it = g_tile.find(key);
   int t = s->tiles[0];
-  if (it != g_tile.end()) {
+  if (forced != g_forced.end()) {
+    t = forced->second;
+  } else if (it != g_tile.end()) {
     t = it->second;
   } else {
-    if (s->count > 1 && autotune_enabled()) PTY_TRY(tune(s, family, &t));
+    if (s->count > 1 && autotune_enabled()) PTY_TRY(tune(s, family, small, &t));
     g_tile[key] = t;
   }
   PTY_TRY(prepare_tile(N0, N1, t));
@@ -286,7 +307,7 @@ extern "C" int pty_frame_tile_candidates(int32_t N0, int32_t N1, int32_t* tiles,
 extern "C" int pty_get_frame_tile(int32_t N0, int32_t N1, int32_t family, int32_t* tile) {
   if (!tile) return set_error(PTY_ERR_ARG, "null argument");
   int t = 0;
-  PTY_TRY(choose_frame_tile(N0, N1, family, &t));
+  PTY_TRY(choose_frame_tile(N0, N1, family, 0, &t));
   *tile = t;
   return PTY_OK;
 }
@@ -300,12 +321,20 @@ extern "C" int pty_set_frame_tile(int32_t N0, int32_t N1, int32_t family, int32_
   int dev = 0;
   PTY_TRY(current_device(&dev));
   std::lock_guard<std::mutex> lock(g_mu);
-  const Key key{dev, (int)N0, (int)N1, (int)family};
-  if (tile == 0) {
-    g_tile.erase(key);
+  const Key key{dev, (int)N0, (int)N1, (int)family, 0};
+  if (tile == 0) {   // forget the forced tile and every tuned choice for the shape
+    g_forced.erase(key);
+    for (auto it = g_tile.begin(); it != g_tile.end();) {
+      const Key& k = it->first;
+      if (std::get<0>(k) == dev && std::get<1>(k) == N0 && std::get<2>(k) == N1 &&
+          std::get<3>(k) == family)
+        it = g_tile.erase(it);
+      else
+        ++it;
+    }
     return PTY_OK;
   }
   PTY_TRY(prepare_tile(N0, N1, tile));
-  g_tile[key] = tile;
+  g_forced[key] = tile;
   return PTY_OK;
 }
