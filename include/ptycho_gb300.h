@@ -186,11 +186,12 @@ int pty_shape_supported(int32_t N0, int32_t N1);
 /* Frame tiles (no reference counterpart): the number of CTAs that transform
  * one frame, 1 = one CTA per frame, C > 1 = a cluster of C CTAs; 100 + C = a
  * cluster of C CTAs whose line transforms run in three stages over 32
- * threads x 8 values (more threads per CTA at fewer registers).  Tiles are
- * chosen per op family: family 0 = the plain forms (Pmod_1, model error,
- * intensities, back projection), family 1 = the background forms (Pmod_7 and
- * the DM background recursion).  Shapes with more than one tile built
- * (128 x 128: 1 or 2; 256 x 256: 8, 4 or 108) get theirs from an autotuner run
+ * threads (8 values per thread at 256 points, 16 at 512: more threads per
+ * CTA at fewer registers).  Tiles are chosen per op family: family 0 = the
+ * plain forms (Pmod_1, model error, intensities, back projection), family 1
+ * = the background forms (Pmod_7 and the DM background recursion).  Shapes
+ * with more than one tile built (128 x 128: 1 or 2; 256 x 256: 8, 4 or 108;
+ * 512 x 512: 16 or 116) get theirs from an autotuner run
  * by the first plan created for the shape on a device (disabled by
  * PTY_AUTOTUNE=0 in the environment: first candidate).  A plan keeps the
  * tiles chosen when it was created.

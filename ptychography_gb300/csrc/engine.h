@@ -80,6 +80,8 @@ PTY_DECLARE_CLUSTER_TILE(256, 8)
 int prepare_cluster_256x8l();
 int launch_cluster_256x8l(int op, const FrameArgs& a, int nframes, cudaStream_t st);
 PTY_DECLARE_CLUSTER_TILE(512, 16)
+int prepare_cluster_512x16l();
+int launch_cluster_512x16l(int op, const FrameArgs& a, int nframes, cudaStream_t st);
 #undef PTY_DECLARE_CLUSTER_TILE
 
 // error reporting (engine.cu)

@@ -10,6 +10,9 @@
 //   256^2: 8-CTA clusters of 256 threads (two CTAs per SM), 4-CTA clusters
 //          of 512 (one per SM), or (tile id 108) 8-CTA clusters of 512 threads
 //          with three-stage line transforms (two CTAs, 32 warps per SM)
+//   512^2: 16-CTA clusters of 256 threads (32 values per thread), or (tile
+//          id 116) of 512 threads with three-stage line transforms (16 values
+//          per thread, 16 warps per SM); one CTA per SM either way
 //
 // Tiles are chosen per op family: the background (Pmod_7) forms move more
 // bytes and hold more registers than the plain ones, and the fastest tile
@@ -25,8 +28,8 @@
 // candidate listed; pty_set_frame_tile forces a tile for every frame count.
 // Tiles with the same line transforms give the same exit waves, object and
 // probe; only the summation order of the per-frame error partials (one per
-// CTA) differs.  Tile 108's three-stage transforms agree with the others to
-// FP32 rounding.
+// CTA) differs.  The three-stage transforms of tiles 108 and 116 agree with
+// the others to FP32 rounding.
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
@@ -50,7 +53,7 @@ struct ShapeTiles {
 constexpr ShapeTiles kShapes[] = {
     {32, 32, 1, {1, 0, 0, 0}},   {64, 64, 1, {1, 0, 0, 0}},   {32, 64, 1, {1, 0, 0, 0}},
     {128, 128, 2, {1, 2, 0, 0}}, {192, 192, 1, {2, 0, 0, 0}}, {256, 256, 3, {8, 4, 108, 0}},
-    {512, 512, 1, {16, 0, 0, 0}},
+    {512, 512, 2, {16, 116, 0, 0}},
 };
 
 const ShapeTiles* find_shape(int N0, int N1) {
@@ -73,6 +76,7 @@ int prepare_tile(int N0, int N1, int tile) {
   if (N0 == 256 && N1 == 256 && tile == 8) return prepare_cluster_256x8();
   if (N0 == 256 && N1 == 256 && tile == 108) return prepare_cluster_256x8l();
   if (N0 == 512 && N1 == 512 && tile == 16) return prepare_cluster_512x16();
+  if (N0 == 512 && N1 == 512 && tile == 116) return prepare_cluster_512x16l();
   return set_error(PTY_ERR_UNSUPPORTED, "frame tile not built for this shape");
 }
 
@@ -253,6 +257,7 @@ int launch_frame_op(int op, int N0, int N1, int tile, const FrameArgs& a, int nf
     if (N0 == 256 && tile == 8) return launch_cluster_256x8(op, a, nframes, st);
     if (N0 == 256 && tile == 108) return launch_cluster_256x8l(op, a, nframes, st);
     if (N0 == 512 && tile == 16) return launch_cluster_512x16(op, a, nframes, st);
+    if (N0 == 512 && tile == 116) return launch_cluster_512x16l(op, a, nframes, st);
   }
   return set_error(PTY_ERR_UNSUPPORTED, "frame tile not built for this shape");
 }
