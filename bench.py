@@ -510,7 +510,9 @@ def roofline_pmod7(job, torch, tile, sm_max_mhz, reps=20):
     # capture of this kernel (256^2 frames, 8-CTA tile): 880.7 MB for 512
     # frames, scaled by frames; recorded for that kernel only
     traffic = round(880.7e6 * job.n / 512) if (job.N == 256 and tile == 8) else None
-    if tile > 100:      # three-stage line transforms
+    if tile > 200:      # staged: row, column and row launches through a frame scratch
+        kname = "staged_rows_kernel<PSI7> + staged_cols_kernel<PSI7> + staged_rows_kernel<PSI7>"
+    elif tile > 100:    # three-stage line transforms
         kname = "line3_cluster_kernel<PSI7>" if job.N == 256 else "line3_512_kernel<PSI7>"
     elif tile > 1:
         kname = "cluster_frame_kernel<%d,%d,PSI7>" % (job.N, tile)

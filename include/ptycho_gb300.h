@@ -187,11 +187,14 @@ int pty_shape_supported(int32_t N0, int32_t N1);
  * one frame, 1 = one CTA per frame, C > 1 = a cluster of C CTAs; 100 + C = a
  * cluster of C CTAs whose line transforms run in three stages over 32
  * threads (8 values per thread at 256 points, 16 at 512: more threads per
- * CTA at fewer registers).  Tiles are chosen per op family: family 0 = the
+ * CTA at fewer registers); 200 + C = staged: a row launch, a column launch
+ * (C CTAs per frame) and an inverse row launch through a frame scratch of
+ * about 2 GiB held by the plan, without clusters (512 x 512: tile 264).
+ * Tiles are chosen per op family: family 0 = the
  * plain forms (Pmod_1, model error, intensities, back projection), family 1
  * = the background forms (Pmod_7 and the DM background recursion).  Shapes
  * with more than one tile built (128 x 128: 1 or 2; 256 x 256: 8, 4 or 108;
- * 512 x 512: 16 or 116) get theirs from an autotuner run
+ * 512 x 512: 16, 116 or 264) get theirs from an autotuner run
  * by the first plan created for the shape on a device (disabled by
  * PTY_AUTOTUNE=0 in the environment: first candidate).  A plan keeps the
  * tiles chosen when it was created.

@@ -63,6 +63,8 @@ struct pty_plan {
   int Km = 1;                    // background-mean frame chunks
   float2* d_mean_part = nullptr;
   double* d_err_part = nullptr;  // [n * eslots]
+  float2* d_stage = nullptr;     // frame scratch of a staged tile
+  int stage_frames = 0;
   int tile[2] = {1, 1};          // CTAs per frame of the fused frame kernels, per op family
   int eslots = 1;                // error-partial slots per frame (the larger family tile)
   int ndn = 304;                 // diffnorm blocks per array (two per SM)
@@ -211,6 +213,10 @@ extern "C" int pty_plan_create(const pty_geometry* g, const int64_t* R_host, pty
   p->eslots = tile_ctas(p->tile[0]) > tile_ctas(p->tile[1]) ? tile_ctas(p->tile[0])
                                                              : tile_ctas(p->tile[1]);
   if ((rc = dalloc_t(p, &p->d_err_part, (size_t)n * p->eslots))) return fail(rc);
+  if (tile_staged(p->tile[0]) || tile_staged(p->tile[1])) {
+    p->stage_frames = staged_group_frames(N0, N1) < n ? staged_group_frames(N0, N1) : n;
+    if ((rc = dalloc_t(p, &p->d_stage, (size_t)p->stage_frames * npix))) return fail(rc);
+  }
   if ((rc = dalloc_t(p, &p->d_dn_part, (size_t)4 * p->ndn))) return fail(rc);
   if ((rc = dalloc_t(p, &p->d_shift, 2))) return fail(rc);
   if ((rc = dalloc_t(p, &p->d_bakO, nobj))) return fail(rc);
@@ -259,6 +265,8 @@ static FrameArgs base_args(const pty_plan* p) {
   a.N0h = p->N0 / 2;
   a.N1h = p->N1 / 2;
   a.err_stride = p->eslots;
+  a.stage = p->d_stage;
+  a.stage_frames = p->stage_frames;
   return a;
 }
 

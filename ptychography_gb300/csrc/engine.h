@@ -43,6 +43,8 @@ struct FrameArgs {
   const float2* tw0;         // twiddles of the column transform (length N0)
   const float2* tw1;         // twiddles of the row transform (length N1)
   const float2* twf;         // W_N1^e, e < N1 (three-stage line transforms)
+  float2* stage;             // [stage_frames][N0][N1] frame scratch of the staged tiles
+  int stage_frames;          // frames the scratch holds (launches run in groups of it)
 };
 
 // Frame tiles: how many CTAs transform one frame.  Tile 1 is the single-CTA
@@ -56,8 +58,13 @@ inline int frame_family(int op) {
   return (op == OP_EXIT7 || op == OP_PSI7 || op == OP_DM7) ? FAM_BG : FAM_PLAIN;
 }
 // Tile ids: C = C CTAs per frame with the two-stage line transforms;
-// 100 + C = C CTAs with three-stage transforms (32 threads x 8 values per line).
+// 100 + C = C CTAs with three-stage transforms (32 threads per line);
+// 200 + C = staged: row, column and row launches through a frame scratch, C
+// column CTAs per frame.  tile_ctas = the error-partial slots a frame needs.
 inline int tile_ctas(int tile) { return tile % 100; }
+inline bool tile_staged(int tile) { return tile >= 200; }
+// frames of scratch a staged tile works through at a time
+int staged_group_frames(int N0, int N1);
 bool frame_shape_supported(int N0, int N1);
 int frame_tile_candidates(int N0, int N1, int* tiles, int cap);   // returns the count
 int max_frame_tile(int N0, int N1);
@@ -82,6 +89,8 @@ int launch_cluster_256x8l(int op, const FrameArgs& a, int nframes, cudaStream_t 
 PTY_DECLARE_CLUSTER_TILE(512, 16)
 int prepare_cluster_512x16l();
 int launch_cluster_512x16l(int op, const FrameArgs& a, int nframes, cudaStream_t st);
+int prepare_staged_512();
+int launch_staged_512(int op, const FrameArgs& a, int nframes, cudaStream_t st);
 #undef PTY_DECLARE_CLUSTER_TILE
 
 // error reporting (engine.cu)

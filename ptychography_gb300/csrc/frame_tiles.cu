@@ -53,7 +53,7 @@ struct ShapeTiles {
 constexpr ShapeTiles kShapes[] = {
     {32, 32, 1, {1, 0, 0, 0}},   {64, 64, 1, {1, 0, 0, 0}},   {32, 64, 1, {1, 0, 0, 0}},
     {128, 128, 2, {1, 2, 0, 0}}, {192, 192, 1, {2, 0, 0, 0}}, {256, 256, 3, {8, 4, 108, 0}},
-    {512, 512, 2, {16, 116, 0, 0}},
+    {512, 512, 3, {16, 116, 264, 0}},
 };
 
 const ShapeTiles* find_shape(int N0, int N1) {
@@ -77,6 +77,7 @@ int prepare_tile(int N0, int N1, int tile) {
   if (N0 == 256 && N1 == 256 && tile == 108) return prepare_cluster_256x8l();
   if (N0 == 512 && N1 == 512 && tile == 16) return prepare_cluster_512x16();
   if (N0 == 512 && N1 == 512 && tile == 116) return prepare_cluster_512x16l();
+  if (N0 == 512 && N1 == 512 && tile == 264) return prepare_staged_512();
   return set_error(PTY_ERR_UNSUPPORTED, "frame tile not built for this shape");
 }
 
@@ -102,7 +103,11 @@ int tune(const ShapeTiles* s, int family, int small_frames, int* best) {
   if (F < 64) F = 64;
   if (F > 8192) F = 8192;
   if (small_frames > 0) F = (size_t)small_frames;
-  float2 *psi = nullptr, *tw0 = nullptr, *tw1 = nullptr, *twf = nullptr;
+  float2 *psi = nullptr, *tw0 = nullptr, *tw1 = nullptr, *twf = nullptr, *stage = nullptr;
+  bool staged = false;
+  for (int i = 0; i < s->count; ++i) staged = staged || tile_staged(s->tiles[i]);
+  int stage_frames = staged_group_frames(N0, N1);
+  if (stage_frames > (int)F) stage_frames = (int)F;
   float *amp = nullptr, *bg = nullptr;
   double* err = nullptr;
   const int op = family == FAM_BG ? OP_PSI7 : OP_PSI1;
@@ -112,7 +117,8 @@ int tune(const ShapeTiles* s, int family, int small_frames, int* best) {
   cudaError_t e = cudaMalloc(&psi, F * npix * sizeof(float2));
   if (e == cudaSuccess) e = cudaMalloc(&amp, F * npix * sizeof(float));
   if (e == cudaSuccess && family == FAM_BG) e = cudaMalloc(&bg, F * npix * sizeof(float));
-  if (e == cudaSuccess) e = cudaMalloc(&err, F * 16 * sizeof(double));
+  if (e == cudaSuccess) e = cudaMalloc(&err, F * 64 * sizeof(double));
+  if (e == cudaSuccess && staged) e = cudaMalloc(&stage, (size_t)stage_frames * npix * sizeof(float2));
   if (e == cudaSuccess) e = cudaMalloc(&tw0, N0 * sizeof(float2));
   if (e == cudaSuccess) e = cudaMalloc(&tw1, N1 * sizeof(float2));
   if (e == cudaSuccess) e = cudaMalloc(&twf, N1 * sizeof(float2));
@@ -143,7 +149,9 @@ int tune(const ShapeTiles* s, int family, int small_frames, int* best) {
     a.amp = amp;
     a.amp_stride = (long long)npix;
     a.err_part = err;
-    a.err_stride = 16;
+    a.err_stride = 64;
+    a.stage = stage;
+    a.stage_frames = stage_frames;
     a.bg_in = bg;
     a.bg_out = bg;
     a.bg_stride = (long long)npix;
@@ -184,6 +192,7 @@ int tune(const ShapeTiles* s, int family, int small_frames, int* best) {
   cudaFree(tw0);
   cudaFree(tw1);
   cudaFree(twf);
+  cudaFree(stage);
   return rc;
 }
 
@@ -196,6 +205,16 @@ int current_device(int* dev) {
 }  // namespace
 
 bool frame_shape_supported(int N0, int N1) { return find_shape(N0, N1) != nullptr; }
+
+int staged_group_frames(int N0, int N1) {
+  // about 2 GiB of scratch: launches large enough that their tails and the
+  // gaps between the three launches of a group cost little (measured: groups
+  // of 1024 512^2 frames ran Pmod_7 3 % faster than groups of 256, 17 %
+  // faster than groups of 64, whose scratch mostly stays in L2)
+  const long long per = (long long)N0 * N1 * (long long)sizeof(float2);
+  const long long g = ((long long)1 << 31) / per;
+  return g < 1 ? 1 : (int)g;
+}
 
 int frame_tile_candidates(int N0, int N1, int* tiles, int cap) {
   const ShapeTiles* s = find_shape(N0, N1);
@@ -258,6 +277,7 @@ int launch_frame_op(int op, int N0, int N1, int tile, const FrameArgs& a, int nf
     if (N0 == 256 && tile == 108) return launch_cluster_256x8l(op, a, nframes, st);
     if (N0 == 512 && tile == 16) return launch_cluster_512x16(op, a, nframes, st);
     if (N0 == 512 && tile == 116) return launch_cluster_512x16l(op, a, nframes, st);
+    if (N0 == 512 && tile == 264) return launch_staged_512(op, a, nframes, st);
   }
   return set_error(PTY_ERR_UNSUPPORTED, "frame tile not built for this shape");
 }

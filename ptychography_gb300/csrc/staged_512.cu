@@ -1,0 +1,293 @@
+// 512 x 512 frames in three launches through a frame scratch (tile 264).
+//
+// A 512^2 complex64 frame (2 MB) fills the shared memory of 16 SMs, so the
+// cluster tiles need 16 free SMs of one GPC per frame: on a 152-SM GB300 only
+// 7 such clusters are resident at once (112 SMs), whatever the kernel does.
+// This tile keeps every SM busy instead, at the price of a scratch round trip:
+//   1. row launch: one warp per frame row forms the input wave (exit wave,
+//      psi, or the DM combination), row-FFTs it (line3_fft512, warp-local
+//      exchanges) and writes the row to the scratch;
+//   2. column launch: a CTA takes 8 columns of one frame (32 line threads
+//      each), forward column FFT, the modulus constraint, inverse column FFT,
+//      and writes the columns back (or, for the forms without an inverse,
+//      writes their result);
+//   3. row launch: inverse row FFT of the scratch rows, scaled, written as the
+//      new wave (with the DM update).
+// The scratch holds stage_frames frames; larger launches run group by group.
+// Each CTA is independent: no cluster barrier, two or three CTAs per SM.  The column launch writes
+// one error partial per CTA: 64 slots per frame (the tile id is 200 + 64).
+// Line transforms, slot layouts and the per-pixel operations are those of the
+// 16-CTA tile 116, so results agree with it to FP32 rounding.
+// Replaces the same reference functions as frame_kernels.cu.
+#include <cstdint>
+
+#include "engine.h"
+#include "fft_line3.cuh"
+#include "frame_ops.cuh"
+
+namespace pty {
+
+namespace {
+
+constexpr int kN = 512;
+constexpr int kA = 32, kB = 16;             // line threads x values
+constexpr int kNT = 256;                    // threads per CTA, both launches
+constexpr int kRows = kNT / kA;             // rows per row CTA (one warp each)
+constexpr int kCols = kNT / kA;             // columns per column CTA
+constexpr int kBlocksPerFrame = kN / kRows; // = kN / kCols = 64
+constexpr int kRowScr = 542;                // row-exchange slots per warp
+constexpr int kColE1 = 527;                 // column exchange-1 slots (33 k1 + t)
+constexpr size_t kColSmem = (size_t)(kColE1 + kN) * kCols * sizeof(float2) + (size_t)2 * kN * kCols * sizeof(float);
+static_assert(kRows == kCols && kBlocksPerFrame == 64, "64 blocks per frame per launch");
+
+// Row slot layouts (a warp is one line; each half-warp touches 16 distinct
+// bank pairs): exchange 1 at 34 k1 + t (max 541), exchange 2 at
+// (k1 xor 8 (t1 & 1)) + 16 t1 + 64 m1 (max 511).
+PTY_DEV int row_s1(int t, int k1) { return 34 * k1 + t; }
+PTY_DEV int any_s2(int k1, int t1, int m1) { return (k1 ^ ((t1 & 1) << 3)) + 16 * t1 + 64 * m1; }
+// Column slot layouts: slot s of a column sits at s * 8 + column, so a
+// half-warp (two line threads x 8 columns) is conflict-free when its two
+// slots differ in parity: exchange 1 at 33 k1 + t (max 526); exchange 2 as
+// along rows (its two slots differ by one in every access).
+PTY_DEV int col_s1(int t, int k1) { return 33 * k1 + t; }
+
+PTY_DEV void load_twiddles(const FrameArgs& g, float2* tw1, float2* tw2) {
+  for (int i = threadIdx.x; i < kN; i += kNT) tw1[i] = g.twf[((i & 31) * (i >> 5)) & 511];   // W^(t k1)
+  if (threadIdx.x < 32) tw2[threadIdx.x] = g.twf[16 * (threadIdx.x & 3) * (threadIdx.x >> 2)];
+}
+
+// Row launch.  !LAST: input wave -> forward row FFT -> scratch.
+// LAST: scratch -> inverse row FFT -> scaled output wave.
+template <int OP, bool LAST>
+__global__ void __launch_bounds__(kNT, 2) staged_rows_kernel(FrameArgs g, int f0) {
+  using T = OpTraits<OP>;
+  constexpr float kInv = 1.0f / (float)(kN * kN);
+  __shared__ float2 tw1[kN];
+  __shared__ float2 tw2[32];
+  __shared__ float2 rscr[kRows * kRowScr];
+  load_twiddles(g, tw1, tw2);
+  const int fl = blockIdx.x / kBlocksPerFrame, f = f0 + fl;
+  const int t = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int a = (blockIdx.x % kBlocksPerFrame) * kRows + w;
+  int r0 = 0, r1 = 0;
+  if (T::IN_EXIT || T::IN_DM) {
+    r0 = g.R[2 * f];
+    r1 = g.R[2 * f + 1];
+  }
+  float2* psi = g.psi + (size_t)f * kN * kN;
+  float2* srow = g.stage + (size_t)fl * kN * kN + (size_t)a * kN;
+  float2* rs = rscr + w * kRowScr;
+  auto row_e = [rs](int s) -> float2& { return rs[s]; };
+  auto warp_sync = [] { __syncwarp(); };
+  __syncthreads();
+  float2 v[kB];
+  if constexpr (!LAST) {
+#pragma unroll
+    for (int j = 0; j < kB; ++j) v[j] = frame_input<kN, OP>(g, f, r0, r1, psi, a, t + kA * j);
+    line3_fft512<T::FIRST_DIR, true>(v, t, row_e, row_e, row_s1, any_s2, warp_sync, tw1, tw2);
+#pragma unroll
+    for (int j = 0; j < kB; ++j) srow[t + kA * j] = v[j];
+  } else {
+#pragma unroll
+    for (int j = 0; j < kB; ++j) v[j] = srow[t + kA * j];
+    line3_fft512<+1, true>(v, t, row_e, row_e, row_s1, any_s2, warp_sync, tw1, tw2);
+#pragma unroll
+    for (int j = 0; j < kB; ++j) v[j] = cscale(v[j], kInv);
+    frame_output_line<kN, OP, kA, kB>(g, r0, r1, psi, a, t, v);
+  }
+}
+
+PTY_DEV void cp_async16(void* smem, const void* gmem) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(sa), "l"(gmem) : "memory");
+}
+PTY_DEV void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
+// Column launch: 8 columns of one frame per CTA, thread (cw, tc) = line
+// thread tc of column c0 + cw.  Every global input of the CTA -- its scratch
+// columns, amplitudes and background -- is copied into shared memory by
+// cp.async at the start, so the CTA waits for HBM once and holds no
+// registers for loads in flight; the mask bytes (shared by all frames,
+// L2-resident) are read alongside, four to a register.
+template <int OP>
+__global__ void __launch_bounds__(kNT, 2) staged_cols_kernel(FrameArgs g, int f0) {
+  using T = OpTraits<OP>;
+  using MI = ModIn<OP, kB>;
+  __shared__ float2 tw1[kN];
+  __shared__ float2 tw2[32];
+  __shared__ double red[32];
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float2* x1 = reinterpret_cast<float2*>(smem_raw);      // [527][8] exchange 1
+  float2* x2 = x1 + (size_t)kColE1 * kCols;               // [512][8] input, then exchange 2
+  float* sa = reinterpret_cast<float*>(x2 + (size_t)kN * kCols);   // [512][8] amplitudes
+  float* sb = sa + (size_t)kN * kCols;                    // [512][8] background (or DM state)
+  const int fl = blockIdx.x / kBlocksPerFrame, f = f0 + fl;
+  const int blk = blockIdx.x % kBlocksPerFrame;
+  const int cw = threadIdx.x % kCols, tc = threadIdx.x / kCols;
+  const int kc = blk * kCols + cw;
+  const size_t fbase = (size_t)f * kN * kN;
+  float2* scol = g.stage + (size_t)fl * kN * kN + kc;
+  constexpr bool BG_ST = MI::BG_IN || OP == OP_DM7;
+  const float* bsrc = nullptr;
+  if constexpr (MI::BG_IN) bsrc = g.bg_in ? g.bg_in + (size_t)g.bg_stride * f : nullptr;
+  if constexpr (OP == OP_DM7) bsrc = g.bg_out + fbase;
+  // 16-byte copies: a row segment of the CTA's 8 columns is 64 bytes of
+  // scratch (4 copies) and 32 bytes of amplitude or background (2 copies)
+  const int c0 = blk * kCols;
+  const float2* ssrc = g.stage + (size_t)fl * kN * kN + c0;
+#pragma unroll
+  for (int i = 0; i < (kN * kCols / 2) / kNT; ++i) {
+    const int q = threadIdx.x + kNT * i, r = q >> 2, p = q & 3;
+    cp_async16(&x2[r * kCols + 2 * p], ssrc + (size_t)r * kN + 2 * p);
+  }
+  if constexpr (MI::NEEDS) {
+    const float* asrc = g.amp + (size_t)g.amp_stride * f + c0;
+#pragma unroll
+    for (int i = 0; i < (kN * kCols / 4) / kNT; ++i) {
+      const int q = threadIdx.x + kNT * i, r = q >> 1, p = q & 1;
+      cp_async16(&sa[r * kCols + 4 * p], asrc + (size_t)r * kN + 4 * p);
+    }
+  }
+  if constexpr (BG_ST) {
+    if (bsrc) {
+#pragma unroll
+      for (int i = 0; i < (kN * kCols / 4) / kNT; ++i) {
+        const int q = threadIdx.x + kNT * i, r = q >> 1, p = q & 1;
+        cp_async16(&sb[r * kCols + 4 * p], bsrc + c0 + (size_t)r * kN + 4 * p);
+      }
+    }
+  }
+  // mask bytes of the 16 pixels, four per register (all ones without a mask)
+  unsigned mk4[kB / 4] = {0x01010101u, 0x01010101u, 0x01010101u, 0x01010101u};
+  if constexpr (MI::NEEDS) {
+    if (g.mask) {
+#pragma unroll
+      for (int q = 0; q < kB / 4; ++q) {
+        unsigned w = 0;
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+          w |= (unsigned)__ldg(&g.mask[(size_t)(tc + kA * (4 * q + i)) * kN + kc]) << (8 * i);
+        mk4[q] = w;
+      }
+    }
+  }
+  load_twiddles(g, tw1, tw2);
+  auto e1 = [x1, cw](int s) -> float2& { return x1[s * kCols + cw]; };
+  auto e2 = [x2, cw](int s) -> float2& { return x2[s * kCols + cw]; };
+  auto cta_sync = [] { __syncthreads(); };
+  cp_async_wait_all();
+  __syncthreads();
+  float2 v[kB];
+  // the transform's first barrier orders these reads before exchange 2
+  // overwrites x2
+#pragma unroll
+  for (int j = 0; j < kB; ++j) v[j] = x2[(tc + kA * j) * kCols + cw];
+  line3_fft512<T::FIRST_DIR, false>(v, tc, e1, e2, col_s1, any_s2, cta_sync, tw1, tw2);
+  ff err = ff_zero();
+  if constexpr (MI::NEEDS) {
+    MI m;
+#pragma unroll
+    for (int j = 0; j < kB; ++j) {
+      const int sl = (tc + kA * j) * kCols + cw;
+      m.am[j] = sa[sl];
+      m.mk[j] = (float)((mk4[j / 4] >> (8 * (j % 4))) & 0xffu);
+      if constexpr (BG_ST) m.bb[j] = bsrc ? sb[sl] : 0.0f;
+      if constexpr (OP == OP_DM7) m.b0v[j] = __ldg(&g.b0[(size_t)(tc + kA * j) * kN + kc]);
+    }
+    modulus_compute<OP, kB>(g, v, m, err);
+    if constexpr (MI::BG_OUT) {
+#pragma unroll
+      for (int j = 0; j < kB; ++j) g.bg_out[fbase + (size_t)(tc + kA * j) * kN + kc] = m.bb[j];
+    }
+  } else {
+    MI m;
+    modulus_apply<kN, kN, OP, kA, kB>(g, fbase, tc, kc, v, m, err);
+  }
+  if constexpr (T::INVERSE) {
+    line3_fft512<+1, false>(v, tc, e1, e2, col_s1, any_s2, cta_sync, tw1, tw2);
+#pragma unroll
+    for (int j = 0; j < kB; ++j) scol[(size_t)(tc + kA * j) * kN] = v[j];
+  }
+  if (g.err_part) {
+    const double sum = block_sum_d(ff_to_double(err), red);
+    if (threadIdx.x == 0) {
+      double* ep = g.err_part + (size_t)f * g.err_stride;
+      ep[blk] = sum;
+      if (blk == 0)
+        for (int k = kBlocksPerFrame; k < g.err_stride; ++k) ep[k] = 0.0;
+    }
+  }
+}
+
+template <int OP>
+int set_attr() {
+  cudaError_t e = cudaFuncSetAttribute(staged_cols_kernel<OP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)kColSmem);
+  if (e != cudaSuccess) return set_cuda_error(e, "staged_cols_kernel attributes");
+  return PTY_OK;
+}
+
+template <int OP>
+int launch(const FrameArgs& a, int nframes, cudaStream_t st) {
+  for (int f0 = 0; f0 < nframes; f0 += a.stage_frames) {
+    const int nf = nframes - f0 < a.stage_frames ? nframes - f0 : a.stage_frames;
+    const dim3 grid(nf * kBlocksPerFrame);
+    staged_rows_kernel<OP, false><<<grid, kNT, 0, st>>>(a, f0);
+    PTY_TRY(check_launch("staged_rows_kernel"));
+    staged_cols_kernel<OP><<<grid, kNT, kColSmem, st>>>(a, f0);
+    PTY_TRY(check_launch("staged_cols_kernel"));
+    if constexpr (OpTraits<OP>::INVERSE) {
+      staged_rows_kernel<OP, true><<<grid, kNT, 0, st>>>(a, f0);
+      PTY_TRY(check_launch("staged_rows_kernel"));
+    }
+  }
+  return PTY_OK;
+}
+
+}  // namespace
+
+int prepare_staged_512() {
+  int rc = PTY_OK;
+  if (!rc) rc = set_attr<OP_EXIT1>();
+  if (!rc) rc = set_attr<OP_EXIT7>();
+  if (!rc) rc = set_attr<OP_PSI1>();
+  if (!rc) rc = set_attr<OP_PSI7>();
+  if (!rc) rc = set_attr<OP_DM1>();
+  if (!rc) rc = set_attr<OP_DM7>();
+  if (!rc) rc = set_attr<OP_MERR>();
+  if (!rc) rc = set_attr<OP_INTENS>();
+  if (!rc) rc = set_attr<OP_MERR_PSI>();
+  if (!rc) rc = set_attr<OP_BP>();
+  return rc;
+}
+
+int launch_staged_512(int op, const FrameArgs& a, int nframes, cudaStream_t st) {
+  if (!a.twf) return set_error(PTY_ERR_ARG, "staged frame tile needs the full twiddle table");
+  if (!a.stage || a.stage_frames < 1) return set_error(PTY_ERR_ARG, "staged frame tile needs a frame scratch");
+  if (a.err_part && a.err_stride < kBlocksPerFrame)
+    return set_error(PTY_ERR_ARG, "staged frame tile needs 64 error slots per frame");
+  // the column launch copies amplitude and background rows in 16-byte pieces;
+  // arrays not 16-byte aligned go through the 16-CTA tile with the same line
+  // transforms instead (same waves and background, error partials grouped
+  // per 16 CTAs)
+  auto misaligned = [](const void* q) { return ((uintptr_t)q & 15u) != 0; };
+  if (misaligned(a.amp) || misaligned(a.bg_in) || misaligned(a.bg_out)) {
+    PTY_TRY(prepare_cluster_512x16l());
+    return launch_cluster_512x16l(op, a, nframes, st);
+  }
+  switch (op) {
+    case OP_EXIT1: return launch<OP_EXIT1>(a, nframes, st);
+    case OP_EXIT7: return launch<OP_EXIT7>(a, nframes, st);
+    case OP_PSI1: return launch<OP_PSI1>(a, nframes, st);
+    case OP_PSI7: return launch<OP_PSI7>(a, nframes, st);
+    case OP_DM1: return launch<OP_DM1>(a, nframes, st);
+    case OP_DM7: return launch<OP_DM7>(a, nframes, st);
+    case OP_MERR: return launch<OP_MERR>(a, nframes, st);
+    case OP_INTENS: return launch<OP_INTENS>(a, nframes, st);
+    case OP_MERR_PSI: return launch<OP_MERR_PSI>(a, nframes, st);
+    case OP_BP: return launch<OP_BP>(a, nframes, st);
+  }
+  return set_error(PTY_ERR_ARG, "unknown frame op");
+}
+
+}  // namespace pty

@@ -3,8 +3,9 @@
 128 x 128 frames have a single-CTA kernel and a 2-CTA cluster kernel, 256 x 256
 frames 8- and 4-CTA cluster kernels (16 x 16 line transforms) and an 8-CTA
 kernel with three-stage 8 x 8 x 4 line transforms (tile 108), 512 x 512
-frames a 16-CTA kernel with 16 x 32 line transforms (tile 16) and one with
-three-stage 16 x 8 x 4 transforms (tile 116).  Each tile,
+frames a 16-CTA kernel with 16 x 32 line transforms (tile 16), one with
+three-stage 16 x 8 x 4 transforms (tile 116) and the staged row / column / row
+launches with the same transforms (tile 264).  Each tile,
 forced in turn, must match the oracle.  Tiles running the same line transforms
 give bit-identical exit waves, object and probe (only the error sums, whose
 per-CTA partials are grouped differently, may differ in rounding); tiles with
@@ -26,7 +27,7 @@ pytestmark = pytest.mark.gpu
 
 
 # tiles sharing a line decomposition (bit-identical results), per frame size
-SAME_LINES = {128: [(1, 2)], 256: [(8, 4), (108,)], 512: [(16,), (116,)]}
+SAME_LINES = {128: [(1, 2)], 256: [(8, 4), (108,)], 512: [(16,), (116, 264)]}
 
 
 def same_lines(N, t0, t1):
@@ -58,7 +59,7 @@ class forced_tile:
 def test_tiles_listed_and_chosen(N):
     lib = _native.load()
     c = candidates(N)
-    assert len(c) == {128: 2, 256: 3, 512: 2}[N]
+    assert len(c) == {128: 2, 256: 3, 512: 3}[N]
     for fam in (0, 1):
         t = ctypes.c_int32(0)
         _native.check(lib.pty_get_frame_tile(N, N, fam, ctypes.byref(t)))
@@ -150,3 +151,33 @@ def test_era_m3_every_tile(N):
             # (each operator agrees with the FP64 oracle to 3e-6)
             assert rel(O_t, res[0][0]) < 5e-5 and rel(P_t, res[0][1]) < 5e-5
             np.testing.assert_allclose(info["eMod"], res[0][2]["eMod"], rtol=2e-5)
+
+
+def test_staged_tile_unaligned_amplitudes():
+    """Tile 264 copies amplitude rows in 16-byte pieces; an amplitude array
+    that is not 16-byte aligned runs through tile 116 (same line transforms):
+    the same exit waves and background bit for bit."""
+    N, n, U = 512, 3, 560
+    rng = np.random.default_rng(11)
+    R = np.stack([-rng.integers(0, U - N + 1, n), -rng.integers(0, U - N + 1, n)], 1)
+    ex = rng.standard_normal((n, N, N)) + 1j * rng.standard_normal((n, N, N))
+    amp = (np.abs(rng.standard_normal((n, N, N))) * 50).astype(np.float32)
+    bg = np.abs(rng.standard_normal((n, N, N))).astype(np.float32)
+    mask = rng.random((N, N)) > 0.05
+    outs = []
+    with forced_tile(N, 264):
+        plan = Plan(n, N, N, U, U, R)
+        try:
+            for off in (0, 1):      # amplitudes at a 16-byte boundary, then 4 bytes past one
+                psi = to_dev(ex, np.complex64)
+                b = to_dev(bg, np.float32)
+                buf = torch.zeros(n * N * N + 4, dtype=torch.float32, device=psi.device)
+                buf[off:off + n * N * N] = to_dev(amp.ravel())
+                amp_d = buf[off:off + n * N * N]
+                mask_d = to_dev(mask, np.uint8)
+                plan.call("pty_pmod_7", ptr(amp_d), ptr(b), ptr(psi), ptr(mask_d), 1e-10, None)
+                outs.append((psi.cpu().numpy(), b.cpu().numpy()))
+        finally:
+            plan.close()
+    np.testing.assert_array_equal(outs[0][0], outs[1][0])
+    np.testing.assert_array_equal(outs[0][1], outs[1][1])
