@@ -64,6 +64,7 @@ struct pty_plan {
   float2* d_mean_part = nullptr;
   double* d_err_part = nullptr;  // [n * eslots]
   float2* d_stage = nullptr;     // frame scratch of a staged tile
+  uint8_t* d_mask_blk = nullptr; // the mask in the staged tile's column-block order
   int stage_frames = 0;
   int tile[2] = {1, 1};          // CTAs per frame of the fused frame kernels, per op family
   int eslots = 1;                // error-partial slots per frame (the larger family tile)
@@ -216,6 +217,7 @@ extern "C" int pty_plan_create(const pty_geometry* g, const int64_t* R_host, pty
   if (tile_staged(p->tile[0]) || tile_staged(p->tile[1])) {
     p->stage_frames = staged_group_frames(N0, N1) < n ? staged_group_frames(N0, N1) : n;
     if ((rc = dalloc_t(p, &p->d_stage, (size_t)p->stage_frames * npix))) return fail(rc);
+    if ((rc = dalloc_t(p, &p->d_mask_blk, npix))) return fail(rc);
   }
   if ((rc = dalloc_t(p, &p->d_dn_part, (size_t)4 * p->ndn))) return fail(rc);
   if ((rc = dalloc_t(p, &p->d_shift, 2))) return fail(rc);
@@ -267,6 +269,7 @@ static FrameArgs base_args(const pty_plan* p) {
   a.err_stride = p->eslots;
   a.stage = p->d_stage;
   a.stage_frames = p->stage_frames;
+  a.mask_blk = p->d_mask_blk;
   return a;
 }
 

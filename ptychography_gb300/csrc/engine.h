@@ -45,6 +45,7 @@ struct FrameArgs {
   const float2* twf;         // W_N1^e, e < N1 (three-stage line transforms)
   float2* stage;             // [stage_frames][N0][N1] frame scratch of the staged tiles
   int stage_frames;          // frames the scratch holds (launches run in groups of it)
+  uint8_t* mask_blk;         // [N0 * N1] mask in column-block order (staged tiles)
 };
 
 // Frame tiles: how many CTAs transform one frame.  Tile 1 is the single-CTA

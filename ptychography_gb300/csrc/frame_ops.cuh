@@ -42,7 +42,7 @@ PTY_DEV float2 frame_input(const FrameArgs& g, int f, int r0, int r1, const floa
     // holding the unit phasors of fftn(P) in natural order
     const int pa = (a + g.N0h) % (2 * g.N0h), pb = (b + g.N1h) % (2 * g.N1h);
     const int pix = pa * N1 + pb;
-    const float m = g.mask ? (float)g.mask[pix] : 1.0f;
+    const float m = g.mask ? byte_to_float(g.mask[pix]) : 1.0f;
     return cscale(__ldg(&g.P[a * N1 + b]), m * g.amp[(size_t)g.amp_stride * f + pix]);
   } else {
     return psi[a * N1 + b];
@@ -74,7 +74,7 @@ PTY_DEV void modulus_load(const FrameArgs& g, int f, size_t fbase, int t, int kc
     for (int j = 0; j < B; ++j) {
       const int pix = (t + A * j) * N1 + kc;
       m.am[j] = __ldg(&amp[pix]);
-      m.mk[j] = g.mask ? (float)__ldg(&g.mask[pix]) : 1.0f;
+      m.mk[j] = g.mask ? byte_to_float(__ldg(&g.mask[pix])) : 1.0f;
       if constexpr (ModIn<OP, B>::BG_IN) m.bb[j] = g.bg_in ? g.bg_in[(size_t)g.bg_stride * f + pix] : 0.0f;
     }
   }
@@ -124,51 +124,58 @@ PTY_DEV void modulus_apply(const FrameArgs& g, size_t fbase, int t, int kc, floa
   }
 }
 
-// The constraint itself (EXIT / PSI / DM / MERR forms): updates v and, for the
+// The constraint on one pixel (EXIT / PSI / DM / MERR forms): F at the
+// pixel's frequency, its amplitude am and mask value mk; bb is the pixel's
+// background (updated in place by the background forms), b0 the DM mean
+// background.  Returns the new F and adds the pixel's error term to line_err.
+template <int OP>
+PTY_DEV float2 modulus_pixel(const FrameArgs& g, float2 F, float am, float mk, float& bb,
+                             const float& b0, float& line_err) {
+  // square roots and quotients use the hardware reciprocal square root
+  // (a few ulp; the engine's tolerances are 1e-5 relative)
+  if constexpr (OP == OP_EXIT1 || OP == OP_PSI1 || OP == OP_DM1) {
+    // era.py:561-571: |F| + alpha, masked pixels keep F
+    const float x2 = cabs2(F);
+    const float mag = (x2 > 0.f ? x2 * rsqrtf(x2) : 0.f) + g.alpha;
+    const float d = mag - am;
+    line_err += d * d * mk;
+    const float fac = (mk != 0.f) ? __fdividef(am, mag) : 1.0f;
+    return cscale(F, fac);
+  } else if constexpr (OP == OP_EXIT7 || OP == OP_PSI7) {
+    // era.py:584-594: sqrt(|F|^2 + b^2 + alpha), masked pixels zeroed
+    const float x2 = cabs2(F) + bb * bb + g.alpha;
+    const float rs = rsqrtf(x2);
+    const float d = x2 * rs - am;
+    line_err += d * d * mk;
+    const float fac = mk * am * rs;
+    bb *= fac;
+    return cscale(F, fac);
+  } else if constexpr (OP == OP_DM7) {
+    // dm.py:219-224 on the background: g1 = g - b0 ; tb = b0 - g1 ; g = g1 + Pmod7(tb)
+    const float g1 = bb - b0;
+    const float tb = b0 - g1;
+    const float fac = mk * am * rsqrtf(cabs2(F) + tb * tb + g.alpha);
+    bb = g1 + tb * fac;
+    return cscale(F, fac);
+  } else if constexpr (OP == OP_MERR || OP == OP_MERR_PSI) {
+    // dm.py:338-340, no alpha
+    const float x2 = cabs2(F) + bb * bb;
+    const float d = (x2 > 0.f ? x2 * rsqrtf(x2) : 0.f) - am;
+    line_err += mk * (d * d);
+    return F;
+  } else {
+    return F;
+  }
+}
+
+// The constraint on a line held in registers: updates v and, for the
 // background forms, m.bb; adds the line's error terms to err.
 template <int OP, int B>
 PTY_DEV void modulus_compute(const FrameArgs& g, float2 (&v)[B], ModIn<OP, B>& m, ff& err) {
-  {
-    float line_err = 0.f;   // FP32 over one line (B terms), folded into err once
+  float line_err = 0.f;   // FP32 over one line (B terms), folded into err once
 #pragma unroll
-    for (int j = 0; j < B; ++j) {
-      const float2 F = v[j];
-      const float am = m.am[j], mk = m.mk[j];
-      // square roots and quotients use the hardware reciprocal square root
-      // (a few ulp; the engine's tolerances are 1e-5 relative)
-      if constexpr (OP == OP_EXIT1 || OP == OP_PSI1 || OP == OP_DM1) {
-        // era.py:561-571: |F| + alpha, masked pixels keep F
-        const float x2 = cabs2(F);
-        const float mag = (x2 > 0.f ? x2 * rsqrtf(x2) : 0.f) + g.alpha;
-        const float d = mag - am;
-        line_err += d * d * mk;
-        const float fac = (mk != 0.f) ? __fdividef(am, mag) : 1.0f;
-        v[j] = cscale(F, fac);
-      } else if constexpr (OP == OP_EXIT7 || OP == OP_PSI7) {
-        // era.py:584-594: sqrt(|F|^2 + b^2 + alpha), masked pixels zeroed
-        const float x2 = cabs2(F) + m.bb[j] * m.bb[j] + g.alpha;
-        const float rs = rsqrtf(x2);
-        const float d = x2 * rs - am;
-        line_err += d * d * mk;
-        const float fac = mk * am * rs;
-        v[j] = cscale(F, fac);
-        m.bb[j] *= fac;
-      } else if constexpr (OP == OP_DM7) {
-        // dm.py:219-224 on the background: g1 = g - b0 ; tb = b0 - g1 ; g = g1 + Pmod7(tb)
-        const float g1 = m.bb[j] - m.b0v[j];
-        const float tb = m.b0v[j] - g1;
-        const float fac = mk * am * rsqrtf(cabs2(F) + tb * tb + g.alpha);
-        v[j] = cscale(F, fac);
-        m.bb[j] = g1 + tb * fac;
-      } else if constexpr (OP == OP_MERR || OP == OP_MERR_PSI) {
-        // dm.py:338-340, no alpha
-        const float x2 = cabs2(F) + m.bb[j] * m.bb[j];
-        const float d = (x2 > 0.f ? x2 * rsqrtf(x2) : 0.f) - am;
-        line_err += mk * (d * d);
-      }
-    }
-    err = ff_add(err, line_err);
-  }
+  for (int j = 0; j < B; ++j) v[j] = modulus_pixel<OP>(g, v[j], m.am[j], m.mk[j], m.bb[j], m.b0v[j], line_err);
+  err = ff_add(err, line_err);
 }
 
 template <int N0, int N1, int OP, int A, int B>

@@ -59,6 +59,12 @@ PTY_DEV ff ff_add(ff a, ff b) {
 }
 PTY_DEV double ff_to_double(ff a) { return (double)a.hi + (double)a.lo; }
 
+// A byte as a float without an int-to-float conversion instruction (those
+// issue through the shared MIO path, where the frame kernels' exchanges
+// already queue): the byte placed in the low mantissa bits of 2^23 gives the
+// float 2^23 + b exactly, and subtracting 2^23 leaves b (exact for b < 2^23).
+PTY_DEV float byte_to_float(unsigned b) { return __int_as_float(0x4B000000u | b) - 8388608.0f; }
+
 // ---------------------------------------------------------------- reductions
 PTY_DEV double warp_sum_d(double v) {
 #pragma unroll

@@ -37,7 +37,8 @@ constexpr int kCols = kNT / kA;             // columns per column CTA
 constexpr int kBlocksPerFrame = kN / kRows; // = kN / kCols = 64
 constexpr int kRowScr = 542;                // row-exchange slots per warp
 constexpr int kColE1 = 527;                 // column exchange-1 slots (33 k1 + t)
-constexpr size_t kColSmem = (size_t)(kColE1 + kN) * kCols * sizeof(float2) + (size_t)2 * kN * kCols * sizeof(float);
+constexpr size_t kColSmem = (size_t)(kColE1 + kN) * kCols * sizeof(float2) +
+                            (size_t)2 * kN * kCols * sizeof(float) + (size_t)kN * kCols;
 static_assert(kRows == kCols && kBlocksPerFrame == 64, "64 blocks per frame per launch");
 
 // Row slot layouts (a warp is one line; each half-warp touches 16 distinct
@@ -103,12 +104,23 @@ PTY_DEV void cp_async16(void* smem, const void* gmem) {
 }
 PTY_DEV void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 
+// The mask in column-block order for the column launch:
+// blk[b][r][c] = mask[r][8 b + c] (64 blocks of 512 rows x 8 columns).
+__global__ void __launch_bounds__(kNT) mask_blocks_kernel(const uint8_t* __restrict__ mask,
+                                                          uint8_t* __restrict__ blk) {
+  const int b = blockIdx.x;
+  for (int i = threadIdx.x; i < kN * kCols; i += kNT) {
+    const int r = i / kCols, c = i % kCols;
+    blk[(size_t)b * kN * kCols + i] = mask[(size_t)r * kN + kCols * b + c];
+  }
+}
+
 // Column launch: 8 columns of one frame per CTA, thread (cw, tc) = line
 // thread tc of column c0 + cw.  Every global input of the CTA -- its scratch
 // columns, amplitudes and background -- is copied into shared memory by
-// cp.async at the start, so the CTA waits for HBM once and holds no
-// registers for loads in flight; the mask bytes (shared by all frames,
-// L2-resident) are read alongside, four to a register.
+// cp.async at the start, with its block of the mask (shared by all frames,
+// L2-resident), so the CTA waits for memory once and holds no registers for
+// loads in flight.
 template <int OP>
 __global__ void __launch_bounds__(kNT, 2) staged_cols_kernel(FrameArgs g, int f0) {
   using T = OpTraits<OP>;
@@ -121,6 +133,7 @@ __global__ void __launch_bounds__(kNT, 2) staged_cols_kernel(FrameArgs g, int f0
   float2* x2 = x1 + (size_t)kColE1 * kCols;               // [512][8] input, then exchange 2
   float* sa = reinterpret_cast<float*>(x2 + (size_t)kN * kCols);   // [512][8] amplitudes
   float* sb = sa + (size_t)kN * kCols;                    // [512][8] background (or DM state)
+  uint8_t* sm = reinterpret_cast<uint8_t*>(sb + (size_t)kN * kCols);   // [512][8] mask
   const int fl = blockIdx.x / kBlocksPerFrame, f = f0 + fl;
   const int blk = blockIdx.x % kBlocksPerFrame;
   const int cw = threadIdx.x % kCols, tc = threadIdx.x / kCols;
@@ -157,19 +170,10 @@ __global__ void __launch_bounds__(kNT, 2) staged_cols_kernel(FrameArgs g, int f0
       }
     }
   }
-  // mask bytes of the 16 pixels, four per register (all ones without a mask)
-  unsigned mk4[kB / 4] = {0x01010101u, 0x01010101u, 0x01010101u, 0x01010101u};
   if constexpr (MI::NEEDS) {
-    if (g.mask) {
-#pragma unroll
-      for (int q = 0; q < kB / 4; ++q) {
-        unsigned w = 0;
-#pragma unroll
-        for (int i = 0; i < 4; ++i)
-          w |= (unsigned)__ldg(&g.mask[(size_t)(tc + kA * (4 * q + i)) * kN + kc]) << (8 * i);
-        mk4[q] = w;
-      }
-    }
+    // the mask's column-block copy: this CTA's 512 rows x 8 columns are 4 KB
+    // in one piece (the natural layout would take 512 separate 8-byte reads)
+    if (g.mask) cp_async16(&sm[16 * threadIdx.x], g.mask_blk + (size_t)blk * kN * kCols + 16 * threadIdx.x);
   }
   load_twiddles(g, tw1, tw2);
   auto e1 = [x1, cw](int s) -> float2& { return x1[s * kCols + cw]; };
@@ -188,11 +192,11 @@ __global__ void __launch_bounds__(kNT, 2) staged_cols_kernel(FrameArgs g, int f0
     MI m;
 #pragma unroll
     for (int j = 0; j < kB; ++j) {
-      const int sl = (tc + kA * j) * kCols + cw;
+      const int r = tc + kA * j, sl = r * kCols + cw;
       m.am[j] = sa[sl];
-      m.mk[j] = (float)((mk4[j / 4] >> (8 * (j % 4))) & 0xffu);
+      m.mk[j] = g.mask ? byte_to_float(sm[sl]) : 1.0f;
       if constexpr (BG_ST) m.bb[j] = bsrc ? sb[sl] : 0.0f;
-      if constexpr (OP == OP_DM7) m.b0v[j] = __ldg(&g.b0[(size_t)(tc + kA * j) * kN + kc]);
+      if constexpr (OP == OP_DM7) m.b0v[j] = __ldg(&g.b0[(size_t)r * kN + kc]);
     }
     modulus_compute<OP, kB>(g, v, m, err);
     if constexpr (MI::BG_OUT) {
@@ -229,6 +233,10 @@ int set_attr() {
 
 template <int OP>
 int launch(const FrameArgs& a, int nframes, cudaStream_t st) {
+  if (a.mask) {
+    mask_blocks_kernel<<<kBlocksPerFrame, kNT, 0, st>>>(a.mask, a.mask_blk);
+    PTY_TRY(check_launch("mask_blocks_kernel"));
+  }
   for (int f0 = 0; f0 < nframes; f0 += a.stage_frames) {
     const int nf = nframes - f0 < a.stage_frames ? nframes - f0 : a.stage_frames;
     const dim3 grid(nf * kBlocksPerFrame);
@@ -263,15 +271,16 @@ int prepare_staged_512() {
 
 int launch_staged_512(int op, const FrameArgs& a, int nframes, cudaStream_t st) {
   if (!a.twf) return set_error(PTY_ERR_ARG, "staged frame tile needs the full twiddle table");
-  if (!a.stage || a.stage_frames < 1) return set_error(PTY_ERR_ARG, "staged frame tile needs a frame scratch");
+  if (!a.stage || a.stage_frames < 1 || (a.mask && !a.mask_blk))
+    return set_error(PTY_ERR_ARG, "staged frame tile needs its frame and mask scratch");
   if (a.err_part && a.err_stride < kBlocksPerFrame)
     return set_error(PTY_ERR_ARG, "staged frame tile needs 64 error slots per frame");
-  // the column launch copies amplitude and background rows in 16-byte pieces;
-  // arrays not 16-byte aligned go through the 16-CTA tile with the same line
-  // transforms instead (same waves and background, error partials grouped
-  // per 16 CTAs)
-  auto misaligned = [](const void* q) { return ((uintptr_t)q & 15u) != 0; };
-  if (misaligned(a.amp) || misaligned(a.bg_in) || misaligned(a.bg_out)) {
+  // the column launch copies amplitude and background rows in 16-byte
+  // pieces; arrays not 16-byte aligned go through the 16-CTA tile with the
+  // same line transforms instead (same waves and background, error partials
+  // grouped per 16 CTAs)
+  auto misaligned = [](const void* q, uintptr_t m) { return ((uintptr_t)q & m) != 0; };
+  if (misaligned(a.amp, 15) || misaligned(a.bg_in, 15) || misaligned(a.bg_out, 15)) {
     PTY_TRY(prepare_cluster_512x16l());
     return launch_cluster_512x16l(op, a, nframes, st);
   }
