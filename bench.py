@@ -123,7 +123,7 @@ class DeviceWorkload:
     is initialised from the known blob (DM method 6 with a given background).
     """
 
-    def __init__(self, dev):
+    def __init__(self, dev, frames=None):
         import torch
         from ptychography_gb300 import _native
         rng = np.random.default_rng(4)
@@ -133,6 +133,8 @@ class DeviceWorkload:
         self.P_true = make_probe(N, 128, 16, 0.0001)
         self.P0 = make_probe(N, 128, 16, 0.00012)
         self.R = raster(rng, side, 36, 4, N, U)
+        if frames:      # the first frames of the scan (profiling a smaller case)
+            self.R = self.R[:frames]
         lib = _native.load()
         n = len(self.R)
         plan = ctypes.c_void_p()
@@ -507,9 +509,14 @@ def roofline_pmod7(job, torch, tile, sm_max_mhz, reps=20):
     t = event_time(torch, fn, reps) / reps
     bytes_ = 28.0 * job.N * job.N * job.n
     # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one ncu
-    # capture of this kernel (256^2 frames, 8-CTA tile): 880.7 MB for 512
-    # frames, scaled by frames; recorded for that kernel only
-    traffic = round(880.7e6 * job.n / 512) if (job.N == 256 and tile == 8) else None
+    # capture, scaled by frames, for the two tiles the benchmark workloads run
+    # on: the 256^2 8-CTA tile (880.7 MB for 512 frames) and the staged 512^2
+    # tile's three launches (3864.6 MB for 256 frames)
+    traffic = None
+    if job.N == 256 and tile == 8:
+        traffic = round(880.7e6 * job.n / 512)
+    elif job.N == 512 and tile == 264:
+        traffic = round(3864.6e6 * job.n / 256)
     if tile > 200:      # staged: row, column and row launches through a frame scratch
         kname = "staged_rows_kernel<PSI7> + staged_cols_kernel<PSI7> + staged_rows_kernel<PSI7>"
     elif tile > 100:    # three-stage line transforms
@@ -729,7 +736,15 @@ def run_reference(args):
     return 0
 
 
-def workload_config(name):
+def workload_config(name, frames=None):
+    cfg = _workload_config(name)
+    if frames and name in ("c1", "c4"):     # a profiling case: the first frames of the scan
+        cfg = dict(cfg, n_frames=min(frames, cfg["n_frames"]),
+                   workload="first %d frames of: %s" % (min(frames, cfg["n_frames"]), cfg["workload"]))
+    return cfg
+
+
+def _workload_config(name):
     if name == "c1":
         return {"workload": "ERA m6 then DM m6 (object+probe+background), 1024 frames 256x256, "
                             "object 1024x1024, Poisson 1e6, beamstop+dead-pixel mask",
@@ -760,8 +775,10 @@ def main():
     ap.add_argument("--no-nmse", action="store_true")
     ap.add_argument("--no-batch", action="store_true",
                     help="skip the 64-reconstruction batched measurement")
+    ap.add_argument("--frame-tile", type=int, default=0,
+                    help="force this frame tile (CTAs per frame; see pty_set_frame_tile) for profiling")
     ap.add_argument("--frames", type=int, default=None,
-                    help="use only the first F frames of the c1 raster (profiling captures)")
+                    help="use only the first F frames of the c1 or c4 raster (profiling captures)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -779,9 +796,12 @@ def main():
     if args.workload == "c1":
         w = workload_c1(gpu_intensities, frames=np.arange(args.frames) if args.frames else None)
     elif args.workload == "c4":
-        w = DeviceWorkload(dev)
+        w = DeviceWorkload(dev, frames=args.frames)
     else:
         w = workload_c0(gpu_intensities)
+    if args.frame_tile:     # profiling one tile: forced for both op families
+        for fam in (0, 1):
+            _native.check(lib.pty_set_frame_tile(w.N, w.N, fam, args.frame_tile))
     job = DeviceJob(w, dev)
     for _ in range(args.warmup):
         job.step()
@@ -833,7 +853,8 @@ def main():
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": round(1e3 * t / args.steps, 4), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": dict(workload_config(args.workload), parallelism="replicas" if world > 1 else "1 GPU",
+        "config": dict(workload_config(args.workload, args.frames),
+                       parallelism="replicas" if world > 1 else "1 GPU",
                        frame_tile_ctas={"plain": tiles[0], "background": tiles[1]}),
         "gpu_launches": int(launches), "clocks": clk.summary(), "roofline": roof,
         "cpu_baseline": cpu, "e2e": e2e,

@@ -10,9 +10,11 @@
 //   256^2: 8-CTA clusters of 256 threads (two CTAs per SM), 4-CTA clusters
 //          of 512 (one per SM), or (tile id 108) 8-CTA clusters of 512 threads
 //          with three-stage line transforms (two CTAs, 32 warps per SM)
-//   512^2: 16-CTA clusters of 256 threads (32 values per thread), or (tile
-//          id 116) of 512 threads with three-stage line transforms (16 values
-//          per thread, 16 warps per SM); one CTA per SM either way
+//   512^2: (tile id 264, the default) the staged row / column / row launches
+//          through a frame scratch (staged_512.cu), or 16-CTA clusters of 512
+//          threads with three-stage line transforms (tile 116, 16 values per
+//          thread, 16 warps per SM) or of 256 threads (tile 16, 32 values per
+//          thread); one cluster CTA per SM
 //
 // Tiles are chosen per op family: the background (Pmod_7) forms move more
 // bytes and hold more registers than the plain ones, and the fastest tile
@@ -53,7 +55,7 @@ struct ShapeTiles {
 constexpr ShapeTiles kShapes[] = {
     {32, 32, 1, {1, 0, 0, 0}},   {64, 64, 1, {1, 0, 0, 0}},   {32, 64, 1, {1, 0, 0, 0}},
     {128, 128, 2, {1, 2, 0, 0}}, {192, 192, 1, {2, 0, 0, 0}}, {256, 256, 3, {8, 4, 108, 0}},
-    {512, 512, 3, {16, 116, 264, 0}},
+    {512, 512, 3, {264, 116, 16, 0}},
 };
 
 const ShapeTiles* find_shape(int N0, int N1) {

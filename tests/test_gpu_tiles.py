@@ -3,9 +3,9 @@
 128 x 128 frames have a single-CTA kernel and a 2-CTA cluster kernel, 256 x 256
 frames 8- and 4-CTA cluster kernels (16 x 16 line transforms) and an 8-CTA
 kernel with three-stage 8 x 8 x 4 line transforms (tile 108), 512 x 512
-frames a 16-CTA kernel with 16 x 32 line transforms (tile 16), one with
-three-stage 16 x 8 x 4 transforms (tile 116) and the staged row / column / row
-launches with the same transforms (tile 264).  Each tile,
+frames the staged row / column / row launches with three-stage 16 x 8 x 4
+line transforms (tile 264), a 16-CTA kernel with the same transforms (tile
+116) and one with 16 x 32 line transforms (tile 16).  Each tile,
 forced in turn, must match the oracle.  Tiles running the same line transforms
 give bit-identical exit waves, object and probe (only the error sums, whose
 per-CTA partials are grouped differently, may differ in rounding); tiles with
