@@ -179,6 +179,14 @@ int pty_legacy_random_background(const uint32_t* key, int32_t pos, int64_t count
                                  uint32_t* key_out, int32_t* pos_out, void* stream);
 /* Scratch words pty_legacy_random_background needs (-1 for invalid input). */
 int64_t pty_legacy_random_scratch_words(int32_t pos, int64_t count);
+/* Host-side jump-ahead of the same generator (no reference counterpart; it
+ * checks the jump-ahead that lets the device draw run in parallel segments):
+ * window_out[624] = the 624 raw (untempered) words at offset `words` of the
+ * sequence whose first 624 words are key (a state as np.random.get_state()
+ * returns it right after a twist), from x^words mod phi, phi the generator's
+ * characteristic polynomial.  The low 31 bits of window_out[0] are not the
+ * sequence's (the generator never reads them). */
+int pty_legacy_random_jump(const uint32_t* key, int64_t words, uint32_t* window_out);
 
 /* 1 if the frame shape N0 x N1 has a fused FFT kernel. */
 int pty_shape_supported(int32_t N0, int32_t N1);

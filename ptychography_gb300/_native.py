@@ -62,6 +62,8 @@ SIGNATURES = {
                                      c_int32, c_void_p, c_void_p, ctypes.POINTER(ctypes.c_uint32),
                                      ctypes.POINTER(c_int32), c_void_p],
     "pty_legacy_random_scratch_words": [c_int32, ctypes.c_int64],
+    "pty_legacy_random_jump": [ctypes.POINTER(ctypes.c_uint32), ctypes.c_int64,
+                               ctypes.POINTER(ctypes.c_uint32)],
     "pty_shape_supported": [c_int32, c_int32],
     "pty_frame_tile_candidates": [c_int32, c_int32, ctypes.POINTER(c_int32), c_int32,
                                   ctypes.POINTER(c_int32)],

@@ -1,8 +1,9 @@
 """The random initial background drawn on the device (pty_legacy_random_background)
 equals NumPy's host draw bit for bit and leaves NumPy's global generator in the
-same state.  (ERA / DM runs of methods 4 and 6 from a random background, which
-now draw it on the device, are compared with the reference's own recorded runs
-in test_gpu_runs.)"""
+same state.  Draws above 2^17 words run as parallel segments started by the
+jump-ahead (37 x 128^2: 10 segments, 33 x 256^2: 33, 2 x 512^2: 8).  (ERA /
+DM runs of methods 4 and 6 from a random background, which now draw it on the
+device, are compared with the reference's own recorded runs in test_gpu_runs.)"""
 import numpy as np
 import pytest
 import torch
@@ -15,7 +16,8 @@ pytestmark = pytest.mark.gpu
 
 @pytest.mark.parametrize("rdt", [np.float32, np.float64])
 @pytest.mark.parametrize("seed,skip,shape", [(0, 0, (3, 32, 32)), (5, 7, (4, 64, 64)),
-                                             (9, 311, (1, 16, 16)), (2, 623, (37, 128, 128))])
+                                             (9, 311, (1, 16, 16)), (2, 623, (37, 128, 128)),
+                                             (17, 100, (33, 256, 256)), (4, 0, (2, 512, 512))])
 def test_device_background_matches_host(rdt, seed, skip, shape):
     lib = _native.load()
     np.random.seed(seed)

@@ -64,3 +64,25 @@ def test_float32_path_matches_astype():
     v = np.round(u * 2.0 ** 53).astype(np.uint64)             # the 53-bit integer
     f = v.astype(np.float32) * np.float32(2.0 ** -53)
     np.testing.assert_array_equal(f + np.float32(0.1), ref)
+
+
+@pytest.mark.parametrize("seed,blocks", [(3, 1), (8, 5), (21, 210), (40, 1025)])
+def test_jump_ahead_matches_numpy(seed, blocks):
+    """The library's jump-ahead (x^J mod phi applied to a window, the same
+    polynomials the device draw uses to start its segments) lands on NumPy's
+    own state after J = 624 * blocks raw words."""
+    import ctypes
+    from ptychography_gb300 import _native
+    lib = _native.load()
+    np.random.seed(seed)
+    key0 = np.ascontiguousarray(np.random.get_state()[1], dtype=np.uint32)
+    np.random.random(312 * blocks)                 # 624 * blocks words, whole blocks
+    st = np.random.get_state()
+    assert st[2] == 624
+    want = np.asarray(st[1], dtype=np.uint32)
+    got = np.empty(624, dtype=np.uint32)
+    u32p = ctypes.POINTER(ctypes.c_uint32)
+    _native.check(lib.pty_legacy_random_jump(key0.ctypes.data_as(u32p), 624 * blocks,
+                                             got.ctypes.data_as(u32p)))
+    np.testing.assert_array_equal(got[1:], want[1:])
+    assert got[0] >> 31 == want[0] >> 31            # only its top bit is state
