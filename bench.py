@@ -602,20 +602,28 @@ def time_to_nmse(torch, dev, target=1e-3, max_iters=2000, check_every=5):
 
 
 def e2e_public_api(w, K):
-    """The public API on host arrays: ERA (K iterations) then DM (K iterations)."""
+    """The public API on host arrays: ERA (K iterations) then DM (K iterations),
+    after one untimed pair of 1-iteration calls (the process's first public
+    calls load kernels and set up the generator's jump tables and the
+    page-locked output pool, once)."""
     import torch
     import ptychography_gb300 as pty
+
+    def api_calls(k):
+        if w.method == 6:
+            O, P, info = pty.ERA(w.I, w.R.copy(), w.P0, None, k, mask=w.M, method=6)
+            O, P, info2 = pty.DM(w.I, w.R.copy(), P, O, k, mask=w.M, method=6,
+                                 background=info["background"])
+            return (O, P, info2["eMod"][-1])
+        O, info = pty.ERA(w.I, w.R.copy(), w.P0, None, k, mask=w.M, method=w.method)
+        return (O, info["eMod"][-1])
+
+    np.random.seed(13)
+    api_calls(1)
     torch.cuda.synchronize()
     np.random.seed(13)
     t0 = time.perf_counter()
-    if w.method == 6:
-        O, P, info = pty.ERA(w.I, w.R.copy(), w.P0, None, K, mask=w.M, method=6)
-        O, P, info2 = pty.DM(w.I, w.R.copy(), P, O, K, mask=w.M, method=6,
-                             background=info["background"])
-        res = (O, P, info2["eMod"][-1])
-    else:
-        O, info = pty.ERA(w.I, w.R.copy(), w.P0, None, K, mask=w.M, method=w.method)
-        res = (O, info["eMod"][-1])
+    res = api_calls(K)
     torch.cuda.synchronize()
     dt = time.perf_counter() - t0
     n, N = w.I.shape[0], w.I.shape[1]
@@ -631,7 +639,8 @@ def e2e_public_api(w, K):
     frames = n * K * calls
     return {"value": round(frames / dt, 1), "unit": "frame-iters/s",
             "h2d_bytes_per_step": int(h2d / K), "d2h_bytes_per_step": int(d2h / K),
-            "wall_s": round(dt, 3), "final_eMod": float(res[-1])}
+            "wall_s": round(dt, 3), "final_eMod": float(res[-1]),
+            "warmup": "one untimed ERA + DM pair of 1 iteration each"}
 
 
 # --------------------------------------------------------------------------- CPU oracle

@@ -225,6 +225,16 @@ class _Job:
             self.close()
             raise
         self.heat_valid = 0
+        self.inten_host = None
+
+    def stage_outputs(self):
+        """Page-locked host memory for the model intensities (info['I'], n x N0 x
+        N1 float32), allocated while the GPU runs the loop: a fresh host array
+        of that size spends most of its download in page faults, which this
+        moves off the critical path (a 268 MB download: ~15 ms -> ~2 ms)."""
+        if self.inten is not None and self.pre.rdt == np.float32:
+            torch = _torch()
+            self.inten_host = torch.empty(tuple(self.inten.shape), dtype=torch.float32, pin_memory=True)
 
     def outputs(self):
         """The reference's return value (era.py:300-332 / dm.py:300-333)."""
@@ -237,7 +247,7 @@ class _Job:
             return O_out if upd == "O" else P_out if upd == "P" else (O_out, P_out)
         rt = pre.rdt
         info = {
-            "I": self.inten.cpu().numpy().astype(rt, copy=False) if self.inten is not None else None,
+            "I": self._intensities(rt),
             "eMod": [rt(x) for x in self.emod.cpu().numpy()[:iters]],
             "eCon": [rt(x) for x in self.econ.cpu().numpy()[:iters]],
             "heatmap": (self.heat.cpu().numpy().astype(rt)
@@ -253,6 +263,14 @@ class _Job:
         if upd == "P":
             return P_out, info
         return O_out, P_out, info
+
+    def _intensities(self, rt):
+        if self.inten is None:
+            return None
+        if self.inten_host is not None:
+            self.inten_host.copy_(self.inten)
+            return self.inten_host.numpy()
+        return self.inten.cpu().numpy().astype(rt, copy=False)
 
     def close(self):
         if self.plan:
@@ -275,6 +293,7 @@ def run(kind, I, R, P, O, iters, OP_iters, mask, background, method, Pmod_probe,
         fn = lib.pty_era if kind == "era" else lib.pty_dm
         _native.check(fn(job.plan, ctypes.byref(job.buf), ctypes.byref(job.opt), job.iters,
                          ctypes.byref(hv), sp))
+        job.stage_outputs()            # host work overlapping the GPU loop
         stream.synchronize()
         job.heat_valid = hv.value
         return job.outputs()
@@ -327,6 +346,8 @@ def run_batch(kind, problems, iters, defaults):
         hv = (ctypes.c_int32 * nrec)()
         _native.check(lib.pty_run_batch(0 if kind == "era" else 1, plans, bufs, opts, nrec,
                                         int(iters), hv, sp))
+        for j in jobs:
+            j.stage_outputs()
         stream.synchronize()
         out = []
         for j, h in zip(jobs, hv):
