@@ -188,6 +188,60 @@ int64_t pty_legacy_random_scratch_words(int32_t pos, int64_t count);
  * sequence's (the generator never reads them). */
 int pty_legacy_random_jump(const uint32_t* key, int64_t words, uint32_t* window_out);
 
+/* ---- Learned warm start (no reference counterpart: the reference starts
+ * ERA from an object of ones, era.py:480-486).  The network that maps sqrt(I)
+ * frames to exit-wave phases (ptychography_gb300/warmstart.py) runs on these
+ * device-memory building blocks; activations NHWC, "bf16" = bfloat16 arrays,
+ * everything stream-ordered on `stream`, no host synchronisation.
+ *   pty_ws_gemm: C(m, n) = sum_k A(m, k) B(k, n), A, B bf16 with element
+ *     strides (A(m, k) = A[m sam + k sak], B(k, n) = B[k sbk + n sbn]), C float
+ *     (C[m scm + n scn]); BF16 tensor-core products, FP32 accumulation.
+ *     splits > 1 splits K (deterministic: partial[splits][M][N] summed in
+ *     order) and needs C contiguous (scm = N, scn = 1).
+ *   pty_ws_im2col: col[p][(ky*3 + kx) C + c] = X[b][y+ky-1][x+kx-1][c] (3 x 3,
+ *     zero padding; X and col bf16); pty_ws_col2im: its adjoint (float).
+ *   pty_ws_pool2 / pty_ws_up2: 2 x 2 average pooling / nearest 2 x
+ *     upsampling (bf16), and their adjoints _bwd (float).
+ *   pty_ws_bias_act: a = act(Z + bias) (relu if relu), out = a + skip (skip
+ *     optional); a, out bf16 (optional), a32 float (optional).
+ *   pty_ws_act_bwd: dZ = dA (relu: where a > 0), bf16; dbias[c] = sum_p dZ;
+ *     scratch of pty_ws_act_bwd_scratch(P, C) floats.
+ *   pty_ws_loss: weighted squared error of Y[P][2] against T[P][2], weights
+ *     w[P] summing to 1: dY = 2 w (Y - T); loss_parts[256] partial sums.
+ *   pty_ws_adam: one Adam step (Kingma and Ba) on float weights w with
+ *     moments m, v (step counts from 1); wb (optional) gets a bf16 copy.
+ *   pty_ws_to_bf16, pty_ws_add: element-wise conversion and sum. */
+int pty_ws_gemm(int32_t M, int32_t N, int32_t K, const void* A, int64_t sam, int64_t sak,
+                const void* B, int64_t sbk, int64_t sbn, float* C, int64_t scm, int64_t scn,
+                int32_t splits, float* partial, void* stream);
+int pty_ws_im2col(int32_t B, int32_t H, int32_t W, int32_t C, const void* X, void* col, void* stream);
+int pty_ws_col2im(int32_t B, int32_t H, int32_t W, int32_t C, const float* dcol, float* dX, void* stream);
+int pty_ws_pool2(int32_t B, int32_t H, int32_t W, int32_t C, const void* X, void* Y, void* stream);
+int pty_ws_pool2_bwd(int32_t B, int32_t H, int32_t W, int32_t C, const float* dY, float* dX, void* stream);
+int pty_ws_up2(int32_t B, int32_t h, int32_t w, int32_t C, const void* X, void* Y, void* stream);
+int pty_ws_up2_bwd(int32_t B, int32_t h, int32_t w, int32_t C, const float* dY, float* dX, void* stream);
+int pty_ws_bias_act(int64_t P, int32_t C, const float* Z, const float* bias, int32_t relu,
+                    const void* skip, void* a, void* out, float* a32, void* stream);
+int64_t pty_ws_act_bwd_scratch(int64_t P, int32_t C);
+int pty_ws_act_bwd(int64_t P, int32_t C, const float* dA, const void* a, int32_t relu, void* dZ,
+                   float* dbias, float* scratch, void* stream);
+int pty_ws_loss(int64_t P, const float* Y, const float* T, const float* w, float* dY,
+                float* loss_parts, void* stream);
+int pty_ws_adam(int64_t n, float* w, void* wb, const float* g, float* m, float* v, float lr,
+                float b1, float b2, float eps, int32_t step, void* stream);
+int pty_ws_to_bf16(int64_t n, const float* x, void* y, void* stream);
+int pty_ws_add(int64_t n, const float* a, const float* b, float* out, void* stream);
+/* Data for the network, nf frames of npix pixels:
+ *   pty_ws_prep_input: x = bf16(sqrt(I) / mean(sqrt(I))) per frame (I float);
+ *   pty_ws_targets: target[2 i .. 2 i + 1] = (cos, sin) arg psi[i] (psi
+ *     complex64), weight[i] = |P[i mod npix]|^2 wscale;
+ *   pty_ws_exits: psi[i] = |P[i mod npix]| (y0 + i y1) / |(y0, y1)|, the exit
+ *     waves with the predicted phases (y float pairs). */
+int pty_ws_prep_input(int32_t nf, int64_t npix, const float* I, void* x, void* stream);
+int pty_ws_targets(int32_t nf, int64_t npix, const void* psi, const void* P, float wscale,
+                   float* target, float* weight, void* stream);
+int pty_ws_exits(int32_t nf, int64_t npix, const float* y, const void* P, void* psi, void* stream);
+
 /* 1 if the frame shape N0 x N1 has a fused FFT kernel. */
 int pty_shape_supported(int32_t N0, int32_t N1);
 

@@ -64,6 +64,27 @@ SIGNATURES = {
     "pty_legacy_random_scratch_words": [c_int32, ctypes.c_int64],
     "pty_legacy_random_jump": [ctypes.POINTER(ctypes.c_uint32), ctypes.c_int64,
                                ctypes.POINTER(ctypes.c_uint32)],
+    "pty_ws_gemm": [c_int32, c_int32, c_int32, c_void_p, c_int64, c_int64, c_void_p, c_int64, c_int64,
+                    c_void_p, c_int64, c_int64, c_int32, c_void_p, c_void_p],
+    "pty_ws_im2col": [c_int32, c_int32, c_int32, c_int32, c_void_p, c_void_p, c_void_p],
+    "pty_ws_col2im": [c_int32, c_int32, c_int32, c_int32, c_void_p, c_void_p, c_void_p],
+    "pty_ws_pool2": [c_int32, c_int32, c_int32, c_int32, c_void_p, c_void_p, c_void_p],
+    "pty_ws_pool2_bwd": [c_int32, c_int32, c_int32, c_int32, c_void_p, c_void_p, c_void_p],
+    "pty_ws_up2": [c_int32, c_int32, c_int32, c_int32, c_void_p, c_void_p, c_void_p],
+    "pty_ws_up2_bwd": [c_int32, c_int32, c_int32, c_int32, c_void_p, c_void_p, c_void_p],
+    "pty_ws_bias_act": [c_int64, c_int32, c_void_p, c_void_p, c_int32, c_void_p, c_void_p, c_void_p,
+                        c_void_p, c_void_p],
+    "pty_ws_act_bwd_scratch": [c_int64, c_int32],
+    "pty_ws_act_bwd": [c_int64, c_int32, c_void_p, c_void_p, c_int32, c_void_p, c_void_p, c_void_p,
+                       c_void_p],
+    "pty_ws_loss": [c_int64, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p],
+    "pty_ws_adam": [c_int64, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, ctypes.c_float,
+                    ctypes.c_float, ctypes.c_float, ctypes.c_float, c_int32, c_void_p],
+    "pty_ws_to_bf16": [c_int64, c_void_p, c_void_p, c_void_p],
+    "pty_ws_add": [c_int64, c_void_p, c_void_p, c_void_p, c_void_p],
+    "pty_ws_prep_input": [c_int32, c_int64, c_void_p, c_void_p, c_void_p],
+    "pty_ws_targets": [c_int32, c_int64, c_void_p, c_void_p, ctypes.c_float, c_void_p, c_void_p, c_void_p],
+    "pty_ws_exits": [c_int32, c_int64, c_void_p, c_void_p, c_void_p, c_void_p],
     "pty_shape_supported": [c_int32, c_int32],
     "pty_frame_tile_candidates": [c_int32, c_int32, ctypes.POINTER(c_int32), c_int32,
                                   ctypes.POINTER(c_int32)],
@@ -74,7 +95,8 @@ SIGNATURES = {
     "pty_launch_count": [],
 }
 _RESTYPES = {"pty_last_error": ctypes.c_char_p, "pty_launch_count": ctypes.c_int64,
-             "pty_legacy_random_scratch_words": ctypes.c_int64}
+             "pty_legacy_random_scratch_words": ctypes.c_int64,
+             "pty_ws_act_bwd_scratch": ctypes.c_int64}
 
 
 class PtyError(RuntimeError):

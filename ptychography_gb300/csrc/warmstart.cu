@@ -1,0 +1,549 @@
+// The learned warm start's network: 3 x 3 convolutions as im2col + BF16
+// tensor-core GEMMs with FP32 accumulation, and the element-wise pieces of
+// its forward pass, backward pass and Adam step.  No reference counterpart:
+// the reference starts ERA from ones (ptychography/era.py:480-486); the warm
+// start replaces that initial object by one stitched from per-frame phases
+// this network predicts from sqrt(I).
+//
+// Layout: activations NHWC (pixel-major, channels contiguous), BF16 between
+// layers; GEMM outputs FP32.  A convolution with C_in inputs is
+//   forward  Y[p][co] = sum_k col[p][k] W[co][k],     col = im2col(X), k = (ky*3 + kx) C_in + ci
+//   dgrad    dcol[p][k] = sum_co dY[p][co] W[co][k],  dX = col2im(dcol)
+//   wgrad    dW[co][k] = sum_p dY[p][co] col[p][k]    (split over p, partials summed in order)
+// all three by one GEMM kernel with strided operands.
+//
+// The GEMM: mma.sync.m16n8k16 (BF16 in, FP32 accumulate), 64 x 64 output
+// tiles, 4 warps of 32 x 32, K in steps of 32 staged through shared memory
+// ([m][k] and [n][k], 40-element rows: the fragment loads of a warp hit 32
+// distinct banks).  Fragment layout of m16n8k16 (PTX ISA): lane = 4 g + t;
+// A: a0 = (g, 2t..2t+1), a1 = (g+8, 2t..), a2 = (g, 2t+8..), a3 = (g+8, 2t+8..);
+// B (k x n, column-major): b0 = (2t..2t+1, g), b1 = (2t+8.., g);
+// C: c0, c1 = (g, 2t..2t+1), c2, c3 = (g+8, 2t..2t+1).
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include "../../include/ptycho_gb300.h"
+#include "engine.h"
+
+namespace pty {
+
+namespace {
+
+constexpr int kTM = 64, kTN = 64, kTK = 32, kPad = 40, kGemmThreads = 128;
+
+struct GemmArgs {
+  int M, N, K;
+  const __nv_bfloat16* A;
+  long long sam, sak;        // A(m, k) = A[m sam + k sak]
+  const __nv_bfloat16* B;
+  long long sbk, sbn;        // B(k, n) = B[k sbk + n sbn]
+  float* C;                  // C(m, n) = C[m scm + n scn] (+ split * M * N for partials)
+  long long scm, scn;
+  int k_per_split;           // K range of one blockIdx.z
+};
+
+__device__ __forceinline__ uint32_t ld_pair(const __nv_bfloat16* p) {
+  return *reinterpret_cast<const uint32_t*>(p);
+}
+
+__global__ void __launch_bounds__(kGemmThreads) ws_gemm_kernel(GemmArgs g) {
+  __shared__ __align__(16) __nv_bfloat16 sa[kTM][kPad];
+  __shared__ __align__(16) __nv_bfloat16 sb[kTN][kPad];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int m0 = blockIdx.y * kTM, n0 = blockIdx.x * kTN;
+  const int kbeg = blockIdx.z * g.k_per_split;
+  const int kend = min(g.K, kbeg + g.k_per_split);
+  const int wm = (warp >> 1) * 32, wn = (warp & 1) * 32;   // warp's 32 x 32 sub-tile
+  const int gq = lane >> 2, tq = lane & 3;
+  float acc[2][4][4];
+#pragma unroll
+  for (int i = 0; i < 2; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+#pragma unroll
+      for (int r = 0; r < 4; ++r) acc[i][j][r] = 0.f;
+  const __nv_bfloat16 zero = __float2bfloat16(0.f);
+  for (int k0 = kbeg; k0 < kend; k0 += kTK) {
+    // stage A[m0 .. +64][k0 .. +32] and B[k0 .. +32][n0 .. +64] (zero outside)
+    for (int i = tid; i < kTM * kTK; i += kGemmThreads) {
+      const int r = i / kTK, c = i % kTK;
+      const int m = m0 + r, k = k0 + c;
+      sa[r][c] = (m < g.M && k < kend) ? g.A[(long long)m * g.sam + (long long)k * g.sak] : zero;
+    }
+    for (int i = tid; i < kTN * kTK; i += kGemmThreads) {
+      const int r = i / kTK, c = i % kTK;
+      const int n = n0 + r, k = k0 + c;
+      sb[r][c] = (n < g.N && k < kend) ? g.B[(long long)k * g.sbk + (long long)n * g.sbn] : zero;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < kTK; kk += 16) {
+      uint32_t af[2][4], bf[4][2];
+#pragma unroll
+      for (int i = 0; i < 2; ++i) {
+        const int r = wm + 16 * i + gq;
+        af[i][0] = ld_pair(&sa[r][kk + 2 * tq]);
+        af[i][1] = ld_pair(&sa[r + 8][kk + 2 * tq]);
+        af[i][2] = ld_pair(&sa[r][kk + 2 * tq + 8]);
+        af[i][3] = ld_pair(&sa[r + 8][kk + 2 * tq + 8]);
+      }
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const int c = wn + 8 * j + gq;
+        bf[j][0] = ld_pair(&sb[c][kk + 2 * tq]);
+        bf[j][1] = ld_pair(&sb[c][kk + 2 * tq + 8]);
+      }
+#pragma unroll
+      for (int i = 0; i < 2; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+          asm volatile(
+              "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 "
+              "{%0, %1, %2, %3}, {%4, %5, %6, %7}, {%8, %9}, {%0, %1, %2, %3};"
+              : "+f"(acc[i][j][0]), "+f"(acc[i][j][1]), "+f"(acc[i][j][2]), "+f"(acc[i][j][3])
+              : "r"(af[i][0]), "r"(af[i][1]), "r"(af[i][2]), "r"(af[i][3]), "r"(bf[j][0]), "r"(bf[j][1]));
+    }
+    __syncthreads();
+  }
+  float* C = g.C + (size_t)blockIdx.z * g.M * g.N;
+#pragma unroll
+  for (int i = 0; i < 2; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+#pragma unroll
+      for (int r = 0; r < 4; ++r) {
+        const int m = m0 + wm + 16 * i + gq + (r >= 2 ? 8 : 0);
+        const int n = n0 + wn + 8 * j + 2 * tq + (r & 1);
+        if (m < g.M && n < g.N) C[(long long)m * g.scm + (long long)n * g.scn] = acc[i][j][r];
+      }
+}
+
+// out[i] = sum over s < splits of part[s][i], in split order (deterministic)
+__global__ void ws_sum_splits_kernel(const float* __restrict__ part, int splits, long long n,
+                                     float* __restrict__ out) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    float s = 0.f;
+    for (int k = 0; k < splits; ++k) s += part[(size_t)k * n + i];
+    out[i] = s;
+  }
+}
+
+#define WS_LOOP(i, n) \
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < (n); i += (long long)gridDim.x * blockDim.x)
+
+// col[p][(ky*3 + kx) C + c] = X[b][y + ky - 1][x + kx - 1][c] (zero outside), p = (b, y, x)
+__global__ void ws_im2col_kernel(int Bt, int H, int W, int C, const __nv_bfloat16* __restrict__ X,
+                                 __nv_bfloat16* __restrict__ col) {
+  const long long K = 9ll * C, n = (long long)Bt * H * W * K;
+  WS_LOOP(i, n) {
+    const long long p = i / K;
+    const int k = (int)(i % K), tap = k / C, c = k % C;
+    const int x = (int)(p % W), y = (int)((p / W) % H), b = (int)(p / ((long long)W * H));
+    const int yy = y + tap / 3 - 1, xx = x + tap % 3 - 1;
+    col[i] = (yy >= 0 && yy < H && xx >= 0 && xx < W)
+                 ? X[(((long long)b * H + yy) * W + xx) * C + c]
+                 : __float2bfloat16(0.f);
+  }
+}
+
+// dX[b][y][x][c] = sum over taps of dcol[(b, y - ky + 1, x - kx + 1)][(ky*3 + kx) C + c]
+__global__ void ws_col2im_kernel(int Bt, int H, int W, int C, const float* __restrict__ dcol,
+                                 float* __restrict__ dX) {
+  const long long n = (long long)Bt * H * W * C, K = 9ll * C;
+  WS_LOOP(i, n) {
+    const int c = (int)(i % C);
+    const long long p = i / C;
+    const int x = (int)(p % W), y = (int)((p / W) % H), b = (int)(p / ((long long)W * H));
+    float s = 0.f;
+#pragma unroll
+    for (int tap = 0; tap < 9; ++tap) {
+      const int yy = y - tap / 3 + 1, xx = x - tap % 3 + 1;
+      if (yy >= 0 && yy < H && xx >= 0 && xx < W)
+        s += dcol[(((long long)b * H + yy) * W + xx) * K + tap * C + c];
+    }
+    dX[i] = s;
+  }
+}
+
+// 2 x 2 average pooling (NHWC) and its adjoint
+__global__ void ws_pool2_kernel(int Bt, int H, int W, int C, const __nv_bfloat16* __restrict__ X,
+                                __nv_bfloat16* __restrict__ Y) {
+  const int h = H / 2, w = W / 2;
+  const long long n = (long long)Bt * h * w * C;
+  WS_LOOP(i, n) {
+    const int c = (int)(i % C);
+    const long long p = i / C;
+    const int x = (int)(p % w), y = (int)((p / w) % h), b = (int)(p / ((long long)w * h));
+    const long long base = (((long long)b * H + 2 * y) * W + 2 * x) * C + c;
+    const float s = __bfloat162float(X[base]) + __bfloat162float(X[base + C]) +
+                    __bfloat162float(X[base + (long long)W * C]) + __bfloat162float(X[base + (long long)W * C + C]);
+    Y[i] = __float2bfloat16(0.25f * s);
+  }
+}
+__global__ void ws_pool2_bwd_kernel(int Bt, int H, int W, int C, const float* __restrict__ dY,
+                                    float* __restrict__ dX) {
+  const long long n = (long long)Bt * H * W * C;
+  WS_LOOP(i, n) {
+    const int c = (int)(i % C);
+    const long long p = i / C;
+    const int x = (int)(p % W), y = (int)((p / W) % H), b = (int)(p / ((long long)W * H));
+    dX[i] = 0.25f * dY[(((long long)b * (H / 2) + y / 2) * (W / 2) + x / 2) * C + c];
+  }
+}
+
+// nearest 2 x upsampling (h x w -> 2h x 2w, NHWC) and its adjoint
+__global__ void ws_up2_kernel(int Bt, int h, int w, int C, const __nv_bfloat16* __restrict__ X,
+                              __nv_bfloat16* __restrict__ Y) {
+  const long long n = (long long)Bt * 4 * h * w * C;
+  WS_LOOP(i, n) {
+    const int c = (int)(i % C);
+    const long long p = i / C;
+    const int x = (int)(p % (2 * w)), y = (int)((p / (2 * w)) % (2 * h)), b = (int)(p / (4ll * w * h));
+    Y[i] = X[(((long long)b * h + y / 2) * w + x / 2) * C + c];
+  }
+}
+__global__ void ws_up2_bwd_kernel(int Bt, int h, int w, int C, const float* __restrict__ dY,
+                                  float* __restrict__ dX) {
+  const long long n = (long long)Bt * h * w * C;
+  WS_LOOP(i, n) {
+    const int c = (int)(i % C);
+    const long long p = i / C;
+    const int x = (int)(p % w), y = (int)((p / w) % h), b = (int)(p / ((long long)w * h));
+    const long long W2 = 2ll * w;
+    const long long base = (((long long)b * 2 * h + 2 * y) * W2 + 2 * x) * C + c;
+    dX[i] = dY[base] + dY[base + C] + dY[base + W2 * C] + dY[base + W2 * C + C];
+  }
+}
+
+// a = act(Z + bias) (relu when relu != 0); out = a + skip (skip may be null).
+// a and out as BF16; a32 (optional) as FP32 (the network's final output).
+__global__ void ws_bias_act_kernel(long long P, int C, const float* __restrict__ Z, const float* __restrict__ bias,
+                                   int relu, const __nv_bfloat16* __restrict__ skip,
+                                   __nv_bfloat16* __restrict__ a, __nv_bfloat16* __restrict__ out,
+                                   float* __restrict__ a32) {
+  const long long n = P * C;
+  WS_LOOP(i, n) {
+    float v = Z[i] + bias[i % C];
+    if (relu) v = fmaxf(v, 0.f);
+    const __nv_bfloat16 vb = __float2bfloat16(v);
+    if (a) a[i] = vb;
+    if (a32) a32[i] = v;
+    if (out) out[i] = skip ? __float2bfloat16(__bfloat162float(vb) + __bfloat162float(skip[i])) : vb;
+  }
+}
+
+// dZ = dA * (a > 0) (relu) or dA; as BF16 for the GEMMs; per-block partial
+// sums of dZ per channel into part[blockIdx.x][C] (bias gradient, summed in
+// block order by ws_sum_rows_kernel)
+__global__ void ws_act_bwd_kernel(long long P, int C, const float* __restrict__ dA,
+                                  const __nv_bfloat16* __restrict__ a, int relu,
+                                  __nv_bfloat16* __restrict__ dZ, float* __restrict__ part,
+                                  long long rows_per_block) {
+  const long long r0 = blockIdx.x * rows_per_block;
+  const long long r1 = min(P, r0 + rows_per_block);
+  for (int c0 = 0; c0 < C; c0 += blockDim.x) {
+    const int c = c0 + threadIdx.x;
+    float s = 0.f;
+    if (c < C) {
+      for (long long r = r0; r < r1; ++r) {
+        const long long i = r * C + c;
+        float g = dA[i];
+        if (relu && !(__bfloat162float(a[i]) > 0.f)) g = 0.f;
+        dZ[i] = __float2bfloat16(g);
+        s += g;
+      }
+      part[(size_t)blockIdx.x * C + c] = s;
+    }
+  }
+}
+
+// out[c] = sum over r < rows of part[r][c], in row order
+__global__ void ws_sum_rows_kernel(const float* __restrict__ part, int rows, int C, float* __restrict__ out) {
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < C; c += gridDim.x * blockDim.x) {
+    float s = 0.f;
+    for (int r = 0; r < rows; ++r) s += part[(size_t)r * C + c];
+    out[c] = s;
+  }
+}
+
+// weighted squared error of Y [P][2] against T [P][2] with per-pixel weights
+// w [P] (already normalised to sum 1): dY = 2 w (Y - T); per-block partial
+// losses into lpart[blockIdx.x]
+__global__ void ws_loss_kernel(long long P, const float* __restrict__ Y, const float* __restrict__ T,
+                               const float* __restrict__ w, float* __restrict__ dY, float* __restrict__ lpart) {
+  __shared__ float red[256];
+  float s = 0.f;
+  WS_LOOP(p, P) {
+    const float w0 = w[p];
+    const float e0 = Y[2 * p] - T[2 * p], e1 = Y[2 * p + 1] - T[2 * p + 1];
+    dY[2 * p] = 2.f * w0 * e0;
+    dY[2 * p + 1] = 2.f * w0 * e1;
+    s += w0 * (e0 * e0 + e1 * e1);
+  }
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if ((int)threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) lpart[blockIdx.x] = red[0];
+}
+
+// Adam (Kingma and Ba, 2015) on FP32 master weights, with a BF16 copy
+__global__ void ws_adam_kernel(long long n, float* __restrict__ w, __nv_bfloat16* __restrict__ wb,
+                               const float* __restrict__ g, float* __restrict__ m, float* __restrict__ v,
+                               float lr, float b1, float b2, float eps, float c1, float c2) {
+  WS_LOOP(i, n) {
+    const float gi = g[i];
+    const float mi = b1 * m[i] + (1.f - b1) * gi;
+    const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
+    m[i] = mi;
+    v[i] = vi;
+    const float wi = w[i] - lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+    w[i] = wi;
+    if (wb) wb[i] = __float2bfloat16(wi);
+  }
+}
+
+__global__ void ws_to_bf16_kernel(long long n, const float* __restrict__ x, __nv_bfloat16* __restrict__ y) {
+  WS_LOOP(i, n) y[i] = __float2bfloat16(x[i]);
+}
+
+// out = a + b (FP32), for gradients meeting at a skip connection
+__global__ void ws_add_kernel(long long n, const float* __restrict__ a, const float* __restrict__ b,
+                              float* __restrict__ out) {
+  WS_LOOP(i, n) out[i] = a[i] + b[i];
+}
+
+inline unsigned grid_for(long long n) {
+  long long g = (n + 255) / 256;
+  if (g > 8 * 152) g = 8 * 152;
+  return (unsigned)(g < 1 ? 1 : g);
+}
+
+}  // namespace
+
+}  // namespace pty
+
+using namespace pty;
+
+namespace {
+typedef __nv_bfloat16 bf16;
+constexpr long long kActRows = 256;   // pixels per block of ws_act_bwd_kernel
+constexpr int kLossBlocks = 256;
+int ws_launched(const char* where) { return check_launch(where); }
+}  // namespace
+
+extern "C" int pty_ws_gemm(int32_t M, int32_t N, int32_t K, const void* A, int64_t sam, int64_t sak,
+                           const void* B, int64_t sbk, int64_t sbn, float* C, int64_t scm, int64_t scn,
+                           int32_t splits, float* partial, void* stream) {
+  if (M < 1 || N < 1 || K < 1 || !A || !B || !C) return set_error(PTY_ERR_ARG, "bad GEMM arguments");
+  if (splits < 1) splits = 1;
+  if (splits > 1 && (!partial || scm != N || scn != 1))
+    return set_error(PTY_ERR_ARG, "split GEMM needs partials and a contiguous M x N output");
+  GemmArgs g;
+  g.M = M;
+  g.N = N;
+  g.K = K;
+  g.A = (const bf16*)A;
+  g.sam = sam;
+  g.sak = sak;
+  g.B = (const bf16*)B;
+  g.sbk = sbk;
+  g.sbn = sbn;
+  g.C = splits > 1 ? partial : C;
+  g.scm = scm;
+  g.scn = scn;
+  // K per split a multiple of the K step, so only the last split is ragged
+  int kps = (K + splits - 1) / splits;
+  kps = ((kps + kTK - 1) / kTK) * kTK;
+  splits = (K + kps - 1) / kps;
+  g.k_per_split = kps;
+  cudaStream_t st = (cudaStream_t)stream;
+  dim3 grid((N + kTN - 1) / kTN, (M + kTM - 1) / kTM, splits);
+  ws_gemm_kernel<<<grid, kGemmThreads, 0, st>>>(g);
+  PTY_TRY(ws_launched("ws_gemm_kernel"));
+  if (g.C != C) {
+    const long long n = (long long)M * N;
+    ws_sum_splits_kernel<<<grid_for(n), 256, 0, st>>>(partial, splits, n, C);
+    PTY_TRY(ws_launched("ws_sum_splits_kernel"));
+  }
+  return PTY_OK;
+}
+
+extern "C" int pty_ws_im2col(int32_t B, int32_t H, int32_t W, int32_t C, const void* X, void* col,
+                             void* stream) {
+  if (B < 1 || H < 1 || W < 1 || C < 1 || !X || !col) return set_error(PTY_ERR_ARG, "bad im2col arguments");
+  const long long n = 9ll * B * H * W * C;
+  ws_im2col_kernel<<<grid_for(n), 256, 0, (cudaStream_t)stream>>>(B, H, W, C, (const bf16*)X, (bf16*)col);
+  return ws_launched("ws_im2col_kernel");
+}
+
+extern "C" int pty_ws_col2im(int32_t B, int32_t H, int32_t W, int32_t C, const float* dcol, float* dX,
+                             void* stream) {
+  if (B < 1 || H < 1 || W < 1 || C < 1 || !dcol || !dX) return set_error(PTY_ERR_ARG, "bad col2im arguments");
+  const long long n = (long long)B * H * W * C;
+  ws_col2im_kernel<<<grid_for(n), 256, 0, (cudaStream_t)stream>>>(B, H, W, C, dcol, dX);
+  return ws_launched("ws_col2im_kernel");
+}
+
+extern "C" int pty_ws_pool2(int32_t B, int32_t H, int32_t W, int32_t C, const void* X, void* Y, void* stream) {
+  if (B < 1 || H < 2 || W < 2 || (H | W) & 1 || C < 1 || !X || !Y) return set_error(PTY_ERR_ARG, "bad pool arguments");
+  const long long n = (long long)B * (H / 2) * (W / 2) * C;
+  ws_pool2_kernel<<<grid_for(n), 256, 0, (cudaStream_t)stream>>>(B, H, W, C, (const bf16*)X, (bf16*)Y);
+  return ws_launched("ws_pool2_kernel");
+}
+
+extern "C" int pty_ws_pool2_bwd(int32_t B, int32_t H, int32_t W, int32_t C, const float* dY, float* dX,
+                                void* stream) {
+  if (B < 1 || H < 2 || W < 2 || (H | W) & 1 || C < 1 || !dY || !dX) return set_error(PTY_ERR_ARG, "bad pool arguments");
+  const long long n = (long long)B * H * W * C;
+  ws_pool2_bwd_kernel<<<grid_for(n), 256, 0, (cudaStream_t)stream>>>(B, H, W, C, dY, dX);
+  return ws_launched("ws_pool2_bwd_kernel");
+}
+
+extern "C" int pty_ws_up2(int32_t B, int32_t h, int32_t w, int32_t C, const void* X, void* Y, void* stream) {
+  if (B < 1 || h < 1 || w < 1 || C < 1 || !X || !Y) return set_error(PTY_ERR_ARG, "bad upsample arguments");
+  const long long n = 4ll * B * h * w * C;
+  ws_up2_kernel<<<grid_for(n), 256, 0, (cudaStream_t)stream>>>(B, h, w, C, (const bf16*)X, (bf16*)Y);
+  return ws_launched("ws_up2_kernel");
+}
+
+extern "C" int pty_ws_up2_bwd(int32_t B, int32_t h, int32_t w, int32_t C, const float* dY, float* dX,
+                              void* stream) {
+  if (B < 1 || h < 1 || w < 1 || C < 1 || !dY || !dX) return set_error(PTY_ERR_ARG, "bad upsample arguments");
+  const long long n = (long long)B * h * w * C;
+  ws_up2_bwd_kernel<<<grid_for(n), 256, 0, (cudaStream_t)stream>>>(B, h, w, C, dY, dX);
+  return ws_launched("ws_up2_bwd_kernel");
+}
+
+extern "C" int pty_ws_bias_act(int64_t P, int32_t C, const float* Z, const float* bias, int32_t relu,
+                               const void* skip, void* a, void* out, float* a32, void* stream) {
+  if (P < 1 || C < 1 || !Z || !bias) return set_error(PTY_ERR_ARG, "bad activation arguments");
+  const long long n = P * C;
+  ws_bias_act_kernel<<<grid_for(n), 256, 0, (cudaStream_t)stream>>>(P, C, Z, bias, relu, (const bf16*)skip,
+                                                                    (bf16*)a, (bf16*)out, a32);
+  return ws_launched("ws_bias_act_kernel");
+}
+
+extern "C" int64_t pty_ws_act_bwd_scratch(int64_t P, int32_t C) {
+  if (P < 1 || C < 1) return -1;
+  return ((P + kActRows - 1) / kActRows) * C;
+}
+
+extern "C" int pty_ws_act_bwd(int64_t P, int32_t C, const float* dA, const void* a, int32_t relu, void* dZ,
+                              float* dbias, float* scratch, void* stream) {
+  if (P < 1 || C < 1 || C > 1024 || !dA || !dZ || !dbias || !scratch || (relu && !a))
+    return set_error(PTY_ERR_ARG, "bad activation-gradient arguments");
+  const long long blocks = (P + kActRows - 1) / kActRows;
+  if (blocks > 2147483647ll) return set_error(PTY_ERR_RANGE, "too many pixels");
+  cudaStream_t st = (cudaStream_t)stream;
+  const int threads = C < 32 ? 32 : (C > 256 ? 256 : ((C + 31) / 32) * 32);
+  ws_act_bwd_kernel<<<(unsigned)blocks, threads, 0, st>>>(P, C, dA, (const bf16*)a, relu, (bf16*)dZ, scratch,
+                                                          kActRows);
+  PTY_TRY(ws_launched("ws_act_bwd_kernel"));
+  ws_sum_rows_kernel<<<(C + 127) / 128, 128, 0, st>>>(scratch, (int)blocks, C, dbias);
+  return ws_launched("ws_sum_rows_kernel");
+}
+
+extern "C" int pty_ws_loss(int64_t P, const float* Y, const float* T, const float* w, float* dY,
+                           float* loss_parts, void* stream) {
+  if (P < 1 || !Y || !T || !w || !dY || !loss_parts) return set_error(PTY_ERR_ARG, "bad loss arguments");
+  ws_loss_kernel<<<kLossBlocks, 256, 0, (cudaStream_t)stream>>>(P, Y, T, w, dY, loss_parts);
+  return ws_launched("ws_loss_kernel");
+}
+
+extern "C" int pty_ws_adam(int64_t n, float* w, void* wb, const float* g, float* m, float* v, float lr,
+                           float b1, float b2, float eps, int32_t step, void* stream) {
+  if (n < 1 || !w || !g || !m || !v || step < 1) return set_error(PTY_ERR_ARG, "bad Adam arguments");
+  const float c1 = 1.f - powf(b1, (float)step), c2 = 1.f - powf(b2, (float)step);
+  ws_adam_kernel<<<grid_for(n), 256, 0, (cudaStream_t)stream>>>(n, w, (bf16*)wb, g, m, v, lr, b1, b2, eps, c1, c2);
+  return ws_launched("ws_adam_kernel");
+}
+
+extern "C" int pty_ws_to_bf16(int64_t n, const float* x, void* y, void* stream) {
+  if (n < 1 || !x || !y) return set_error(PTY_ERR_ARG, "bad conversion arguments");
+  ws_to_bf16_kernel<<<grid_for(n), 256, 0, (cudaStream_t)stream>>>(n, x, (bf16*)y);
+  return ws_launched("ws_to_bf16_kernel");
+}
+
+extern "C" int pty_ws_add(int64_t n, const float* a, const float* b, float* out, void* stream) {
+  if (n < 1 || !a || !b || !out) return set_error(PTY_ERR_ARG, "bad add arguments");
+  ws_add_kernel<<<grid_for(n), 256, 0, (cudaStream_t)stream>>>(n, a, b, out);
+  return ws_launched("ws_add_kernel");
+}
+
+// ---------------------------------------------------------------- data
+namespace pty {
+namespace {
+
+// x[f][p] = bf16(sqrt(I[f][p]) / mean_p sqrt(I[f][p])) (one block per frame)
+__global__ void ws_prep_kernel(long long npix, const float* __restrict__ I, __nv_bfloat16* __restrict__ x) {
+  __shared__ float red[256];
+  const float* If = I + (size_t)blockIdx.x * npix;
+  __nv_bfloat16* xf = x + (size_t)blockIdx.x * npix;
+  float s = 0.f;
+  for (long long p = threadIdx.x; p < npix; p += blockDim.x) s += sqrtf(fmaxf(If[p], 0.f));
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if ((int)threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+    __syncthreads();
+  }
+  const float inv = red[0] > 0.f ? (float)npix / red[0] : 0.f;
+  for (long long p = threadIdx.x; p < npix; p += blockDim.x) xf[p] = __float2bfloat16(sqrtf(fmaxf(If[p], 0.f)) * inv);
+}
+
+// target[f][p] = (cos, sin) of arg psi[f][p]; weight[f][p] = |P[p]|^2 * wscale
+__global__ void ws_targets_kernel(long long nf, long long npix, const float2* __restrict__ psi,
+                                  const float2* __restrict__ P, float wscale, float* __restrict__ target,
+                                  float* __restrict__ weight) {
+  const long long n = nf * npix;
+  WS_LOOP(i, n) {
+    const float2 v = psi[i];
+    const float r = sqrtf(v.x * v.x + v.y * v.y);
+    target[2 * i] = r > 0.f ? v.x / r : 1.f;
+    target[2 * i + 1] = r > 0.f ? v.y / r : 0.f;
+    const float2 q = P[i % npix];
+    weight[i] = (q.x * q.x + q.y * q.y) * wscale;
+  }
+}
+
+// psi[f][p] = |P[p]| (y0 + i y1) / |y| : the exit wave with the predicted phase
+__global__ void ws_exits_kernel(long long nf, long long npix, const float* __restrict__ y,
+                                const float2* __restrict__ P, float2* __restrict__ psi) {
+  const long long n = nf * npix;
+  WS_LOOP(i, n) {
+    const float a = y[2 * i], b = y[2 * i + 1];
+    const float r = sqrtf(a * a + b * b);
+    const float2 q = P[i % npix];
+    const float m = sqrtf(q.x * q.x + q.y * q.y);
+    psi[i] = r > 0.f ? make_float2(m * a / r, m * b / r) : make_float2(m, 0.f);
+  }
+}
+
+}  // namespace
+}  // namespace pty
+
+extern "C" int pty_ws_prep_input(int32_t nf, int64_t npix, const float* I, void* x, void* stream) {
+  if (nf < 1 || npix < 1 || !I || !x) return set_error(PTY_ERR_ARG, "bad input-preparation arguments");
+  ws_prep_kernel<<<nf, 256, 0, (cudaStream_t)stream>>>(npix, I, (bf16*)x);
+  return ws_launched("ws_prep_kernel");
+}
+
+extern "C" int pty_ws_targets(int32_t nf, int64_t npix, const void* psi, const void* P, float wscale,
+                              float* target, float* weight, void* stream) {
+  if (nf < 1 || npix < 1 || !psi || !P || !target || !weight) return set_error(PTY_ERR_ARG, "bad target arguments");
+  const long long n = (long long)nf * npix;
+  ws_targets_kernel<<<grid_for(n), 256, 0, (cudaStream_t)stream>>>(nf, npix, (const float2*)psi, (const float2*)P,
+                                                                   wscale, target, weight);
+  return ws_launched("ws_targets_kernel");
+}
+
+extern "C" int pty_ws_exits(int32_t nf, int64_t npix, const float* y, const void* P, void* psi, void* stream) {
+  if (nf < 1 || npix < 1 || !y || !P || !psi) return set_error(PTY_ERR_ARG, "bad exit-wave arguments");
+  const long long n = (long long)nf * npix;
+  ws_exits_kernel<<<grid_for(n), 256, 0, (cudaStream_t)stream>>>(nf, npix, y, (const float2*)P, (float2*)psi);
+  return ws_launched("ws_exits_kernel");
+}

@@ -1,0 +1,238 @@
+"""Learned warm start: a small conv encoder-decoder predicts each frame's
+exit-wave phase from sqrt(I); the predicted exit waves are stitched into an
+initial object (the overlap update, era.py:336-369) from which ERA starts
+instead of from ones (era.py:480-486).  No reference counterpart.
+
+The network (6 layers, 3 x 3 kernels, 32-128 channels, BF16 weights and
+activations, FP32 accumulation) runs forward and backward on the library's
+kernels (``pty_ws_*``: im2col + BF16 tensor-core GEMMs, pooling, upsampling,
+activations, loss, Adam); torch only holds device memory.
+
+    x  = sqrt(I) (centred, scaled to unit mean)          H x W x 1
+    h1 = relu(conv(x))                                    H x W x 32
+    h2 = relu(conv(pool(h1)))                             H/2 x W/2 x 64
+    h3 = relu(conv(pool(h2)))                             H/4 x W/4 x 128
+    h4 = relu(conv(up(h3))) + h2                          H/2 x W/2 x 64
+    h5 = relu(conv(up(h4))) + h1                          H x W x 32
+    y  = conv(h5)                                         H x W x 2  (cos, sin of the phase)
+"""
+import ctypes
+
+import numpy as np
+
+from . import _native
+
+# (C_in, C_out, relu, level) of the six convolutions; level = log2 of the
+# downsampling
+LAYERS = ((1, 32, True, 0), (32, 64, True, 1), (64, 128, True, 2),
+          (128, 64, True, 1), (64, 32, True, 0), (32, 2, False, 0))
+
+
+def _torch():
+    import torch
+    return torch
+
+
+def _p(t):
+    return ctypes.c_void_p(t.data_ptr()) if t is not None else None
+
+
+class WarmStartNet:
+    """Parameters (FP32 masters, BF16 copies, Adam moments) and the
+    forward / backward passes for frames of H x W pixels (H, W multiples of 4)."""
+
+    def __init__(self, H, W, seed=0, device=None):
+        torch = _torch()
+        if H % 4 or W % 4:
+            raise ValueError("frame sides must be multiples of 4")
+        self.H, self.W = H, W
+        self.dev = device or torch.device("cuda", torch.cuda.current_device())
+        self.lib = _native.load()
+        rng = np.random.default_rng(seed)
+        self.w, self.b, self.wb = [], [], []
+        for cin, cout, _, _ in LAYERS:
+            std = float(np.sqrt(2.0 / (9 * cin)))                 # He initialisation
+            w = (rng.standard_normal((cout, 9 * cin)) * std).astype(np.float32)
+            self.w.append(torch.from_numpy(w).to(self.dev))
+            self.b.append(torch.zeros(cout, dtype=torch.float32, device=self.dev))
+            self.wb.append(torch.empty((cout, 9 * cin), dtype=torch.bfloat16, device=self.dev))
+        self.m = [torch.zeros_like(t) for t in self.w + self.b]
+        self.v = [torch.zeros_like(t) for t in self.w + self.b]
+        self.step_count = 0
+        self._sync_bf16()
+        self._bufs = {}
+
+    def _sp(self):
+        torch = _torch()
+        return ctypes.c_void_p(torch.cuda.current_stream(self.dev).cuda_stream)
+
+    def _sync_bf16(self):
+        for w, wb in zip(self.w, self.wb):
+            assert w.dtype == _torch().float32 and wb.dtype == _torch().bfloat16
+            _native.check(self.lib.pty_ws_to_bf16(w.numel(), _p(w), _p(wb), self._sp()))
+
+    def state_dict(self):
+        return {"w": [t.cpu().numpy() for t in self.w], "b": [t.cpu().numpy() for t in self.b]}
+
+    def load_state_dict(self, st):
+        torch = _torch()
+        for i in range(len(LAYERS)):
+            self.w[i].copy_(torch.from_numpy(np.asarray(st["w"][i], np.float32)))
+            self.b[i].copy_(torch.from_numpy(np.asarray(st["b"][i], np.float32)))
+        self._sync_bf16()
+
+    def _buf(self, name, shape, dtype):
+        torch = _torch()
+        t = self._bufs.get(name)
+        n = int(np.prod(shape))
+        if t is None or t.numel() < n or t.dtype != dtype:
+            t = torch.empty(n, dtype=dtype, device=self.dev)
+            self._bufs[name] = t
+        return t[:n].view(*shape)
+
+    # ------------------------------------------------------------ layers
+    def _conv_fwd(self, i, x, B, H, W, skip=None, last=False):
+        """x: (B, H, W, C_in) bf16 -> (a, out) bf16, or the FP32 output if last."""
+        torch = _torch()
+        cin, cout, relu, _ = LAYERS[i]
+        lib, sp = self.lib, self._sp()
+        P, K = B * H * W, 9 * cin
+        col = self._buf("col%d" % i, (P, K), torch.bfloat16)
+        _native.check(lib.pty_ws_im2col(B, H, W, cin, _p(x), _p(col), sp))
+        Z = self._buf("z%d" % i, (P, cout), torch.float32)
+        _native.check(lib.pty_ws_gemm(P, cout, K, _p(col), K, 1, _p(self.wb[i]), 1, K,
+                                      _p(Z), cout, 1, 1, None, sp))
+        if last:
+            y = self._buf("y", (B, H, W, cout), torch.float32)
+            _native.check(lib.pty_ws_bias_act(P, cout, _p(Z), _p(self.b[i]), 0, None, None, None,
+                                              _p(y), sp))
+            return y
+        a = self._buf("a%d" % i, (B, H, W, cout), torch.bfloat16)
+        out = self._buf("h%d" % i, (B, H, W, cout), torch.bfloat16) if skip is not None else a
+        _native.check(lib.pty_ws_bias_act(P, cout, _p(Z), _p(self.b[i]), int(relu), _p(skip), _p(a),
+                                          _p(out) if skip is not None else None, None, sp))
+        return out
+
+    def forward(self, x):
+        """x: (B, H, W, 1) bf16 device tensor (normalised sqrt(I)); returns y
+        (B, H, W, 2) float32, (cos, sin) of the predicted phase (unnormalised)."""
+        torch = _torch()
+        B, H, W = x.shape[0], self.H, self.W
+        lib, sp = self.lib, self._sp()
+        self._x = x
+        h1 = self._conv_fwd(0, x, B, H, W)
+        p1 = self._buf("p1", (B, H // 2, W // 2, 32), torch.bfloat16)
+        _native.check(lib.pty_ws_pool2(B, H, W, 32, _p(h1), _p(p1), sp))
+        h2 = self._conv_fwd(1, p1, B, H // 2, W // 2)
+        p2 = self._buf("p2", (B, H // 4, W // 4, 64), torch.bfloat16)
+        _native.check(lib.pty_ws_pool2(B, H // 2, W // 2, 64, _p(h2), _p(p2), sp))
+        h3 = self._conv_fwd(2, p2, B, H // 4, W // 4)
+        u3 = self._buf("u3", (B, H // 2, W // 2, 128), torch.bfloat16)
+        _native.check(lib.pty_ws_up2(B, H // 4, W // 4, 128, _p(h3), _p(u3), sp))
+        h4 = self._conv_fwd(3, u3, B, H // 2, W // 2, skip=h2)
+        u4 = self._buf("u4", (B, H, W, 64), torch.bfloat16)
+        _native.check(lib.pty_ws_up2(B, H // 2, W // 2, 64, _p(h4), _p(u4), sp))
+        h5 = self._conv_fwd(4, u4, B, H, W, skip=h1)
+        return self._conv_fwd(5, h5, B, H, W, last=True)
+
+    def _conv_bwd(self, i, dA, B, H, W, need_dx):
+        """dA: gradient (FP32, B x H x W x C_out) at layer i's activation; sets
+        the layer's weight and bias gradients, returns the input gradient."""
+        torch = _torch()
+        cin, cout, relu, _ = LAYERS[i]
+        lib, sp = self.lib, self._sp()
+        P, K = B * H * W, 9 * cin
+        a = self._bufs["a%d" % i] if relu else None
+        dZ = self._buf("dz", (P, cout), torch.bfloat16)
+        scr = self._buf("actscr", (int(lib.pty_ws_act_bwd_scratch(P, cout)),), torch.float32)
+        _native.check(lib.pty_ws_act_bwd(P, cout, _p(dA), _p(a), int(relu), _p(dZ), _p(self.gb[i]),
+                                         _p(scr), sp))
+        # wgrad: dW[co][k] = sum_p dZ[p][co] col[p][k], split over pixels
+        splits = max(1, min(64, P // 4096))
+        part = self._buf("wpart", (splits, cout, K), torch.float32)
+        col = self._bufs["col%d" % i]
+        _native.check(lib.pty_ws_gemm(cout, K, P, _p(dZ), 1, cout, _p(col), K, 1,
+                                      _p(self.gw[i]), K, 1, splits, _p(part), sp))
+        if not need_dx:
+            return None
+        dcol = self._buf("dcol", (P, K), torch.float32)
+        _native.check(lib.pty_ws_gemm(P, K, cout, _p(dZ), cout, 1, _p(self.wb[i]), K, 1,
+                                      _p(dcol), K, 1, 1, None, sp))
+        dX = self._buf("dx%d" % i, (B, H, W, cin), torch.float32)
+        _native.check(lib.pty_ws_col2im(B, H, W, cin, _p(dcol), _p(dX), sp))
+        return dX
+
+    def backward(self, dy):
+        """dy: (B, H, W, 2) FP32 gradient at the output; fills self.gw / self.gb."""
+        torch = _torch()
+        if not hasattr(self, "gw"):
+            self.gw = [torch.empty_like(w) for w in self.w]
+            self.gb = [torch.empty_like(b) for b in self.b]
+        B, H, W = dy.shape[0], self.H, self.W
+        lib, sp = self.lib, self._sp()
+        dh5 = self._conv_bwd(5, dy, B, H, W, True)                  # h5 = a4 + h1
+        du4 = self._conv_bwd(4, dh5, B, H, W, True)
+        dh4 = self._buf("dh4", (B, H // 2, W // 2, 64), torch.float32)
+        _native.check(lib.pty_ws_up2_bwd(B, H // 2, W // 2, 64, _p(du4), _p(dh4), sp))
+        du3 = self._conv_bwd(3, dh4, B, H // 2, W // 2, True)       # h4 = a3 + h2
+        dh3 = self._buf("dh3", (B, H // 4, W // 4, 128), torch.float32)
+        _native.check(lib.pty_ws_up2_bwd(B, H // 4, W // 4, 128, _p(du3), _p(dh3), sp))
+        dp2 = self._conv_bwd(2, dh3, B, H // 4, W // 4, True)
+        dh2 = self._buf("dh2", (B, H // 2, W // 2, 64), torch.float32)
+        _native.check(lib.pty_ws_pool2_bwd(B, H // 2, W // 2, 64, _p(dp2), _p(dh2), sp))
+        _native.check(lib.pty_ws_add(dh2.numel(), _p(dh2), _p(dh4), _p(dh2), sp))
+        dp1 = self._conv_bwd(1, dh2, B, H // 2, W // 2, True)
+        dh1 = self._buf("dh1", (B, H, W, 32), torch.float32)
+        _native.check(lib.pty_ws_pool2_bwd(B, H, W, 32, _p(dp1), _p(dh1), sp))
+        _native.check(lib.pty_ws_add(dh1.numel(), _p(dh1), _p(dh5), _p(dh1), sp))
+        self._conv_bwd(0, dh1, B, H, W, False)
+
+    def loss_grad(self, y, target, weight):
+        """Weighted squared error (weights summing to 1) and its gradient; the
+        loss is returned as a device scalar tensor (no host sync)."""
+        torch = _torch()
+        P = y.shape[0] * self.H * self.W
+        dy = self._buf("dy", tuple(y.shape), torch.float32)
+        parts = self._buf("lparts", (256,), torch.float32)
+        _native.check(self.lib.pty_ws_loss(P, _p(y), _p(target), _p(weight), _p(dy), _p(parts),
+                                           self._sp()))
+        return parts, dy
+
+    def adam_step(self, lr=1e-3, b1=0.9, b2=0.999, eps=1e-8):
+        self.step_count += 1
+        sp = self._sp()
+        params = list(zip(self.w, self.wb, self.gw)) + [(b, None, g) for b, g in zip(self.b, self.gb)]
+        for (w, wb, g), m, v in zip(params, self.m, self.v):
+            _native.check(self.lib.pty_ws_adam(w.numel(), _p(w), _p(wb), _p(g), _p(m), _p(v),
+                                               lr, b1, b2, eps, self.step_count, sp))
+
+    def train_step(self, x, target, weight, lr=1e-3):
+        y = self.forward(x)
+        parts, dy = self.loss_grad(y, target, weight)
+        self.backward(dy)
+        self.adam_step(lr)
+        return parts
+
+    # ------------------------------------------------------------ data
+    def prep_input(self, I):
+        """I: (n, H, W) float32 device tensor of centred intensities -> network input."""
+        torch = _torch()
+        n = I.shape[0]
+        x = torch.empty((n, self.H, self.W, 1), dtype=torch.bfloat16, device=self.dev)
+        _native.check(self.lib.pty_ws_prep_input(n, self.H * self.W, _p(I), _p(x), self._sp()))
+        return x
+
+    def predict_exits(self, I, P, batch=64):
+        """Exit waves |P| exp(i phase) with the predicted phases, for centred
+        intensities I (n, H, W) float32 on the device and the probe P (H, W)
+        complex64 on the device."""
+        torch = _torch()
+        n = I.shape[0]
+        psi = torch.empty((n, self.H, self.W), dtype=torch.complex64, device=self.dev)
+        for s in range(0, n, batch):
+            e = min(n, s + batch)
+            x = self.prep_input(I[s:e].contiguous())
+            y = self.forward(x)
+            _native.check(self.lib.pty_ws_exits(e - s, self.H * self.W, _p(y), _p(P), _p(psi[s:]),
+                                                self._sp()))
+        return psi
