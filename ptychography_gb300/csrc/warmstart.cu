@@ -478,7 +478,9 @@ extern "C" int pty_ws_add(int64_t n, const float* a, const float* b, float* out,
 namespace pty {
 namespace {
 
-// x[f][p] = bf16(sqrt(I[f][p]) / mean_p sqrt(I[f][p])) (one block per frame)
+// x[f][p] = bf16(log(1 + sqrt(I[f][p]) / mean_p sqrt(I[f][p]))) (one block per
+// frame): the logarithm compresses the central peak, which in unit-mean
+// amplitudes reaches ~100, to the range of the rest of the pattern
 __global__ void ws_prep_kernel(long long npix, const float* __restrict__ I, __nv_bfloat16* __restrict__ x) {
   __shared__ float red[256];
   const float* If = I + (size_t)blockIdx.x * npix;
@@ -492,16 +494,22 @@ __global__ void ws_prep_kernel(long long npix, const float* __restrict__ I, __nv
     __syncthreads();
   }
   const float inv = red[0] > 0.f ? (float)npix / red[0] : 0.f;
-  for (long long p = threadIdx.x; p < npix; p += blockDim.x) xf[p] = __float2bfloat16(sqrtf(fmaxf(If[p], 0.f)) * inv);
+  for (long long p = threadIdx.x; p < npix; p += blockDim.x)
+    xf[p] = __float2bfloat16(log1pf(sqrtf(fmaxf(If[p], 0.f)) * inv));
 }
 
-// target[f][p] = (cos, sin) of arg psi[f][p]; weight[f][p] = |P[p]|^2 * wscale
+// target[f][p] = (cos, sin) of arg psi[f][p] (object_phase: of arg psi conj(P),
+// the object's phase under the probe); weight[f][p] = |P[p]|^2 * wscale
 __global__ void ws_targets_kernel(long long nf, long long npix, const float2* __restrict__ psi,
-                                  const float2* __restrict__ P, float wscale, float* __restrict__ target,
-                                  float* __restrict__ weight) {
+                                  const float2* __restrict__ P, int object_phase, float wscale,
+                                  float* __restrict__ target, float* __restrict__ weight) {
   const long long n = nf * npix;
   WS_LOOP(i, n) {
-    const float2 v = psi[i];
+    float2 v = psi[i];
+    if (object_phase) {
+      const float2 q = P[i % npix];
+      v = make_float2(v.x * q.x + v.y * q.y, v.y * q.x - v.x * q.y);
+    }
     const float r = sqrtf(v.x * v.x + v.y * v.y);
     target[2 * i] = r > 0.f ? v.x / r : 1.f;
     target[2 * i + 1] = r > 0.f ? v.y / r : 0.f;
@@ -510,16 +518,22 @@ __global__ void ws_targets_kernel(long long nf, long long npix, const float2* __
   }
 }
 
-// psi[f][p] = |P[p]| (y0 + i y1) / |y| : the exit wave with the predicted phase
+// psi[f][p] = |P[p]| (y0 + i y1) / |y|, the exit wave with the predicted phase
+// (object_phase: P[p] (y0 + i y1) / |y|, the probe's phase added back)
 __global__ void ws_exits_kernel(long long nf, long long npix, const float* __restrict__ y,
-                                const float2* __restrict__ P, float2* __restrict__ psi) {
+                                const float2* __restrict__ P, int object_phase, float2* __restrict__ psi) {
   const long long n = nf * npix;
   WS_LOOP(i, n) {
     const float a = y[2 * i], b = y[2 * i + 1];
     const float r = sqrtf(a * a + b * b);
+    const float ca = r > 0.f ? a / r : 1.f, sa = r > 0.f ? b / r : 0.f;
     const float2 q = P[i % npix];
-    const float m = sqrtf(q.x * q.x + q.y * q.y);
-    psi[i] = r > 0.f ? make_float2(m * a / r, m * b / r) : make_float2(m, 0.f);
+    if (object_phase) {
+      psi[i] = make_float2(q.x * ca - q.y * sa, q.x * sa + q.y * ca);
+    } else {
+      const float m = sqrtf(q.x * q.x + q.y * q.y);
+      psi[i] = make_float2(m * ca, m * sa);
+    }
   }
 }
 
@@ -532,18 +546,20 @@ extern "C" int pty_ws_prep_input(int32_t nf, int64_t npix, const float* I, void*
   return ws_launched("ws_prep_kernel");
 }
 
-extern "C" int pty_ws_targets(int32_t nf, int64_t npix, const void* psi, const void* P, float wscale,
-                              float* target, float* weight, void* stream) {
+extern "C" int pty_ws_targets(int32_t nf, int64_t npix, const void* psi, const void* P, int32_t object_phase,
+                              float wscale, float* target, float* weight, void* stream) {
   if (nf < 1 || npix < 1 || !psi || !P || !target || !weight) return set_error(PTY_ERR_ARG, "bad target arguments");
   const long long n = (long long)nf * npix;
   ws_targets_kernel<<<grid_for(n), 256, 0, (cudaStream_t)stream>>>(nf, npix, (const float2*)psi, (const float2*)P,
-                                                                   wscale, target, weight);
+                                                                   object_phase, wscale, target, weight);
   return ws_launched("ws_targets_kernel");
 }
 
-extern "C" int pty_ws_exits(int32_t nf, int64_t npix, const float* y, const void* P, void* psi, void* stream) {
+extern "C" int pty_ws_exits(int32_t nf, int64_t npix, const float* y, const void* P, int32_t object_phase,
+                            void* psi, void* stream) {
   if (nf < 1 || npix < 1 || !y || !P || !psi) return set_error(PTY_ERR_ARG, "bad exit-wave arguments");
   const long long n = (long long)nf * npix;
-  ws_exits_kernel<<<grid_for(n), 256, 0, (cudaStream_t)stream>>>(nf, npix, y, (const float2*)P, (float2*)psi);
+  ws_exits_kernel<<<grid_for(n), 256, 0, (cudaStream_t)stream>>>(nf, npix, y, (const float2*)P, object_phase,
+                                                                 (float2*)psi);
   return ws_launched("ws_exits_kernel");
 }

@@ -8,7 +8,7 @@ activations, FP32 accumulation) runs forward and backward on the library's
 kernels (``pty_ws_*``: im2col + BF16 tensor-core GEMMs, pooling, upsampling,
 activations, loss, Adam); torch only holds device memory.
 
-    x  = sqrt(I) (centred, scaled to unit mean)          H x W x 1
+    x  = log(1 + sqrt(I) / mean sqrt(I)) (centred)        H x W x 1
     h1 = relu(conv(x))                                    H x W x 32
     h2 = relu(conv(pool(h1)))                             H/2 x W/2 x 64
     h3 = relu(conv(pool(h2)))                             H/4 x W/4 x 128
@@ -41,8 +41,12 @@ class WarmStartNet:
     """Parameters (FP32 masters, BF16 copies, Adam moments) and the
     forward / backward passes for frames of H x W pixels (H, W multiples of 4)."""
 
-    def __init__(self, H, W, seed=0, device=None):
+    def __init__(self, H, W, seed=0, device=None, object_phase=True):
         torch = _torch()
+        # target: the object's phase under the probe (the exit-wave phase less
+        # the probe's, which a known probe restores at stitching), or the
+        # exit-wave phase itself
+        self.object_phase = bool(object_phase)
         if H % 4 or W % 4:
             raise ValueError("frame sides must be multiples of 4")
         self.H, self.W = H, W
@@ -233,6 +237,115 @@ class WarmStartNet:
             e = min(n, s + batch)
             x = self.prep_input(I[s:e].contiguous())
             y = self.forward(x)
-            _native.check(self.lib.pty_ws_exits(e - s, self.H * self.W, _p(y), _p(P), _p(psi[s:]),
-                                                self._sp()))
+            _native.check(self.lib.pty_ws_exits(e - s, self.H * self.W, _p(y), _p(P),
+                                                int(self.object_phase), _p(psi[s:]), self._sp()))
         return psi
+
+
+# ---------------------------------------------------------------- training data
+def smooth01(rng, shape, sigma=4.0):
+    """Gaussian-filtered uniform noise rescaled to [0, 1]."""
+    import scipy.ndimage as ndi
+    a = ndi.gaussian_filter(rng.random(shape), sigma)
+    return (a - a.min()) / (a.max() - a.min())
+
+
+def random_object(rng, U, V=None):
+    """amplitude 0.5 + 0.5 s1, phase pi (s2 - 1/2), s1, s2 smooth random fields."""
+    V = V or U
+    return (0.5 + 0.5 * smooth01(rng, (U, V))) * np.exp(1j * np.pi * (smooth01(rng, (U, V)) - 0.5))
+
+
+def aperture_probe(N, radius, edge, quad):
+    """Circular aperture with a Gaussian edge and quadratic phase quad r^2."""
+    y, x = np.mgrid[:N, :N] - N / 2
+    r = np.sqrt(x ** 2 + y ** 2)
+    amp = np.exp(-np.clip(r - radius, 0, None) ** 2 / (2 * edge ** 2)) * (r < radius + 3 * edge)
+    return amp * np.exp(1j * quad * r ** 2)
+
+
+class _FramePlan:
+    """A plan for n frames of N x N in a U x V object (the library's C ABI)."""
+
+    def __init__(self, n, N, U, V, R):
+        self.lib = _native.load()
+        R64 = np.ascontiguousarray(np.asarray(R)[:, :2], dtype=np.int64)
+        self.h = ctypes.c_void_p()
+        _native.check(self.lib.pty_plan_create(ctypes.byref(_native.Geometry(n, N, N, U, V)),
+                                               R64.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)),
+                                               ctypes.byref(self.h)))
+
+    def close(self):
+        if self.h:
+            self.lib.pty_plan_destroy(self.h)
+            self.h = ctypes.c_void_p()
+
+
+def make_training_set(net, n_frames, seed=0, frames_per_object=8, batch=32, pad=64):
+    """Frames of random objects (random_object) under random probes (aperture
+    radius 24-40 px, edge 4 px, quadratic phase 0.001-0.004 rad/px^2) at
+    random positions: the network input (normalised sqrt of the centred
+    intensities), the targets (cos, sin of the exit-wave phase) and weights
+    |P|^2 scaled so that `batch` frames sum to 1.  All on the device."""
+    torch = _torch()
+    N, dev, lib = net.H, net.dev, net.lib
+    rng = np.random.default_rng(seed)
+    n = (n_frames // frames_per_object) * frames_per_object
+    x = torch.empty((n, N, N, 1), dtype=torch.bfloat16, device=dev)
+    t = torch.empty((n, N, N, 2), dtype=torch.float32, device=dev)
+    w = torch.empty((n, N, N), dtype=torch.float32, device=dev)
+    k = frames_per_object
+    I = torch.empty((k, N, N), dtype=torch.float32, device=dev)
+    psi = torch.empty((k, N, N), dtype=torch.complex64, device=dev)
+    U = N + pad
+    sp = net._sp()
+    for s in range(0, n, k):
+        O = random_object(rng, U)
+        P = aperture_probe(N, rng.uniform(24, 40), 4.0, rng.uniform(0.001, 0.004))
+        R = -rng.integers(0, U - N + 1, (k, 2))
+        R[0] = 0                                       # the plan's window starts at R.max() = 0
+        Od = torch.from_numpy(O.astype(np.complex64)).to(dev)
+        Pd = torch.from_numpy(P.astype(np.complex64)).to(dev)
+        plan = _FramePlan(k, N, U, U, R)
+        try:
+            _native.check(lib.pty_intensities(plan.h, _p(Od), _p(Pd), _p(I), sp))
+            _native.check(lib.pty_make_exits(plan.h, _p(Od), _p(Pd), _p(psi), sp))
+            _native.check(lib.pty_ws_prep_input(k, N * N, _p(I), _p(x[s:]), sp))
+            wscale = 1.0 / (batch * float(np.sum(np.abs(P) ** 2)))
+            _native.check(lib.pty_ws_targets(k, N * N, _p(psi), _p(Pd), int(net.object_phase), wscale,
+                                             _p(t[s:]), _p(w[s:]), sp))
+            torch.cuda.current_stream(dev).synchronize()
+        finally:
+            plan.close()
+    return x, t, w
+
+
+def train(net, data, steps, batch=32, lr=1e-3, seed=0, log_every=0):
+    """Adam on random contiguous batches of the training set; returns the
+    per-step losses (host floats, read once at the end)."""
+    torch = _torch()
+    x, t, w = data
+    n = x.shape[0]
+    rng = np.random.default_rng(seed)
+    hist = torch.zeros((steps, 256), dtype=torch.float32, device=net.dev)
+    for step in range(steps):
+        s = int(rng.integers(0, n - batch + 1))
+        lr_s = lr * (0.1 if step >= int(0.8 * steps) else 1.0)     # one decay step
+        hist[step].copy_(net.train_step(x[s:s + batch], t[s:s + batch], w[s:s + batch], lr_s))
+        if log_every and (step + 1) % log_every == 0:
+            print("step %d loss %.4f" % (step + 1, float(hist[step].sum().cpu())), flush=True)
+    return hist.sum(dim=1, dtype=torch.float64).cpu().numpy().tolist()
+
+
+def warm_start_object(net, I_dev, P_dev, plan_h, U, V, alpha=1e-10, heat=None):
+    """The initial object for ERA: the network's exit waves for the centred
+    intensities I_dev (n, N, N) float32, stitched by the overlap update
+    (psup_O, era.py:336-369) with the probe P_dev on the plan's U x V grid.
+    Returns a complex64 (U, V) device tensor."""
+    torch = _torch()
+    psi = net.predict_exits(I_dev, P_dev)
+    O = torch.empty((U, V), dtype=torch.complex64, device=net.dev)
+    if heat is None:
+        heat = torch.empty((U, V), dtype=torch.float64, device=net.dev)
+    _native.check(net.lib.pty_psup_O(plan_h, _p(psi), _p(P_dev), _p(heat), 1, alpha, _p(O), net._sp()))
+    return O
