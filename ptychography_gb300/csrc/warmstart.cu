@@ -22,6 +22,8 @@
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
+#include <cstdint>
+
 #include "../../include/ptycho_gb300.h"
 #include "engine.h"
 
@@ -40,7 +42,53 @@ struct GemmArgs {
   float* C;                  // C(m, n) = C[m scm + n scn] (+ split * M * N for partials)
   long long scm, scn;
   int k_per_split;           // K range of one blockIdx.z
+  int a_vec, b_vec;          // 16-byte loads: 1 along k, 2 along m (A) / n (B), 0 none
 };
+
+// Stage an R x 32 operand tile (R = 64 rows of m or n) into s[row][k].
+// vec 1: k contiguous (8 k per 16-byte load); vec 2: rows contiguous (8 rows
+// per load, scattered); chunks crossing the operand's edge load element-wise.
+__device__ __forceinline__ void stage_tile(__nv_bfloat16 (*s)[kPad], const __nv_bfloat16* __restrict__ src,
+                                           long long s_row, long long s_k, int rows, int row0, int k0,
+                                           int kend, int vec) {
+  const __nv_bfloat16 zero = __float2bfloat16(0.f);
+  const int tid = threadIdx.x;
+  if (vec == 1) {
+    for (int c = tid; c < kTM * (kTK / 8); c += kGemmThreads) {
+      const int r = c >> 2, kc = (c & 3) * 8;
+      const int row = row0 + r, k = k0 + kc;
+      if (row < rows && k + 8 <= kend) {
+        *reinterpret_cast<uint4*>(&s[r][kc]) =
+            __ldg(reinterpret_cast<const uint4*>(src + (long long)row * s_row + k));
+      } else {
+#pragma unroll
+        for (int j = 0; j < 8; ++j)
+          s[r][kc + j] = (row < rows && k + j < kend) ? src[(long long)row * s_row + k + j] : zero;
+      }
+    }
+  } else if (vec == 2) {
+    for (int c = tid; c < (kTM / 8) * kTK; c += kGemmThreads) {
+      const int kk = c >> 3, rc = (c & 7) * 8;
+      const int row = row0 + rc, k = k0 + kk;
+      if (row + 8 <= rows && k < kend) {
+        const uint4 v = __ldg(reinterpret_cast<const uint4*>(src + row + (long long)k * s_k));
+        const __nv_bfloat16* e = reinterpret_cast<const __nv_bfloat16*>(&v);
+#pragma unroll
+        for (int j = 0; j < 8; ++j) s[rc + j][kk] = e[j];
+      } else {
+#pragma unroll
+        for (int j = 0; j < 8; ++j)
+          s[rc + j][kk] = (row + j < rows && k < kend) ? src[(long long)(row + j) + (long long)k * s_k] : zero;
+      }
+    }
+  } else {
+    for (int i = tid; i < kTM * kTK; i += kGemmThreads) {
+      const int r = i / kTK, c = i % kTK;
+      const int row = row0 + r, k = k0 + c;
+      s[r][c] = (row < rows && k < kend) ? src[(long long)row * s_row + (long long)k * s_k] : zero;
+    }
+  }
+}
 
 __device__ __forceinline__ uint32_t ld_pair(const __nv_bfloat16* p) {
   return *reinterpret_cast<const uint32_t*>(p);
@@ -62,19 +110,10 @@ __global__ void __launch_bounds__(kGemmThreads) ws_gemm_kernel(GemmArgs g) {
     for (int j = 0; j < 4; ++j)
 #pragma unroll
       for (int r = 0; r < 4; ++r) acc[i][j][r] = 0.f;
-  const __nv_bfloat16 zero = __float2bfloat16(0.f);
   for (int k0 = kbeg; k0 < kend; k0 += kTK) {
     // stage A[m0 .. +64][k0 .. +32] and B[k0 .. +32][n0 .. +64] (zero outside)
-    for (int i = tid; i < kTM * kTK; i += kGemmThreads) {
-      const int r = i / kTK, c = i % kTK;
-      const int m = m0 + r, k = k0 + c;
-      sa[r][c] = (m < g.M && k < kend) ? g.A[(long long)m * g.sam + (long long)k * g.sak] : zero;
-    }
-    for (int i = tid; i < kTN * kTK; i += kGemmThreads) {
-      const int r = i / kTK, c = i % kTK;
-      const int n = n0 + r, k = k0 + c;
-      sb[r][c] = (n < g.N && k < kend) ? g.B[(long long)k * g.sbk + (long long)n * g.sbn] : zero;
-    }
+    stage_tile(sa, g.A, g.sam, g.sak, g.M, m0, k0, kend, g.a_vec);
+    stage_tile(sb, g.B, g.sbn, g.sbk, g.N, n0, k0, kend, g.b_vec);
     __syncthreads();
 #pragma unroll
     for (int kk = 0; kk < kTK; kk += 16) {
@@ -145,6 +184,49 @@ __global__ void ws_im2col_kernel(int Bt, int H, int W, int C, const __nv_bfloat1
                  ? X[(((long long)b * H + yy) * W + xx) * C + c]
                  : __float2bfloat16(0.f);
   }
+}
+
+// The same with 8 channels per thread (C a multiple of 8): thread = (pixel,
+// channel chunk), grid row = tap; 16-byte copies, 32-bit index arithmetic
+// (pixels x C / 8 < 2^31).
+__global__ void ws_im2col8_kernel(int Bt, int H, int W, int C, const __nv_bfloat16* __restrict__ X,
+                                  __nv_bfloat16* __restrict__ col) {
+  const int chunks = C >> 3, tap = blockIdx.y;
+  const int n = Bt * H * W * chunks;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int p = i / chunks, ch = i - p * chunks;
+  const int x = p % W, t = p / W, y = t % H, b = t / H;
+  const int yy = y + tap / 3 - 1, xx = x + tap % 3 - 1;
+  uint4 v = make_uint4(0u, 0u, 0u, 0u);
+  if (yy >= 0 && yy < H && xx >= 0 && xx < W)
+    v = __ldg(reinterpret_cast<const uint4*>(X + ((size_t)(b * H + yy) * W + xx) * C + ch * 8));
+  *reinterpret_cast<uint4*>(col + (size_t)p * 9 * C + tap * C + ch * 8) = v;
+}
+
+// col2im with 4 channels per thread (C a multiple of 4), float4 reads
+__global__ void ws_col2im4_kernel(int Bt, int H, int W, int C, const float* __restrict__ dcol,
+                                  float* __restrict__ dX) {
+  const int chunks = C >> 2;
+  const int n = Bt * H * W * chunks;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int p = i / chunks, ch = i - p * chunks;
+  const int x = p % W, t = p / W, y = t % H, b = t / H;
+  float4 s = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+  for (int tap = 0; tap < 9; ++tap) {
+    const int yy = y - tap / 3 + 1, xx = x - tap % 3 + 1;
+    if (yy >= 0 && yy < H && xx >= 0 && xx < W) {
+      const float4 v = __ldg(reinterpret_cast<const float4*>(
+          dcol + ((size_t)(b * H + yy) * W + xx) * 9 * C + tap * C + ch * 4));
+      s.x += v.x;
+      s.y += v.y;
+      s.z += v.z;
+      s.w += v.w;
+    }
+  }
+  *reinterpret_cast<float4*>(dX + (size_t)p * C + ch * 4) = s;
 }
 
 // dX[b][y][x][c] = sum over taps of dcol[(b, y - ky + 1, x - kx + 1)][(ky*3 + kx) C + c]
@@ -360,6 +442,16 @@ extern "C" int pty_ws_gemm(int32_t M, int32_t N, int32_t K, const void* A, int64
   kps = ((kps + kTK - 1) / kTK) * kTK;
   splits = (K + kps - 1) / kps;
   g.k_per_split = kps;
+  // 16-byte loads where the operand has a contiguous dimension, 16-byte
+  // aligned rows and a base aligned to 16 bytes
+  auto vec_of = [](const void* ptr, long long s_row, long long s_k) {
+    if (((uintptr_t)ptr & 15u) != 0) return 0;
+    if (s_k == 1 && s_row % 8 == 0) return 1;
+    if (s_row == 1 && s_k % 8 == 0) return 2;
+    return 0;
+  };
+  g.a_vec = vec_of(A, sam, sak);
+  g.b_vec = vec_of(B, sbn, sbk);
   cudaStream_t st = (cudaStream_t)stream;
   dim3 grid((N + kTN - 1) / kTN, (M + kTM - 1) / kTM, splits);
   ws_gemm_kernel<<<grid, kGemmThreads, 0, st>>>(g);
@@ -376,6 +468,13 @@ extern "C" int pty_ws_im2col(int32_t B, int32_t H, int32_t W, int32_t C, const v
                              void* stream) {
   if (B < 1 || H < 1 || W < 1 || C < 1 || !X || !col) return set_error(PTY_ERR_ARG, "bad im2col arguments");
   const long long n = 9ll * B * H * W * C;
+  const long long n8 = (long long)B * H * W * (C / 8);
+  const bool vec = C % 8 == 0 && n8 < (1ll << 31) && ((uintptr_t)X & 15u) == 0 && ((uintptr_t)col & 15u) == 0;
+  if (vec) {
+    const dim3 grid((unsigned)((n8 + 255) / 256), 9);
+    ws_im2col8_kernel<<<grid, 256, 0, (cudaStream_t)stream>>>(B, H, W, C, (const bf16*)X, (bf16*)col);
+    return ws_launched("ws_im2col8_kernel");
+  }
   ws_im2col_kernel<<<grid_for(n), 256, 0, (cudaStream_t)stream>>>(B, H, W, C, (const bf16*)X, (bf16*)col);
   return ws_launched("ws_im2col_kernel");
 }
@@ -384,6 +483,12 @@ extern "C" int pty_ws_col2im(int32_t B, int32_t H, int32_t W, int32_t C, const f
                              void* stream) {
   if (B < 1 || H < 1 || W < 1 || C < 1 || !dcol || !dX) return set_error(PTY_ERR_ARG, "bad col2im arguments");
   const long long n = (long long)B * H * W * C;
+  const long long n4 = n / 4;
+  const bool vec = C % 4 == 0 && n4 < (1ll << 31) && ((uintptr_t)dcol & 15u) == 0 && ((uintptr_t)dX & 15u) == 0;
+  if (vec) {
+    ws_col2im4_kernel<<<(unsigned)((n4 + 255) / 256), 256, 0, (cudaStream_t)stream>>>(B, H, W, C, dcol, dX);
+    return ws_launched("ws_col2im4_kernel");
+  }
   ws_col2im_kernel<<<grid_for(n), 256, 0, (cudaStream_t)stream>>>(B, H, W, C, dcol, dX);
   return ws_launched("ws_col2im_kernel");
 }
