@@ -8,13 +8,14 @@ forward_sim API of andyofmelbourne/Ptychography.
 The reconstruction loops run in libptycho_gb300.so (hand-written sm_103a CUDA,
 C ABI in include/ptycho_gb300.h); Python prepares inputs and returns outputs.
 """
-from . import back_projection, cxi, dm, era, forward_models  # noqa: F401
+from . import back_projection, cxi, dm, era, forward_models, warmstart  # noqa: F401
 from .back_projection import Back_projection
 from .dm import DM, DM_batch
 from .era import ERA, ERA_batch
 from .cxi import read_cxi, write_cxi
 from .forward_models import forward_sim
+from .warmstart import WarmStartNet
 
-__all__ = ["ERA", "DM", "ERA_batch", "DM_batch", "write_cxi", "read_cxi", "forward_sim", "Back_projection", "era", "dm", "forward_models",
-           "back_projection"]
+__all__ = ["ERA", "DM", "ERA_batch", "DM_batch", "write_cxi", "read_cxi", "forward_sim", "Back_projection",
+           "WarmStartNet", "era", "dm", "forward_models", "back_projection", "warmstart"]
 __version__ = "0.1.0"

@@ -349,3 +349,31 @@ def warm_start_object(net, I_dev, P_dev, plan_h, U, V, alpha=1e-10, heat=None):
         heat = torch.empty((U, V), dtype=torch.float64, device=net.dev)
     _native.check(net.lib.pty_psup_O(plan_h, _p(psi), _p(P_dev), _p(heat), 1, alpha, _p(O), net._sp()))
     return O
+
+
+def initial_object(net, I, R, P, O_shape=None, alpha=1e-10):
+    """The warm start for ``ERA(I, R, P, O, ...)`` on host arrays: centred
+    intensities I (n, N, N), scan offsets R (n, 2) and the probe P (N, N),
+    as ERA takes them.  R is shifted as ERA's preamble shifts it
+    (era.py:504-505, on a copy); the object has ERA's default shape
+    (era.py:480-486) unless O_shape is given.  Returns a complex64 host array
+    to pass as ERA's O."""
+    torch = _torch()
+    I = np.asarray(I)
+    n, N0, N1 = I.shape
+    if (N0, N1) != (net.H, net.W):
+        raise ValueError("the network was built for %d x %d frames" % (net.H, net.W))
+    R = np.array(R, dtype=np.int64, copy=True)[:, :2]
+    R[:, 0] -= R[:, 0].max()
+    R[:, 1] -= R[:, 1].max()
+    if O_shape is None:
+        O_shape = (N0 + int(R[:, 0].max() - R[:, 0].min()), N1 + int(R[:, 1].max() - R[:, 1].min()))
+    U, V = O_shape
+    plan = _FramePlan(n, N0, U, V, R)
+    try:
+        I_d = torch.from_numpy(np.ascontiguousarray(I, dtype=np.float32)).to(net.dev)
+        P_d = torch.from_numpy(np.ascontiguousarray(P, dtype=np.complex64)).to(net.dev)
+        O = warm_start_object(net, I_d, P_d, plan.h, U, V, alpha)
+        return O.cpu().numpy()
+    finally:
+        plan.close()

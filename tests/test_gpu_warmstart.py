@@ -187,3 +187,26 @@ def test_training_on_simulated_frames_learns_the_phase():
     after = err(net)
     assert np.isfinite(losses).all()
     assert after < 0.6 * before and after < 1.0     # 1.0: predicting zero
+
+
+def test_initial_object_feeds_era():
+    """The public warm-start path: initial_object on host arrays, then ERA
+    from it (known probe, object update) converges like ERA from ones."""
+    import ptychography_gb300 as pty
+    from ptychography_gb300 import warmstart as ws
+    N = 64
+    net = ws.WarmStartNet(N, N, seed=0, device=dev())
+    ws.train(net, ws.make_training_set(net, 1024, seed=1, pad=32), 200, batch=32, lr=3e-4)
+    rng = np.random.default_rng(4)
+    O_true = ws.random_object(rng, 160)
+    P = ws.aperture_probe(N, 16, 3.0, 0.004)
+    pos = np.arange(8) * 12 + 4
+    R = -np.stack(np.meshgrid(pos, pos, indexing="ij"), -1).reshape(-1, 2)
+    ex = np.stack([O_true[-r0:-r0 + N, -r1:-r1 + N] * P for r0, r1 in R])
+    I = np.fft.fftshift(np.abs(np.fft.fft2(ex)) ** 2, axes=(-2, -1)).astype(np.float32)
+    O0 = ws.initial_object(net, I, R, P)
+    assert O0.shape == (N + 84, N + 84) and np.isfinite(O0).all()
+    O_a, info_a = pty.ERA(I, R.copy(), P, O0, 20, method=1)
+    O_b, info_b = pty.ERA(I, R.copy(), P, None, 20, method=1)
+    assert np.isfinite(O_a).all()
+    assert info_a["eMod"][-1] < 2.0 * info_b["eMod"][-1]
