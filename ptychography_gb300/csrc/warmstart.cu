@@ -58,8 +58,11 @@ __device__ __forceinline__ void stage_tile(__nv_bfloat16 (*s)[kPad], const __nv_
       const int r = c >> 2, kc = (c & 3) * 8;
       const int row = row0 + r, k = k0 + kc;
       if (row < rows && k + 8 <= kend) {
-        *reinterpret_cast<uint4*>(&s[r][kc]) =
-            __ldg(reinterpret_cast<const uint4*>(src + (long long)row * s_row + k));
+        // asynchronous 16-byte copy: lands while the other buffer is computed
+        const unsigned sa = (unsigned)__cvta_generic_to_shared(&s[r][kc]);
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(sa),
+                     "l"(src + (long long)row * s_row + k)
+                     : "memory");
       } else {
 #pragma unroll
         for (int j = 0; j < 8; ++j)
@@ -72,9 +75,10 @@ __device__ __forceinline__ void stage_tile(__nv_bfloat16 (*s)[kPad], const __nv_
       const int row = row0 + rc, k = k0 + kk;
       if (row + 8 <= rows && k < kend) {
         const uint4 v = __ldg(reinterpret_cast<const uint4*>(src + row + (long long)k * s_k));
-        const __nv_bfloat16* e = reinterpret_cast<const __nv_bfloat16*>(&v);
+        const uint32_t w[4] = {v.x, v.y, v.z, v.w};
 #pragma unroll
-        for (int j = 0; j < 8; ++j) s[rc + j][kk] = e[j];
+        for (int j = 0; j < 8; ++j)
+          s[rc + j][kk] = __ushort_as_bfloat16((unsigned short)((w[j >> 1] >> (16 * (j & 1))) & 0xffffu));
       } else {
 #pragma unroll
         for (int j = 0; j < 8; ++j)
@@ -95,8 +99,8 @@ __device__ __forceinline__ uint32_t ld_pair(const __nv_bfloat16* p) {
 }
 
 __global__ void __launch_bounds__(kGemmThreads) ws_gemm_kernel(GemmArgs g) {
-  __shared__ __align__(16) __nv_bfloat16 sa[kTM][kPad];
-  __shared__ __align__(16) __nv_bfloat16 sb[kTN][kPad];
+  __shared__ __align__(16) __nv_bfloat16 sa[2][kTM][kPad];
+  __shared__ __align__(16) __nv_bfloat16 sb[2][kTN][kPad];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int m0 = blockIdx.y * kTM, n0 = blockIdx.x * kTN;
   const int kbeg = blockIdx.z * g.k_per_split;
@@ -110,10 +114,21 @@ __global__ void __launch_bounds__(kGemmThreads) ws_gemm_kernel(GemmArgs g) {
     for (int j = 0; j < 4; ++j)
 #pragma unroll
       for (int r = 0; r < 4; ++r) acc[i][j][r] = 0.f;
-  for (int k0 = kbeg; k0 < kend; k0 += kTK) {
-    // stage A[m0 .. +64][k0 .. +32] and B[k0 .. +32][n0 .. +64] (zero outside)
-    stage_tile(sa, g.A, g.sam, g.sak, g.M, m0, k0, kend, g.a_vec);
-    stage_tile(sb, g.B, g.sbn, g.sbk, g.N, n0, k0, kend, g.b_vec);
+  // double buffering: the tile of step k0 + 32 is staged (asynchronously for
+  // k-contiguous operands) while step k0 is multiplied
+  int buf = 0;
+  if (kbeg < kend) {
+    stage_tile(sa[0], g.A, g.sam, g.sak, g.M, m0, kbeg, kend, g.a_vec);
+    stage_tile(sb[0], g.B, g.sbn, g.sbk, g.N, n0, kbeg, kend, g.b_vec);
+  }
+  asm volatile("cp.async.commit_group;" ::: "memory");
+  for (int k0 = kbeg; k0 < kend; k0 += kTK, buf ^= 1) {
+    if (k0 + kTK < kend) {
+      stage_tile(sa[buf ^ 1], g.A, g.sam, g.sak, g.M, m0, k0 + kTK, kend, g.a_vec);
+      stage_tile(sb[buf ^ 1], g.B, g.sbn, g.sbk, g.N, n0, k0 + kTK, kend, g.b_vec);
+    }
+    asm volatile("cp.async.commit_group;" ::: "memory");
+    asm volatile("cp.async.wait_group 1;" ::: "memory");   // this step's copies landed
     __syncthreads();
 #pragma unroll
     for (int kk = 0; kk < kTK; kk += 16) {
@@ -121,16 +136,16 @@ __global__ void __launch_bounds__(kGemmThreads) ws_gemm_kernel(GemmArgs g) {
 #pragma unroll
       for (int i = 0; i < 2; ++i) {
         const int r = wm + 16 * i + gq;
-        af[i][0] = ld_pair(&sa[r][kk + 2 * tq]);
-        af[i][1] = ld_pair(&sa[r + 8][kk + 2 * tq]);
-        af[i][2] = ld_pair(&sa[r][kk + 2 * tq + 8]);
-        af[i][3] = ld_pair(&sa[r + 8][kk + 2 * tq + 8]);
+        af[i][0] = ld_pair(&sa[buf][r][kk + 2 * tq]);
+        af[i][1] = ld_pair(&sa[buf][r + 8][kk + 2 * tq]);
+        af[i][2] = ld_pair(&sa[buf][r][kk + 2 * tq + 8]);
+        af[i][3] = ld_pair(&sa[buf][r + 8][kk + 2 * tq + 8]);
       }
 #pragma unroll
       for (int j = 0; j < 4; ++j) {
         const int c = wn + 8 * j + gq;
-        bf[j][0] = ld_pair(&sb[c][kk + 2 * tq]);
-        bf[j][1] = ld_pair(&sb[c][kk + 2 * tq + 8]);
+        bf[j][0] = ld_pair(&sb[buf][c][kk + 2 * tq]);
+        bf[j][1] = ld_pair(&sb[buf][c][kk + 2 * tq + 8]);
       }
 #pragma unroll
       for (int i = 0; i < 2; ++i)
