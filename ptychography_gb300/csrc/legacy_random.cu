@@ -32,9 +32,9 @@
 // INFORMS J. Computing 20(3), 2008.  phi comes from the Berlekamp-Massey
 // algorithm run on 2 x 19937 output bits of the generator itself, the jump
 // polynomials x^(2^e) mod phi from repeated squaring; both once per process
-// on the host.  Windows of segments 2^r .. 2^(r+1) - 1 are jumps of 2^r
-// segments from windows 0 .. 2^r - 1, so a draw of S segments needs
-// ceil(log2 S) rounds of jumps, each a launch of independent CTAs.  The low
+// on the host.  Windows of segments [4^l, 4^(l+1)) are jumps of 1, 2 or 3 x
+// 4^l segments from windows [0, 4^l), so a draw of S segments needs
+// ceil(log4 S) rounds of jumps, each a launch of independent CTAs.  The low
 // 31 bits of a jumped window's first word are not the sequence's (T ignores
 // them): a segment uses only that word's top bit and writes only the words
 // after its window.
@@ -59,7 +59,8 @@ constexpr int kMtDeg = 19937;                        // bits of generator state
 constexpr int kPolyW = (kMtDeg + 63) / 64;           // 312 64-bit words
 constexpr int kSegLog = 17;                          // segment: 2^17 words
 constexpr long long kSegWords = 1ll << kSegLog;
-constexpr int kMaxRounds = 24;                       // jumps up to 2^(17+23) words
+constexpr int kMaxRounds = 24;                       // x^(2^(17 + r)), r < 24
+constexpr int kLevels = kMaxRounds / 2;              // radix-4 rounds: up to 4^12 segments
 constexpr int kJumpThreads = 640;
 constexpr int kChunks = (kMtDeg + kMtLag - 1) / kMtLag;   // 88 chunks of 227 coefficients
 
@@ -113,22 +114,29 @@ __global__ void __launch_bounds__(kThreads)
   }
 }
 
-// win[dst0 + i] = g(T) win[src0 + i], one CTA per jump; g as 19968 bits (624
-// 32-bit words, degree < 19937).  Horner's rule 227 coefficients at a time:
+// One radix-4 round of jumps: windows [0, nsrc) are the sources; block b
+// computes window (j + 1) nsrc + i = g_j(T) window i, j = b / nsrc,
+// i = b mod nsrc, with g_j = polys[j] = x^((j + 1) nsrc L) mod phi (windows
+// at or past segs are skipped).  g as 19968 bits (624 32-bit words, degree
+// < 19937).  Horner's rule 227 coefficients at a time:
 // with S the source window extended by 227 words (sx[0, 851)),
 //   R <- T^227 R  xor  sum_{j < 227} g_(hi - j) T^(226 - j) S,
 // where T^227 R is 227 new words that each depend on R alone and T^k S is
 // the window sx[k, k + 624).  88 chunks cover the coefficients (the highest
 // chunk padded with zeros).
 __global__ void __launch_bounds__(kJumpThreads)
-    legacy_jump_kernel(const uint32_t* __restrict__ g, uint32_t* win, int src0, int dst0) {
+    legacy_jump_kernel(const uint32_t* __restrict__ polys, uint32_t* win, int nsrc, long long segs) {
   constexpr int kR = 1024;                   // R as a ring: window at [base, base + 624)
   __shared__ uint32_t sx[kMtN + kMtLag];
   __shared__ uint32_t r[kR];
   __shared__ uint32_t gb[kMtN + 8];          // coefficients, zero above bit 19967
   const int tid = threadIdx.x;
-  const uint32_t* src = win + (size_t)(src0 + blockIdx.x) * kMtN;
-  uint32_t* dst = win + (size_t)(dst0 + blockIdx.x) * kMtN;
+  const int jj = blockIdx.x / nsrc, i0 = blockIdx.x % nsrc;
+  const long long d = (long long)(jj + 1) * nsrc + i0;
+  if (d >= segs) return;                     // whole block: no barrier skipped
+  const uint32_t* g = polys + (size_t)jj * kMtN;
+  const uint32_t* src = win + (size_t)i0 * kMtN;
+  uint32_t* dst = win + (size_t)d * kMtN;
   for (int i = tid; i < kR; i += kJumpThreads) r[i] = 0u;
   for (int i = tid; i < kMtN + 8; i += kJumpThreads) gb[i] = i < kMtN ? g[i] : 0u;
   for (int i = tid; i < kMtN; i += kJumpThreads) sx[i] = src[i];
@@ -145,10 +153,11 @@ __global__ void __launch_bounds__(kJumpThreads)
     base += kMtLag;
     if (tid < kMtN) {
       const int hi = kChunks * kMtLag - 1 - kMtLag * c;   // this chunk's top coefficient
-      uint32_t term = 0u;
+      uint32_t acc[4] = {0u, 0u, 0u, 0u};      // independent XOR chains
+#pragma unroll
       for (int j = 0; j < kMtLag; j += 32) {
-        // coefficients hi - j - k (k < 32) as bit k, walked by their set bits
-        // (the same for every thread of the warp)
+        // coefficients hi - j - k (k < 32) as bit k (the same for every
+        // thread of the warp), applied as masks: no data-dependent loop
         const int top = hi - j, lo = top - 31;
         uint32_t bits;
         if (lo >= 0) {
@@ -159,14 +168,12 @@ __global__ void __launch_bounds__(kJumpThreads)
           bits = gb[0] << (-lo);                             // no coefficients below 0
         }
         bits = __brev(bits);                                 // bit k = coefficient top - k
-        if (kMtLag - j < 32) bits &= (1u << (kMtLag - j)) - 1u;
-        while (bits) {
-          const int k = __ffs(bits) - 1;
-          bits &= bits - 1u;
-          term ^= sx[kMtLag - 1 - (j + k) + tid];
-        }
+        const uint32_t* sp = sx + (kMtLag - 1 - j) + tid;    // sp[-k] = sx[226 - (j + k) + tid]
+#pragma unroll
+        for (int k = 0; k < 32; ++k)
+          if (j + k < kMtLag) acc[k & 3] ^= sp[-k] & (0u - ((bits >> k) & 1u));
       }
-      r[(base + tid) & (kR - 1)] ^= term;
+      r[(base + tid) & (kR - 1)] ^= (acc[0] ^ acc[1]) ^ (acc[2] ^ acc[3]);
     }
     __syncthreads();
   }
@@ -302,6 +309,7 @@ Bits mul_mod(const Bits& a, const Bits& b, const Bits& phi) {
 struct JumpTable {
   Bits phi;
   std::vector<Bits> pow2;      // pow2[r] = x^(2^(17 + r)) mod phi
+  std::vector<Bits> pow3;      // pow3[l] = x^(3 4^l 2^17) mod phi
   bool ok = false;
 };
 
@@ -318,6 +326,7 @@ const JumpTable& jump_table() {
       t.pow2.push_back(p);
       p = sqr_mod(p, t.phi);
     }
+    for (int l = 0; l < kLevels; ++l) t.pow3.push_back(mul_mod(t.pow2[2 * l], t.pow2[2 * l + 1], t.phi));
     t.ok = true;
   });
   return t;
@@ -364,11 +373,16 @@ int device_jump_polys(const uint32_t** out) {
   }
   const JumpTable& jt = jump_table();
   if (!jt.ok) return set_error(PTY_ERR_CUDA, "MT19937 characteristic polynomial not found");
-  std::vector<uint32_t> h((size_t)kMaxRounds * kMtN, 0u);
-  for (int r = 0; r < kMaxRounds; ++r)
-    for (int i = 0; i < kPolyW; ++i) {
-      h[(size_t)r * kMtN + 2 * i] = (uint32_t)jt.pow2[(size_t)r][(size_t)i];
-      h[(size_t)r * kMtN + 2 * i + 1] = (uint32_t)(jt.pow2[(size_t)r][(size_t)i] >> 32);
+  // level l: x^(j 4^l 2^17) for j = 1, 2, 3 (pow2[2 l], pow2[2 l + 1], pow3[l])
+  std::vector<uint32_t> h((size_t)kLevels * 3 * kMtN, 0u);
+  for (int l = 0; l < kLevels; ++l)
+    for (int j = 0; j < 3; ++j) {
+      const Bits& q = j == 0 ? jt.pow2[(size_t)(2 * l)] : j == 1 ? jt.pow2[(size_t)(2 * l + 1)] : jt.pow3[(size_t)l];
+      uint32_t* o = &h[((size_t)l * 3 + j) * kMtN];
+      for (int i = 0; i < kPolyW; ++i) {
+        o[2 * i] = (uint32_t)q[(size_t)i];
+        o[2 * i + 1] = (uint32_t)(q[(size_t)i] >> 32);
+      }
     }
   uint32_t* d = nullptr;
   e = cudaMalloc(&d, h.size() * sizeof(uint32_t));
@@ -404,7 +418,7 @@ extern "C" int pty_legacy_random_background(const uint32_t* key, int32_t pos, in
   cudaStream_t st = (cudaStream_t)stream;
   const DrawSize d = draw_size(pos, count);
   const long long total = d.total, segs = d.segs;
-  if (segs > (1ll << kMaxRounds)) return set_error(PTY_ERR_RANGE, "draw too large");
+  if (segs > (1ll << (2 * kLevels))) return set_error(PTY_ERR_RANGE, "draw too large");
   const uint32_t* polys = nullptr;
   if (segs > 1) PTY_TRY(device_jump_polys(&polys));
   // the sequence x[0, total), 624 spare words, the segment windows: the
@@ -423,11 +437,14 @@ extern "C" int pty_legacy_random_background(const uint32_t* key, int32_t pos, in
   int rc = PTY_OK;
   e = cudaMemcpyAsync(d_win, key, kMtN * sizeof(uint32_t), cudaMemcpyHostToDevice, st);
   if (e != cudaSuccess) rc = set_cuda_error(e, "generator state upload");
-  // windows of segments 2^r .. 2^(r+1) - 1: jumps of 2^r segments from 0 .. 2^r - 1
-  for (int r = 0; rc == PTY_OK && (1ll << r) < segs; ++r) {
-    const long long half = 1ll << r;
-    const int jumps = (int)(segs - half < half ? segs - half : half);
-    legacy_jump_kernel<<<jumps, kJumpThreads, 0, st>>>(polys + (size_t)r * kMtN, d_win, 0, (int)half);
+  // radix-4 rounds: windows of segments [4^l, 4^(l+1)) jump 1, 2 or 3 x 4^l
+  // segments from windows [0, 4^l)
+  int level = 0;
+  for (long long nsrc = 1; rc == PTY_OK && nsrc < segs; nsrc *= 4, ++level) {
+    const long long want = segs - nsrc < 3 * nsrc ? segs - nsrc : 3 * nsrc;
+    const long long blocks = ((want + nsrc - 1) / nsrc) * nsrc;       // whole j groups
+    legacy_jump_kernel<<<(unsigned)blocks, kJumpThreads, 0, st>>>(polys + (size_t)level * 3 * kMtN, d_win,
+                                                                 (int)nsrc, segs);
     rc = check_launch("legacy_jump_kernel");
   }
   if (rc == PTY_OK) {
