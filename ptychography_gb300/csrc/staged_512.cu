@@ -14,8 +14,9 @@
 //   3. row launch: inverse row FFT of the scratch rows, scaled, written as the
 //      new wave (with the DM update).
 // The scratch holds stage_frames frames; larger launches run group by group.
-// Each CTA is independent: no cluster barrier, two or three CTAs per SM.  The column launch writes
-// one error partial per CTA: 64 slots per frame (the tile id is 200 + 64).
+// Each CTA is independent: no cluster barrier; three row CTAs or two column
+// CTAs per SM.  The column launch writes one error partial per CTA: 64 slots
+// per frame (the tile id is 200 + 64).
 // Line transforms, slot layouts and the per-pixel operations are those of the
 // 16-CTA tile 116, so results agree with it to FP32 rounding.
 // Replaces the same reference functions as frame_kernels.cu.
@@ -58,9 +59,11 @@ PTY_DEV void load_twiddles(const FrameArgs& g, float2* tw1, float2* tw2) {
 }
 
 // Row launch.  !LAST: input wave -> forward row FFT -> scratch.
-// LAST: scratch -> inverse row FFT -> scaled output wave.
+// LAST: scratch -> inverse row FFT -> scaled output wave.  Three CTAs (24
+// warps) per SM: the DM forms, which also read psi and the exit wave, fit in
+// 80 registers without spills (at their unconstrained 107-109, two CTAs).
 template <int OP, bool LAST>
-__global__ void __launch_bounds__(kNT, 2) staged_rows_kernel(FrameArgs g, int f0) {
+__global__ void __launch_bounds__(kNT, 3) staged_rows_kernel(FrameArgs g, int f0) {
   using T = OpTraits<OP>;
   constexpr float kInv = 1.0f / (float)(kN * kN);
   __shared__ float2 tw1[kN];
