@@ -200,6 +200,12 @@ class ClockSampler:
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
+            # nvidia-smi's start-up (NVML initialisation) must not fall inside
+            # the timed region: wait for its first sample (it stalled a
+            # 3-step timing by ~1 s otherwise)
+            t0 = time.perf_counter()
+            while not self.rows and self.proc.poll() is None and time.perf_counter() - t0 < 10.0:
+                time.sleep(0.01)
         except OSError:
             self.proc = None
         return self
@@ -821,6 +827,8 @@ def main():
     ap.add_argument("--no-nmse", action="store_true")
     ap.add_argument("--no-batch", action="store_true",
                     help="skip the 64-reconstruction batched measurement")
+    ap.add_argument("--warm-steps", type=int, default=2000,
+                    help="training steps of the warm start's network in the time-to-NMSE measurement")
     ap.add_argument("--frame-tile", type=int, default=0,
                     help="force this frame tile (CTAs per frame; see pty_set_frame_tile) for profiling")
     ap.add_argument("--frames", type=int, default=None,
@@ -908,7 +916,7 @@ def main():
     if m1:
         line["era_m1"] = m1
     if not args.no_nmse:
-        line["time_to_nmse"] = time_to_nmse(torch, dev)
+        line["time_to_nmse"] = time_to_nmse(torch, dev, warm_steps=args.warm_steps)
     if args.workload == "c1" and not args.no_batch:
         line["batched"] = batched_rate(dev)
     print(json.dumps(line))
