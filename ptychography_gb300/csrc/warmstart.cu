@@ -355,13 +355,21 @@ __global__ void ws_act_bwd_kernel(long long P, int C, const float* __restrict__ 
   }
 }
 
-// out[c] = sum over r < rows of part[r][c], in row order
-__global__ void ws_sum_rows_kernel(const float* __restrict__ part, int rows, int C, float* __restrict__ out) {
-  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < C; c += gridDim.x * blockDim.x) {
-    float s = 0.f;
-    for (int r = 0; r < rows; ++r) s += part[(size_t)r * C + c];
-    out[c] = s;
+// out[c] = sum over r < rows of part[r][c]: one block per channel, each
+// thread a fixed stride of rows, then a fixed tree (deterministic)
+__global__ void __launch_bounds__(256) ws_sum_rows_kernel(const float* __restrict__ part, int rows, int C,
+                                                          float* __restrict__ out) {
+  __shared__ float red[256];
+  const int c = blockIdx.x;
+  float s = 0.f;
+  for (int r = threadIdx.x; r < rows; r += blockDim.x) s += part[(size_t)r * C + c];
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if ((int)threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+    __syncthreads();
   }
+  if (threadIdx.x == 0) out[c] = red[0];
 }
 
 // weighted squared error of Y [P][2] against T [P][2] with per-pixel weights
@@ -563,7 +571,7 @@ extern "C" int pty_ws_act_bwd(int64_t P, int32_t C, const float* dA, const void*
   ws_act_bwd_kernel<<<(unsigned)blocks, threads, 0, st>>>(P, C, dA, (const bf16*)a, relu, (bf16*)dZ, scratch,
                                                           kActRows);
   PTY_TRY(ws_launched("ws_act_bwd_kernel"));
-  ws_sum_rows_kernel<<<(C + 127) / 128, 128, 0, st>>>(scratch, (int)blocks, C, dbias);
+  ws_sum_rows_kernel<<<C, 256, 0, st>>>(scratch, (int)blocks, C, dbias);
   return ws_launched("ws_sum_rows_kernel");
 }
 
@@ -601,8 +609,9 @@ namespace {
 // x[f][p] = bf16(log(1 + sqrt(I[f][p]) / mean_p sqrt(I[f][p]))) (one block per
 // frame): the logarithm compresses the central peak, which in unit-mean
 // amplitudes reaches ~100, to the range of the rest of the pattern
-__global__ void ws_prep_kernel(long long npix, const float* __restrict__ I, __nv_bfloat16* __restrict__ x) {
-  __shared__ float red[256];
+__global__ void __launch_bounds__(1024) ws_prep_kernel(long long npix, const float* __restrict__ I,
+                                                       __nv_bfloat16* __restrict__ x) {
+  __shared__ float red[1024];
   const float* If = I + (size_t)blockIdx.x * npix;
   __nv_bfloat16* xf = x + (size_t)blockIdx.x * npix;
   float s = 0.f;
@@ -662,7 +671,7 @@ __global__ void ws_exits_kernel(long long nf, long long npix, const float* __res
 
 extern "C" int pty_ws_prep_input(int32_t nf, int64_t npix, const float* I, void* x, void* stream) {
   if (nf < 1 || npix < 1 || !I || !x) return set_error(PTY_ERR_ARG, "bad input-preparation arguments");
-  ws_prep_kernel<<<nf, 256, 0, (cudaStream_t)stream>>>(npix, I, (bf16*)x);
+  ws_prep_kernel<<<nf, 1024, 0, (cudaStream_t)stream>>>(npix, I, (bf16*)x);
   return ws_launched("ws_prep_kernel");
 }
 
