@@ -86,3 +86,14 @@ def test_jump_ahead_matches_numpy(seed, blocks):
                                              got.ctypes.data_as(u32p)))
     np.testing.assert_array_equal(got[1:], want[1:])
     assert got[0] >> 31 == want[0] >> 31            # only its top bit is state
+
+
+def test_jump_rejects_bad_arguments():
+    import ctypes
+    from ptychography_gb300 import _native
+    lib = _native.load()
+    key = np.zeros(624, dtype=np.uint32)
+    out = np.empty(624, dtype=np.uint32)
+    u32p = ctypes.POINTER(ctypes.c_uint32)
+    assert lib.pty_legacy_random_jump(key.ctypes.data_as(u32p), -1, out.ctypes.data_as(u32p)) != 0
+    assert lib.pty_legacy_random_jump(None, 5, out.ctypes.data_as(u32p)) != 0

@@ -1,0 +1,38 @@
+"""Host-side pieces of the learned warm start (no GPU): the simulated objects
+and probes of its training set and the C ABI's argument checks."""
+import numpy as np
+
+from ptychography_gb300 import _native
+from ptychography_gb300 import warmstart as ws
+
+
+def test_random_object_and_probe_ranges():
+    rng = np.random.default_rng(0)
+    O = ws.random_object(rng, 96)
+    a, ph = np.abs(O), np.angle(O)
+    assert O.shape == (96, 96)
+    assert a.min() >= 0.5 - 1e-12 and a.max() <= 1.0 + 1e-12
+    assert ph.min() >= -np.pi / 2 - 1e-12 and ph.max() <= np.pi / 2 + 1e-12
+    P = ws.aperture_probe(64, 20, 3.0, 0.002)
+    y, x = np.mgrid[:64, :64] - 32
+    r = np.sqrt(x ** 2 + y ** 2)
+    assert np.all(np.abs(P[r < 20]) > 0.999)
+    assert np.all(P[r >= 20 + 9] == 0)
+    np.testing.assert_allclose(np.angle(P[32, 32 + 5]), 0.002 * 25)
+
+
+def test_network_layout():
+    # six 3 x 3 convolutions, channels 32-128, (cos, sin) output
+    assert len(ws.LAYERS) == 6 and ws.LAYERS[0][0] == 1 and ws.LAYERS[-1][1] == 2
+    assert max(c for _, c, _, _ in ws.LAYERS) == 128
+    assert [l for _, _, _, l in ws.LAYERS] == [0, 1, 2, 1, 0, 0]
+
+
+def test_c_abi_rejects_bad_arguments_without_a_gpu():
+    lib = _native.load()
+    assert lib.pty_ws_gemm(0, 4, 4, None, 1, 1, None, 1, 1, None, 1, 1, 1, None, None) != 0
+    assert lib.pty_ws_im2col(1, 0, 4, 4, None, None, None) != 0
+    assert lib.pty_ws_pool2(1, 5, 4, 4, None, None, None) != 0        # odd side
+    assert lib.pty_ws_act_bwd_scratch(0, 4) == -1
+    assert lib.pty_ws_act_bwd_scratch(1000, 4) == 4 * 4                 # ceil(1000 / 256) blocks x C
+    assert lib.pty_ws_adam(10, None, None, None, None, None, 1e-3, 0.9, 0.999, 1e-8, 1, None) != 0
