@@ -27,13 +27,17 @@ PTY_DEV float2 exit_wave(const FrameArgs& g, int r0, int r1, int a, int b) {
 }
 
 template <int N1, int OP>
-PTY_DEV float2 frame_input(const FrameArgs& g, int f, int r0, int r1, const float2* psi, int a, int b) {
+PTY_DEV float2 frame_input(const FrameArgs& g, int f, int r0, int r1, float2* psi, int a, int b) {
   if constexpr (OpTraits<OP>::IN_EXIT) {
     return exit_wave<N1>(g, r0, r1, a, b);
   } else if constexpr (OpTraits<OP>::IN_DM) {
-    // dm.py:94-95: e1 = psi - ex0 ; x = ex0 - e1  (= 2 ex0 - psi, rounded as the reference)
+    // dm.py:94-95: e1 = psi - ex0 ; x = ex0 - e1  (= 2 ex0 - psi, rounded as the reference).
+    // e1 replaces psi at this pixel: the output stage (frame_output_line)
+    // needs exactly e1, and one load of it is cheaper there than re-reading
+    // psi and forming the exit wave again; no other thread reads the pixel.
     const float2 ex0 = exit_wave<N1>(g, r0, r1, a, b);
     const float2 e1 = csub(psi[a * N1 + b], ex0);
+    psi[a * N1 + b] = e1;
     return csub(ex0, e1);
   } else if constexpr (OP == OP_BP) {
     // back_projection.py:74-77: mask * sqrt(I) * exp(i angle(fftn(P))), with the
@@ -195,11 +199,9 @@ PTY_DEV void frame_output_line(const FrameArgs& g, int r0, int r1, float2* psi, 
   if constexpr (OpTraits<OP>::IN_DM) {
 #pragma unroll
     for (int j = 0; j < B; ++j) {
-      // dm.py:94-97: psi_new = (psi - ex0) + Pmod(2 ex0 - psi)
-      const int b = t + A * j;
-      const float2 ex0 = exit_wave<N1>(g, r0, r1, a, b);
-      const float2 e1 = csub(psi[a * N1 + b], ex0);
-      v[j] = cadd(e1, v[j]);
+      // dm.py:94-97: psi_new = (psi - ex0) + Pmod(2 ex0 - psi), with psi - ex0
+      // (e1) left in psi by frame_input
+      v[j] = cadd(psi[a * N1 + t + A * j], v[j]);
     }
   }
 #pragma unroll
