@@ -632,6 +632,7 @@ def time_to_nmse(torch, dev, target=1e-3, max_iters=2000, warm_steps=2000, warm_
     warm["training"] = {"steps": warm_steps, "batch": 32, "frames": warm_frames,
                         "data_seconds": round(t1 - t0, 2), "train_seconds": round(t2 - t1, 2),
                         "loss_first_20": float(np.mean(losses[:20])), "loss_last_20": float(np.mean(losses[-20:])),
+                        "input": "back-projection ifftn(sqrt(I) exp(i angle fftn P)) conj(P), (Re, Im)",
                         "target": "object phase under the probe (cos, sin), weights |P|^2",
                         "kernels": "pty_ws_*: im2col + BF16 mma.sync GEMMs, FP32 accumulation"}
     job.close()

@@ -232,14 +232,22 @@ int pty_ws_adam(int64_t n, float* w, void* wb, const float* g, float* m, float* 
 int pty_ws_to_bf16(int64_t n, const float* x, void* y, void* stream);
 int pty_ws_add(int64_t n, const float* a, const float* b, float* out, void* stream);
 /* Data for the network, nf frames of npix pixels:
- *   pty_ws_prep_input: x = bf16(log(1 + sqrt(I) / mean(sqrt(I)))) per frame (I float);
+ *   pty_ws_prep_bp: the network's input from back-projected exit waves bp
+ *     (complex64 [nf][N0][N1]) under the probe P (complex64 [N0][N1]):
+ *     x[f][p] = bf16 of (Re, Im) of s bp conj(P) / (max|P|^2 r), with
+ *     r = sqrt(sum |bp|^2 / sum |P|^2) per frame and s = (-1)^(row + col)
+ *     when checker != 0 (bp made by pty_back_project from the engine-order
+ *     amplitudes and the fftshifted phasors fftshift(exp(i angle(fftn P))),
+ *     which is the back-projection ifftn(sqrt(I) exp(i angle(fftn P))) in
+ *     natural order times (-1)^(row + col)), else 1.  x: bf16 [nf][N0][N1][2];
  *   pty_ws_targets: target[2 i .. 2 i + 1] = (cos, sin) of arg psi[i] (psi
  *     complex64), or with object_phase of arg psi[i] conj(P[i mod npix]);
  *     weight[i] = |P[i mod npix]|^2 wscale;
  *   pty_ws_exits: psi[i] = |P[i mod npix]| (y0 + i y1) / |(y0, y1)|, or with
  *     object_phase P[i mod npix] (y0 + i y1) / |(y0, y1)|: the exit waves with
  *     the predicted phases (y float pairs). */
-int pty_ws_prep_input(int32_t nf, int64_t npix, const float* I, void* x, void* stream);
+int pty_ws_prep_bp(int32_t nf, int32_t N0, int32_t N1, const void* bp, const void* P, int32_t checker,
+                   void* x, void* stream);
 int pty_ws_targets(int32_t nf, int64_t npix, const void* psi, const void* P, int32_t object_phase,
                    float wscale, float* target, float* weight, void* stream);
 int pty_ws_exits(int32_t nf, int64_t npix, const float* y, const void* P, int32_t object_phase,

@@ -82,7 +82,7 @@ SIGNATURES = {
                     ctypes.c_float, ctypes.c_float, ctypes.c_float, c_int32, c_void_p],
     "pty_ws_to_bf16": [c_int64, c_void_p, c_void_p, c_void_p],
     "pty_ws_add": [c_int64, c_void_p, c_void_p, c_void_p, c_void_p],
-    "pty_ws_prep_input": [c_int32, c_int64, c_void_p, c_void_p, c_void_p],
+    "pty_ws_prep_bp": [c_int32, c_int32, c_int32, c_void_p, c_void_p, c_int32, c_void_p, c_void_p],
     "pty_ws_targets": [c_int32, c_int64, c_void_p, c_void_p, c_int32, ctypes.c_float, c_void_p, c_void_p,
                        c_void_p],
     "pty_ws_exits": [c_int32, c_int64, c_void_p, c_void_p, c_int32, c_void_p, c_void_p],

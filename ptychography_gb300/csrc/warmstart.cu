@@ -606,25 +606,47 @@ extern "C" int pty_ws_add(int64_t n, const float* a, const float* b, float* out,
 namespace pty {
 namespace {
 
-// x[f][p] = bf16(log(1 + sqrt(I[f][p]) / mean_p sqrt(I[f][p]))) (one block per
-// frame): the logarithm compresses the central peak, which in unit-mean
-// amplitudes reaches ~100, to the range of the rest of the pattern
-__global__ void __launch_bounds__(1024) ws_prep_kernel(long long npix, const float* __restrict__ I,
-                                                       __nv_bfloat16* __restrict__ x) {
-  __shared__ float red[1024];
-  const float* If = I + (size_t)blockIdx.x * npix;
-  __nv_bfloat16* xf = x + (size_t)blockIdx.x * npix;
-  float s = 0.f;
-  for (long long p = threadIdx.x; p < npix; p += blockDim.x) s += sqrtf(fmaxf(If[p], 0.f));
-  red[threadIdx.x] = s;
+// The network's input from back-projected exit waves bp (one block per frame):
+// z = s bp conj(P) / (max|P|^2 r), r = sqrt(sum |bp|^2 / sum |P|^2) the frame's
+// RMS object amplitude, s = (-1)^(row + col) when `checker` (undoing the
+// modulation that a half-period shift of the far-field product leaves in bp),
+// else 1; x[f][p] = bf16(Re z, Im z).  Inside the probe z is the object up to
+// its scale r; outside it fades with |P|^2.
+__global__ void __launch_bounds__(1024) ws_prep_bp_kernel(int N1, long long npix, const float2* __restrict__ bp,
+                                                          const float2* __restrict__ P, int checker,
+                                                          __nv_bfloat16* __restrict__ x) {
+  __shared__ float red[3][1024];
+  const float2* bf = bp + (size_t)blockIdx.x * npix;
+  __nv_bfloat16* xf = x + (size_t)blockIdx.x * npix * 2;
+  float sb = 0.f, sp = 0.f, mp = 0.f;
+  for (long long p = threadIdx.x; p < npix; p += blockDim.x) {
+    const float2 v = bf[p], q = P[p];
+    const float a = q.x * q.x + q.y * q.y;
+    sb += v.x * v.x + v.y * v.y;
+    sp += a;
+    mp = fmaxf(mp, a);
+  }
+  red[0][threadIdx.x] = sb;
+  red[1][threadIdx.x] = sp;
+  red[2][threadIdx.x] = mp;
   __syncthreads();
   for (int o = blockDim.x / 2; o > 0; o >>= 1) {
-    if ((int)threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+    if ((int)threadIdx.x < o) {
+      red[0][threadIdx.x] += red[0][threadIdx.x + o];
+      red[1][threadIdx.x] += red[1][threadIdx.x + o];
+      red[2][threadIdx.x] = fmaxf(red[2][threadIdx.x], red[2][threadIdx.x + o]);
+    }
     __syncthreads();
   }
-  const float inv = red[0] > 0.f ? (float)npix / red[0] : 0.f;
-  for (long long p = threadIdx.x; p < npix; p += blockDim.x)
-    xf[p] = __float2bfloat16(log1pf(sqrtf(fmaxf(If[p], 0.f)) * inv));
+  const float r = (red[0][0] > 0.f && red[1][0] > 0.f) ? sqrtf(red[0][0] / red[1][0]) : 1.f;
+  const float scale = red[2][0] > 0.f ? 1.f / (red[2][0] * r) : 0.f;
+  for (long long p = threadIdx.x; p < npix; p += blockDim.x) {
+    const long long row = p / N1, col = p - row * N1;
+    const float s = (checker && ((row + col) & 1)) ? -scale : scale;
+    const float2 v = bf[p], q = P[p];
+    xf[2 * p] = __float2bfloat16((v.x * q.x + v.y * q.y) * s);
+    xf[2 * p + 1] = __float2bfloat16((v.y * q.x - v.x * q.y) * s);
+  }
 }
 
 // target[f][p] = (cos, sin) of arg psi[f][p] (object_phase: of arg psi conj(P),
@@ -669,10 +691,13 @@ __global__ void ws_exits_kernel(long long nf, long long npix, const float* __res
 }  // namespace
 }  // namespace pty
 
-extern "C" int pty_ws_prep_input(int32_t nf, int64_t npix, const float* I, void* x, void* stream) {
-  if (nf < 1 || npix < 1 || !I || !x) return set_error(PTY_ERR_ARG, "bad input-preparation arguments");
-  ws_prep_kernel<<<nf, 1024, 0, (cudaStream_t)stream>>>(npix, I, (bf16*)x);
-  return ws_launched("ws_prep_kernel");
+extern "C" int pty_ws_prep_bp(int32_t nf, int32_t N0, int32_t N1, const void* bp, const void* P,
+                              int32_t checker, void* x, void* stream) {
+  if (nf < 1 || N0 < 1 || N1 < 1 || !bp || !P || !x)
+    return set_error(PTY_ERR_ARG, "bad back-projection input arguments");
+  ws_prep_bp_kernel<<<nf, 1024, 0, (cudaStream_t)stream>>>(N1, (long long)N0 * N1, (const float2*)bp,
+                                                           (const float2*)P, checker, (bf16*)x);
+  return ws_launched("ws_prep_bp_kernel");
 }
 
 extern "C" int pty_ws_targets(int32_t nf, int64_t npix, const void* psi, const void* P, int32_t object_phase,

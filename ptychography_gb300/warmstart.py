@@ -1,14 +1,23 @@
 """Learned warm start: a small conv encoder-decoder predicts each frame's
-exit-wave phase from sqrt(I); the predicted exit waves are stitched into an
-initial object (the overlap update, era.py:336-369) from which ERA starts
-instead of from ones (era.py:480-486).  No reference counterpart.
+object phase under the probe from the frame's back-projection; the predicted
+exit waves are stitched into an initial object (the overlap update,
+era.py:336-369) from which ERA starts instead of from ones (era.py:480-486).
+No reference counterpart.
+
+The input is local in the object: the back-projection
+bp = ifftn(sqrt(I) exp(i angle(fftn P))) (Back_projection's exit waves,
+back_projection.py:74-78, with the amplitudes in natural FFT order) gives
+bp conj(P) ~ |P|^2 (1 + i phase / 2 + a defocused twin term) for a weak phase
+object under a probe with a quadratic phase, so 3 x 3 convolutions with a
+receptive field of a few tens of pixels can refine it.  sqrt(I) itself would
+need the whole pattern for every output pixel.
 
 The network (6 layers, 3 x 3 kernels, 32-128 channels, BF16 weights and
 activations, FP32 accumulation) runs forward and backward on the library's
 kernels (``pty_ws_*``: im2col + BF16 tensor-core GEMMs, pooling, upsampling,
 activations, loss, Adam); torch only holds device memory.
 
-    x  = log(1 + sqrt(I) / mean sqrt(I)) (centred)        H x W x 1
+    x  = bp conj(P) / (max|P|^2 r), r the RMS amplitude     H x W x 2  (Re, Im)
     h1 = relu(conv(x))                                    H x W x 32
     h2 = relu(conv(pool(h1)))                             H/2 x W/2 x 64
     h3 = relu(conv(pool(h2)))                             H/4 x W/4 x 128
@@ -24,7 +33,7 @@ from . import _native
 
 # (C_in, C_out, relu, level) of the six convolutions; level = log2 of the
 # downsampling
-LAYERS = ((1, 32, True, 0), (32, 64, True, 1), (64, 128, True, 2),
+LAYERS = ((2, 32, True, 0), (32, 64, True, 1), (64, 128, True, 2),
           (128, 64, True, 1), (64, 32, True, 0), (32, 2, False, 0))
 
 
@@ -218,28 +227,48 @@ class WarmStartNet:
         return parts
 
     # ------------------------------------------------------------ data
-    def prep_input(self, I):
-        """I: (n, H, W) float32 device tensor of centred intensities -> network input."""
+    def input_from_intensities(self, plan_h, I, P, phasors, x=None):
+        """The network input for the frames of a plan (n frames of H x W): the
+        centred intensities I (n, H, W) float32, the probe P (H, W) and
+        phasors = probe_phasors(P) (complex64), all device tensors.  Returns
+        x (n, H, W, 2) bf16 (written into x when given)."""
         torch = _torch()
-        n = I.shape[0]
-        x = torch.empty((n, self.H, self.W, 1), dtype=torch.bfloat16, device=self.dev)
-        _native.check(self.lib.pty_ws_prep_input(n, self.H * self.W, _p(I), _p(x), self._sp()))
+        n, H, W = I.shape[0], self.H, self.W
+        lib, sp = self.lib, self._sp()
+        if x is None:
+            x = torch.empty((n, H, W, 2), dtype=torch.bfloat16, device=self.dev)
+        amp = self._buf("amp", (n, H, W), torch.float32)
+        _native.check(lib.pty_amp_from_intensity(plan_h, _p(I), 0, _p(amp), sp))
+        bp = self._buf("bp", (n, H, W), torch.complex64)
+        _native.check(lib.pty_back_project(plan_h, _p(amp), None, _p(phasors), _p(bp), sp))
+        _native.check(lib.pty_ws_prep_bp(n, H, W, _p(bp), _p(P), 1, _p(x), sp))
         return x
 
-    def predict_exits(self, I, P, batch=64):
-        """Exit waves |P| exp(i phase) with the predicted phases, for centred
-        intensities I (n, H, W) float32 on the device and the probe P (H, W)
-        complex64 on the device."""
+    def predict_exits(self, I, P, plan_h, batch=64):
+        """Exit waves P exp(i phase) (or |P| exp(i phase)) with the predicted
+        phases, for the centred intensities I (n, H, W) float32 of the plan's
+        frames and the probe P (H, W) complex64, both on the device."""
         torch = _torch()
         n = I.shape[0]
+        phasors = probe_phasors(P.cpu().numpy(), self.dev)
+        x = self.input_from_intensities(plan_h, I, P, phasors)
         psi = torch.empty((n, self.H, self.W), dtype=torch.complex64, device=self.dev)
         for s in range(0, n, batch):
             e = min(n, s + batch)
-            x = self.prep_input(I[s:e].contiguous())
-            y = self.forward(x)
+            y = self.forward(x[s:e])
             _native.check(self.lib.pty_ws_exits(e - s, self.H * self.W, _p(y), _p(P),
                                                 int(self.object_phase), _p(psi[s:]), self._sp()))
         return psi
+
+
+def probe_phasors(P, device):
+    """fftshift(exp(i angle(fftn(P)))) as a complex64 device tensor.
+    pty_back_project uses the amplitudes in the reference's centred order;
+    with these shifted phasors its output is the back-projection with natural
+    order amplitudes times (-1)^(row + col), which pty_ws_prep_bp undoes."""
+    torch = _torch()
+    ph = np.fft.fftshift(np.exp(1j * np.angle(np.fft.fftn(np.asarray(P, np.complex128)))))
+    return torch.from_numpy(np.ascontiguousarray(ph.astype(np.complex64))).to(device)
 
 
 # ---------------------------------------------------------------- training data
@@ -284,14 +313,15 @@ class _FramePlan:
 def make_training_set(net, n_frames, seed=0, frames_per_object=8, batch=32, pad=64):
     """Frames of random objects (random_object) under random probes (aperture
     radius 24-40 px, edge 4 px, quadratic phase 0.001-0.004 rad/px^2) at
-    random positions: the network input (normalised sqrt of the centred
-    intensities), the targets (cos, sin of the exit-wave phase) and weights
-    |P|^2 scaled so that `batch` frames sum to 1.  All on the device."""
+    random positions: the network input (the frames' back-projections,
+    input_from_intensities), the targets (cos, sin of the object phase under
+    the probe) and weights |P|^2 scaled so that `batch` frames sum to 1.  All
+    on the device."""
     torch = _torch()
     N, dev, lib = net.H, net.dev, net.lib
     rng = np.random.default_rng(seed)
     n = (n_frames // frames_per_object) * frames_per_object
-    x = torch.empty((n, N, N, 1), dtype=torch.bfloat16, device=dev)
+    x = torch.empty((n, N, N, LAYERS[0][0]), dtype=torch.bfloat16, device=dev)
     t = torch.empty((n, N, N, 2), dtype=torch.float32, device=dev)
     w = torch.empty((n, N, N), dtype=torch.float32, device=dev)
     k = frames_per_object
@@ -310,7 +340,7 @@ def make_training_set(net, n_frames, seed=0, frames_per_object=8, batch=32, pad=
         try:
             _native.check(lib.pty_intensities(plan.h, _p(Od), _p(Pd), _p(I), sp))
             _native.check(lib.pty_make_exits(plan.h, _p(Od), _p(Pd), _p(psi), sp))
-            _native.check(lib.pty_ws_prep_input(k, N * N, _p(I), _p(x[s:]), sp))
+            net.input_from_intensities(plan.h, I, Pd, probe_phasors(P, dev), x[s:s + k])
             wscale = 1.0 / (batch * float(np.sum(np.abs(P) ** 2)))
             _native.check(lib.pty_ws_targets(k, N * N, _p(psi), _p(Pd), int(net.object_phase), wscale,
                                              _p(t[s:]), _p(w[s:]), sp))
@@ -343,7 +373,7 @@ def warm_start_object(net, I_dev, P_dev, plan_h, U, V, alpha=1e-10, heat=None):
     (psup_O, era.py:336-369) with the probe P_dev on the plan's U x V grid.
     Returns a complex64 (U, V) device tensor."""
     torch = _torch()
-    psi = net.predict_exits(I_dev, P_dev)
+    psi = net.predict_exits(I_dev, P_dev, plan_h)
     O = torch.empty((U, V), dtype=torch.complex64, device=net.dev)
     if heat is None:
         heat = torch.empty((U, V), dtype=torch.float64, device=net.dev)

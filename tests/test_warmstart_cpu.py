@@ -23,7 +23,8 @@ def test_random_object_and_probe_ranges():
 
 def test_network_layout():
     # six 3 x 3 convolutions, channels 32-128, (cos, sin) output
-    assert len(ws.LAYERS) == 6 and ws.LAYERS[0][0] == 1 and ws.LAYERS[-1][1] == 2
+    # input: (Re, Im) of the back-projected object estimate
+    assert len(ws.LAYERS) == 6 and ws.LAYERS[0][0] == 2 and ws.LAYERS[-1][1] == 2
     assert max(c for _, c, _, _ in ws.LAYERS) == 128
     assert [l for _, _, _, l in ws.LAYERS] == [0, 1, 2, 1, 0, 0]
 
@@ -36,3 +37,4 @@ def test_c_abi_rejects_bad_arguments_without_a_gpu():
     assert lib.pty_ws_act_bwd_scratch(0, 4) == -1
     assert lib.pty_ws_act_bwd_scratch(1000, 4) == 4 * 4                 # ceil(1000 / 256) blocks x C
     assert lib.pty_ws_adam(10, None, None, None, None, None, 1e-3, 0.9, 0.999, 1e-8, 1, None) != 0
+    assert lib.pty_ws_prep_bp(1, 0, 8, None, None, 1, None, None) != 0
