@@ -239,7 +239,8 @@ int pty_ws_add(int64_t n, const float* a, const float* b, float* out, void* stre
  *     when checker != 0 (bp made by pty_back_project from the engine-order
  *     amplitudes and the fftshifted phasors fftshift(exp(i angle(fftn P))),
  *     which is the back-projection ifftn(sqrt(I) exp(i angle(fftn P))) in
- *     natural order times (-1)^(row + col)), else 1.  x: bf16 [nf][N0][N1][2];
+ *     natural order times (-1)^(row + col); even sides only, else
+ *     PTY_ERR_SHAPE), else 1.  x: bf16 [nf][N0][N1][2];
  *   pty_ws_targets: target[2 i .. 2 i + 1] = (cos, sin) of arg psi[i] (psi
  *     complex64), or with object_phase of arg psi[i] conj(P[i mod npix]);
  *     weight[i] = |P[i mod npix]|^2 wscale;

@@ -3,7 +3,7 @@
 // its forward pass, backward pass and Adam step.  No reference counterpart:
 // the reference starts ERA from ones (ptychography/era.py:480-486); the warm
 // start replaces that initial object by one stitched from per-frame phases
-// this network predicts from sqrt(I).
+// this network predicts from each frame's back-projection.
 //
 // Layout: activations NHWC (pixel-major, channels contiguous), BF16 between
 // layers; GEMM outputs FP32.  A convolution with C_in inputs is
@@ -695,6 +695,8 @@ extern "C" int pty_ws_prep_bp(int32_t nf, int32_t N0, int32_t N1, const void* bp
                               int32_t checker, void* x, void* stream) {
   if (nf < 1 || N0 < 1 || N1 < 1 || !bp || !P || !x)
     return set_error(PTY_ERR_ARG, "bad back-projection input arguments");
+  // the (-1)^(row + col) correction is the half-period shift only for even sides
+  if (checker && ((N0 | N1) & 1)) return set_error(PTY_ERR_SHAPE, "checker sign needs even frame sides");
   ws_prep_bp_kernel<<<nf, 1024, 0, (cudaStream_t)stream>>>(N1, (long long)N0 * N1, (const float2*)bp,
                                                            (const float2*)P, checker, (bf16*)x);
   return ws_launched("ws_prep_bp_kernel");

@@ -1,5 +1,7 @@
 """Host-side pieces of the learned warm start (no GPU): the simulated objects
 and probes of its training set and the C ABI's argument checks."""
+import ctypes
+
 import numpy as np
 
 from ptychography_gb300 import _native
@@ -38,3 +40,6 @@ def test_c_abi_rejects_bad_arguments_without_a_gpu():
     assert lib.pty_ws_act_bwd_scratch(1000, 4) == 4 * 4                 # ceil(1000 / 256) blocks x C
     assert lib.pty_ws_adam(10, None, None, None, None, None, 1e-3, 0.9, 0.999, 1e-8, 1, None) != 0
     assert lib.pty_ws_prep_bp(1, 0, 8, None, None, 1, None, None) != 0
+    one = ctypes.c_void_p(16)                                          # never dereferenced: rejected first
+    assert lib.pty_ws_prep_bp(1, 8, 7, one, one, 1, one, None) != 0     # odd side with the sign correction
+    assert b"even" in lib.pty_last_error()
