@@ -371,7 +371,8 @@ def warm_start_object(net, I_dev, P_dev, plan_h, U, V, alpha=1e-10, heat=None):
     """The initial object for ERA: the network's exit waves for the centred
     intensities I_dev (n, N, N) float32, stitched by the overlap update
     (psup_O, era.py:336-369) with the probe P_dev on the plan's U x V grid.
-    Returns a complex64 (U, V) device tensor."""
+    plan_h must be a plan of exactly these n frames of N x N (its kernels
+    read n frames of I_dev).  Returns a complex64 (U, V) device tensor."""
     torch = _torch()
     psi = net.predict_exits(I_dev, P_dev, plan_h)
     O = torch.empty((U, V), dtype=torch.complex64, device=net.dev)
