@@ -77,6 +77,10 @@ typedef struct {
  * preamble(), ptychography/era.py:435-548 (R must already be shifted). */
 int pty_plan_create(const pty_geometry* geom, const int64_t* R_host, pty_plan** plan_out);
 int pty_plan_destroy(pty_plan* plan);
+/* The geometry a plan was created with (host memory out; no device work).
+ * No reference counterpart: callers that size buffers for a plan's entry
+ * points (which write n_frames frames) check their arrays against it. */
+int pty_plan_geometry(const pty_plan* plan, pty_geometry* geom_out);
 
 /* Whole reconstructions.  pty_era replaces ERA, ptychography/era.py:13-332;
  * pty_dm replaces DM, ptychography/dm.py:13-333.  *heatmap_valid (host) is
@@ -158,10 +162,15 @@ int pty_amp_and_norm(pty_plan* plan, const void* I, int32_t is_double, const uin
  * live in fixed arrays compiled into the library (8 MiB + 128 KiB on every
  * GPU that loads it, until the process exits); sizes beyond them --
  * N0 * N1 > 65536 or n_frames > 16384 -- are rejected with PTY_ERR_RANGE.
- * The first call on a device looks those arrays up for that device; make it
- * before any stream capture.  All calls share the arrays, so calls whose GPU
- * work overlaps (other streams, other host threads) race; nothing in them
- * needs clearing between calls, as each call writes every slot it reads. */
+ * The offsets go to the device as kernel parameters of small copy launches
+ * (one per 2048 frames), so the call makes no memcpy and does not
+ * synchronise the host.  The first call on a device looks up that device's
+ * copies of the arrays (cudaGetSymbolAddress, serialised across host
+ * threads); make that first call on each device before any stream capture
+ * begins.  All calls on one GPU share its arrays, so calls whose GPU work
+ * overlaps (other streams, other host threads on the same GPU) race; nothing
+ * in them needs clearing between calls, as each call writes every slot it
+ * reads. */
 int pty_psup_P_noalloc(const pty_geometry* geom, const int64_t* R_host, const void* psi,
                        const void* O, double* O_heatmap, int32_t recompute_heatmap, double alpha,
                        void* P_out, void* stream);

@@ -35,6 +35,7 @@ class Options(ctypes.Structure):
 SIGNATURES = {
     "pty_plan_create": [ctypes.POINTER(Geometry), ctypes.POINTER(c_int64), ctypes.POINTER(c_void_p)],
     "pty_plan_destroy": [c_void_p],
+    "pty_plan_geometry": [c_void_p, ctypes.POINTER(Geometry)],
     "pty_era": [c_void_p, ctypes.POINTER(Buffers), ctypes.POINTER(Options), c_int32,
                 ctypes.POINTER(c_int32), c_void_p],
     "pty_dm": [c_void_p, ctypes.POINTER(Buffers), ctypes.POINTER(Options), c_int32,
@@ -143,3 +144,10 @@ def check(rc):
 
 class PtyValueError(PtyError, ValueError):
     """Bad argument, unsupported frame shape or scan window outside the object."""
+
+
+def plan_geometry(plan_h):
+    """The Geometry a plan handle was created with."""
+    g = Geometry()
+    check(load().pty_plan_geometry(plan_h, ctypes.byref(g)))
+    return g

@@ -141,6 +141,16 @@ extern "C" int pty_plan_destroy(pty_plan* p) {
   return PTY_OK;
 }
 
+extern "C" int pty_plan_geometry(const pty_plan* p, pty_geometry* g) {
+  if (!p || !g) return set_error(PTY_ERR_ARG, "pty_plan_geometry: null argument");
+  g->n_frames = p->n;
+  g->N0 = p->N0;
+  g->N1 = p->N1;
+  g->U = p->U;
+  g->V = p->V;
+  return PTY_OK;
+}
+
 extern "C" int pty_plan_create(const pty_geometry* g, const int64_t* R_host, pty_plan** out) {
   if (!g || !R_host || !out) return set_error(PTY_ERR_ARG, "null argument");
   *out = nullptr;

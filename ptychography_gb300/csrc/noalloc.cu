@@ -12,7 +12,14 @@
 // Those arrays live on every GPU that loads the library, for the life of the
 // process: 8 MiB of partial sums (8 chunks x 65536 pixels x 2 float2) plus
 // 128 KiB of scan offsets (16384 frames x 2 int32).
+//
+// The offsets reach the device as kernel parameters (batches of
+// kOffsetsPerLaunch frames, copied by a small kernel into g_noalloc_R): the
+// launch copies its parameters when it is enqueued, so the call needs no host
+// staging buffer, no pageable memcpy and no host synchronisation.
 #include <cuda_runtime.h>
+
+#include <mutex>
 
 #include "../../include/ptycho_gb300.h"
 #include "engine.h"
@@ -30,8 +37,19 @@ static __device__ __align__(256) float2 g_noalloc_scratch[kNoAllocElems];
 // Scan offsets of the current call, int32 [n][2].
 static __device__ __align__(256) int g_noalloc_R[2 * kNoAllocMaxFrames];
 
-// Host-side staging of the offsets (converted to int32 before the copy).
-static int g_R_host[2 * kNoAllocMaxFrames];
+// One launch's share of the offsets, passed by value (16 KiB of parameters,
+// inside the 32 KiB kernel-parameter limit of sm_70 and later).
+constexpr int kOffsetsPerLaunch = 2048;
+struct OffsetsBatch {
+  int first;                       // first frame of the batch
+  int count;                       // frames in the batch
+  int r[2 * kOffsetsPerLaunch];    // (r0, r1) per frame
+};
+
+__global__ void noalloc_stage_offsets_kernel(const OffsetsBatch b) {
+  for (int i = threadIdx.x; i < 2 * b.count; i += blockDim.x)
+    g_noalloc_R[2 * b.first + i] = b.r[i];
+}
 
 constexpr int kMaxDevices = 64;
 struct NoAllocSymbols {
@@ -39,14 +57,19 @@ struct NoAllocSymbols {
   int* R = nullptr;
 };
 static NoAllocSymbols g_symbols[kMaxDevices];
+static std::mutex g_symbols_mutex;
 
-// Addresses of the fixed arrays on the current device, looked up once per device.
+// Addresses of the fixed arrays on the current device, looked up once per
+// device (under a lock, so host threads driving different GPUs may call at
+// the same time).  In host code the arrays' names are host-side stand-ins,
+// not device addresses: only these looked-up pointers may go to a kernel.
 static int symbols_on_current_device(NoAllocSymbols* out) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return set_cuda_error(e, "pty_psup_P_noalloc: cudaGetDevice");
   if (dev < 0 || dev >= kMaxDevices)
     return set_error(PTY_ERR_ARG, "pty_psup_P_noalloc: device index too large");
+  std::lock_guard<std::mutex> lock(g_symbols_mutex);
   NoAllocSymbols& s = g_symbols[dev];
   if (!s.scratch || !s.R) {
     void* p = nullptr;
@@ -85,17 +108,20 @@ extern "C" int pty_psup_P_noalloc(const pty_geometry* geom, const int64_t* R_hos
     if (r0 > 0 || r1 > 0 || -r0 + N0 > U || -r1 + N1 > V)
       return set_error(PTY_ERR_RANGE,
                        "pty_psup_P_noalloc: scan position places the probe window outside the object");
-    g_R_host[2 * f] = (int)r0;
-    g_R_host[2 * f + 1] = (int)r1;
   }
   NoAllocSymbols sym;
   int rc = symbols_on_current_device(&sym);
   if (rc != PTY_OK) return rc;
   cudaStream_t st = (cudaStream_t)stream;
-  // pageable source: the copy has read g_R_host before this call returns
-  cudaError_t e = cudaMemcpyAsync(sym.R, g_R_host, sizeof(int) * 2 * (size_t)n,
-                                  cudaMemcpyHostToDevice, st);
-  if (e != cudaSuccess) return set_cuda_error(e, "pty_psup_P_noalloc: offsets copy");
+  OffsetsBatch b;
+  for (int f0 = 0; f0 < n; f0 += kOffsetsPerLaunch) {
+    b.first = f0;
+    b.count = n - f0 < kOffsetsPerLaunch ? n - f0 : kOffsetsPerLaunch;
+    for (int i = 0; i < 2 * b.count; ++i) b.r[i] = (int)R_host[2 * f0 + i];
+    noalloc_stage_offsets_kernel<<<1, 256, 0, st>>>(b);
+    rc = check_launch("noalloc_stage_offsets_kernel");
+    if (rc != PTY_OK) return rc;
+  }
   const int K = n < kNoAllocChunks ? n : kNoAllocChunks;
   float2* part_num = sym.scratch;
   float2* part_den = sym.scratch + (size_t)kNoAllocChunks * kNoAllocMaxPixels;

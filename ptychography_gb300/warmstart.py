@@ -234,6 +234,11 @@ class WarmStartNet:
         x (n, H, W, 2) bf16 (written into x when given)."""
         torch = _torch()
         n, H, W = I.shape[0], self.H, self.W
+        g = _native.plan_geometry(plan_h)
+        # the plan's kernels write all of its frames: the buffers below hold n
+        if (g.n_frames, g.N0, g.N1) != (n, H, W):
+            raise ValueError("the plan is for %d frames of %d x %d, the intensities hold %s"
+                             % (g.n_frames, g.N0, g.N1, tuple(I.shape)))
         lib, sp = self.lib, self._sp()
         if x is None:
             x = torch.empty((n, H, W, 2), dtype=torch.bfloat16, device=self.dev)
@@ -372,8 +377,12 @@ def warm_start_object(net, I_dev, P_dev, plan_h, U, V, alpha=1e-10, heat=None):
     intensities I_dev (n, N, N) float32, stitched by the overlap update
     (psup_O, era.py:336-369) with the probe P_dev on the plan's U x V grid.
     plan_h must be a plan of exactly these n frames of N x N (its kernels
-    read n frames of I_dev).  Returns a complex64 (U, V) device tensor."""
+    read n frames of I_dev; a mismatch raises ValueError).  Returns a
+    complex64 (U, V) device tensor."""
     torch = _torch()
+    g = _native.plan_geometry(plan_h)
+    if (g.U, g.V) != (U, V):
+        raise ValueError("the plan's object is %d x %d, not %d x %d" % (g.U, g.V, U, V))
     psi = net.predict_exits(I_dev, P_dev, plan_h)
     O = torch.empty((U, V), dtype=torch.complex64, device=net.dev)
     if heat is None:

@@ -1,9 +1,9 @@
 """Generate the golden fixtures from the reference implementation itself.
 
-Run from the repository root in a checkout where the reference is mounted
-(default ``/root/reference``; override with ``PTY_REFERENCE_ROOT``)::
+Run from the repository root with ``PTY_REFERENCE_ROOT`` naming the root of a
+reference checkout (the directory holding ``ptychography/era.py``)::
 
-    python tests/golden/make_golden.py
+    PTY_REFERENCE_ROOT=<reference checkout> python tests/golden/make_golden.py
 
 It loads the reference's own ``era``/``dm``/``forward_models`` through
 ``reference_loader`` (Python-2 spellings rewritten at load time, single-rank MPI)

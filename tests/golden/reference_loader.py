@@ -25,7 +25,16 @@ import re
 import sys
 import types
 
-REF_ROOT = os.environ.get("PTY_REFERENCE_ROOT", "/root/reference")
+
+def _reference_root():
+    root = os.environ.get("PTY_REFERENCE_ROOT")
+    if not root:
+        raise RuntimeError("set PTY_REFERENCE_ROOT to the root of a reference checkout "
+                           "(the directory holding ptychography/era.py)")
+    return root
+
+
+REF_ROOT = _reference_root()
 PKG_DIR = os.path.join(REF_ROOT, "ptychography")
 
 
