@@ -15,8 +15,42 @@
 #define PTY_HD __host__ __device__ __forceinline__
 
 // ---------------------------------------------------------------- complex
+// Complex additions, subtractions and real scalings issue as one packed
+// FP32x2 instruction (add / sub / mul .rn.f32x2, sm_100 and later) instead of
+// two scalar ones: the FFT butterflies are mostly such operations and the
+// frame kernels are bound by instruction issue (measured on the 256^2 Pmod_7
+// kernel: 18 % fewer warp instructions, 4 % less time).  Each lane rounds as
+// the scalar add.rn / sub.rn / mul.rn does; the compiler can no longer
+// contract a packed product into a following addition (one FMA), so results
+// may differ from the scalar forms (PTY_PACKED_F32X2=0) in the last bit.
+#ifndef PTY_PACKED_F32X2
+#define PTY_PACKED_F32X2 1
+#endif
+#if PTY_PACKED_F32X2
+PTY_DEV unsigned long long f2_pack(float2 a) {
+  unsigned long long r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a.x), "f"(a.y));
+  return r;
+}
+PTY_DEV float2 f2_unpack(unsigned long long r) {
+  float2 a;
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(a.x), "=f"(a.y) : "l"(r));
+  return a;
+}
+PTY_DEV float2 cadd(float2 a, float2 b) {
+  unsigned long long r;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(f2_pack(a)), "l"(f2_pack(b)));
+  return f2_unpack(r);
+}
+PTY_DEV float2 csub(float2 a, float2 b) {
+  unsigned long long r;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(f2_pack(a)), "l"(f2_pack(b)));
+  return f2_unpack(r);
+}
+#else
 PTY_DEV float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
 PTY_DEV float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+#endif
 PTY_DEV float2 cmul(float2 a, float2 b) {
   return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }
@@ -24,7 +58,15 @@ PTY_DEV float2 cmul(float2 a, float2 b) {
 PTY_DEV float2 cmulc(float2 a, float2 b) {
   return make_float2(a.x * b.x + a.y * b.y, a.y * b.x - a.x * b.y);
 }
+#if PTY_PACKED_F32X2
+PTY_DEV float2 cscale(float2 a, float s) {
+  unsigned long long r;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(f2_pack(a)), "l"(f2_pack(make_float2(s, s))));
+  return f2_unpack(r);
+}
+#else
 PTY_DEV float2 cscale(float2 a, float s) { return make_float2(a.x * s, a.y * s); }
+#endif
 PTY_DEV float cabs2(float2 a) { return a.x * a.x + a.y * a.y; }
 // multiply by W or conj(W) depending on the transform direction
 template <int DIR>
