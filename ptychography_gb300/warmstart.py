@@ -148,6 +148,40 @@ class WarmStartNet:
         h5 = self._conv_fwd(4, u4, B, H, W, skip=h1)
         return self._conv_fwd(5, h5, B, H, W, last=True)
 
+    def _conv_tc(self, i, x, B, H, W, skip=None):
+        """Layer i on the tensor-core implicit-GEMM convolution (bias,
+        activation and skip fused): x (B, H, W, C_in) bf16 -> (B, H, W, C_out) bf16."""
+        torch = _torch()
+        cin, cout, relu, _ = LAYERS[i]
+        out = self._buf("t%d" % i, (B, H, W, cout), torch.bfloat16)
+        _native.check(self.lib.pty_ws_conv3x3_tc(B, H, W, cin, cout, _p(x), _p(self.wb[i]), _p(self.b[i]),
+                                                 int(relu), _p(skip), _p(out), self._sp()))
+        return out
+
+    def forward_infer(self, x):
+        """The forward pass for inference: layers 1-4 (the network's bulk,
+        32-128 channels) on the tensor-core convolution, which writes no
+        im2col buffer and keeps nothing for a backward pass; the 2-channel
+        first and last layers on the im2col path.  Same result as forward()
+        up to FP32 summation order."""
+        torch = _torch()
+        B, H, W = x.shape[0], self.H, self.W
+        lib, sp = self.lib, self._sp()
+        h1 = self._conv_fwd(0, x, B, H, W)
+        p1 = self._buf("p1", (B, H // 2, W // 2, 32), torch.bfloat16)
+        _native.check(lib.pty_ws_pool2(B, H, W, 32, _p(h1), _p(p1), sp))
+        h2 = self._conv_tc(1, p1, B, H // 2, W // 2)
+        p2 = self._buf("p2", (B, H // 4, W // 4, 64), torch.bfloat16)
+        _native.check(lib.pty_ws_pool2(B, H // 2, W // 2, 64, _p(h2), _p(p2), sp))
+        h3 = self._conv_tc(2, p2, B, H // 4, W // 4)
+        u3 = self._buf("u3", (B, H // 2, W // 2, 128), torch.bfloat16)
+        _native.check(lib.pty_ws_up2(B, H // 4, W // 4, 128, _p(h3), _p(u3), sp))
+        h4 = self._conv_tc(3, u3, B, H // 2, W // 2, skip=h2)
+        u4 = self._buf("u4", (B, H, W, 64), torch.bfloat16)
+        _native.check(lib.pty_ws_up2(B, H // 2, W // 2, 64, _p(h4), _p(u4), sp))
+        h5 = self._conv_tc(4, u4, B, H, W, skip=h1)
+        return self._conv_fwd(5, h5, B, H, W, last=True)
+
     def _conv_bwd(self, i, dA, B, H, W, need_dx):
         """dA: gradient (FP32, B x H x W x C_out) at layer i's activation; sets
         the layer's weight and bias gradients, returns the input gradient."""
@@ -249,7 +283,7 @@ class WarmStartNet:
         _native.check(lib.pty_ws_prep_bp(n, H, W, _p(bp), _p(P), 1, _p(x), sp))
         return x
 
-    def predict_exits(self, I, P, plan_h, batch=64):
+    def predict_exits(self, I, P, plan_h, batch=64, tensor_cores=True):
         """Exit waves P exp(i phase) (or |P| exp(i phase)) with the predicted
         phases, for the centred intensities I (n, H, W) float32 of the plan's
         frames and the probe P (H, W) complex64, both on the device."""
@@ -260,7 +294,7 @@ class WarmStartNet:
         psi = torch.empty((n, self.H, self.W), dtype=torch.complex64, device=self.dev)
         for s in range(0, n, batch):
             e = min(n, s + batch)
-            y = self.forward(x[s:e])
+            y = self.forward_infer(x[s:e]) if tensor_cores else self.forward(x[s:e])
             _native.check(self.lib.pty_ws_exits(e - s, self.H * self.W, _p(y), _p(P),
                                                 int(self.object_phase), _p(psi[s:]), self._sp()))
         return psi
