@@ -273,13 +273,10 @@ int pty_ws_exits(int32_t nf, int64_t npix, const float* y, const void* P, int32_
  * summation order.  C_in = 32 or a multiple of 64, C_out a multiple of 32 up
  * to 128, W dividing 128 (H a multiple of 128 / W) or a multiple of 128;
  * arrays 16-byte aligned; others are PTY_ERR_UNSUPPORTED.  Its mbarrier waits
- * are bounded: pty_ws_conv_tc_status (which synchronises the device) reports
- * and clears a wait that ran out (*timed_out = 1; the outputs are then
- * invalid). */
+ * are bounded (see pty_timeout_status). */
 int pty_ws_conv3x3_tc(int32_t B, int32_t H, int32_t W, int32_t Cin, int32_t Cout, const void* X,
                       const void* Wt, const float* bias, int32_t relu, const void* skip, void* out,
                       void* stream);
-int pty_ws_conv_tc_status(int32_t* timed_out);
 
 /* 1 if the frame shape N0 x N1 has a fused FFT kernel. */
 int pty_shape_supported(int32_t N0, int32_t N1);
@@ -311,6 +308,14 @@ int pty_frame_tile_candidates(int32_t N0, int32_t N1, int32_t* tiles, int32_t ca
 int pty_get_frame_tile(int32_t N0, int32_t N1, int32_t family, int32_t* tile);
 int pty_set_frame_tile(int32_t N0, int32_t N1, int32_t family, int32_t tile);
 const char* pty_last_error(void);
+/* Kernels that wait on TMA copies or tensor-core work through mbarriers
+ * (pty_ws_conv3x3_tc, the staged 512 x 512 frame tile) bound every wait; one
+ * that runs out sets a per-device flag, finishes its copies in flight and
+ * returns, leaving its outputs invalid.  This reads the flag of the current
+ * device into *timed_out (1: a wait ran out since the last call) and clears
+ * it; it synchronises the calling thread with the device.  No reference
+ * counterpart. */
+int pty_timeout_status(int32_t* timed_out);
 int pty_version(void);
 /* Kernels this library has launched in the process so far (direct launches
  * plus the kernel nodes of replayed CUDA graphs).  No reference counterpart:

@@ -89,7 +89,7 @@ SIGNATURES = {
     "pty_ws_exits": [c_int32, c_int64, c_void_p, c_void_p, c_int32, c_void_p, c_void_p],
     "pty_ws_conv3x3_tc": [c_int32, c_int32, c_int32, c_int32, c_int32, c_void_p, c_void_p, c_void_p,
                           c_int32, c_void_p, c_void_p, c_void_p],
-    "pty_ws_conv_tc_status": [ctypes.POINTER(c_int32)],
+    "pty_timeout_status": [ctypes.POINTER(c_int32)],
     "pty_shape_supported": [c_int32, c_int32],
     "pty_frame_tile_candidates": [c_int32, c_int32, ctypes.POINTER(c_int32), c_int32,
                                   ctypes.POINTER(c_int32)],

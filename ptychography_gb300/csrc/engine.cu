@@ -9,6 +9,7 @@
 // are written to device arrays.
 #include <atomic>
 #include <cmath>
+#include <mutex>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -32,6 +33,42 @@ int set_cuda_error(cudaError_t e, const char* where) {
 static std::atomic<long long> g_launches{0};
 void count_launches(long long k) { g_launches += k; }
 long long launch_total() { return g_launches.load(); }
+
+// One int per GPU, set by a kernel whose bounded wait ran out (the TMA-staged
+// and tensor-core kernels).  Allocated before any stream capture: by
+// pty_plan_create, or by the first call of an entry point that uses it.
+static int* g_timeout_flag[64] = {};
+static std::mutex g_timeout_mutex;
+int device_timeout_flag(int** out) {
+  int dev = 0;
+  PTY_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) return set_error(PTY_ERR_ARG, "device index too large");
+  std::lock_guard<std::mutex> lock(g_timeout_mutex);
+  if (!g_timeout_flag[dev]) {
+    void* q = nullptr;
+    PTY_CUDA(cudaMalloc(&q, sizeof(int)));
+    PTY_CUDA(cudaMemset(q, 0, sizeof(int)));
+    g_timeout_flag[dev] = static_cast<int*>(q);
+  }
+  *out = g_timeout_flag[dev];
+  return PTY_OK;
+}
+
+static PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
+static std::once_flag g_encode_once;
+int tensor_map_encoder(PFN_cuTensorMapEncodeTiled_v12000* out) {
+  std::call_once(g_encode_once, [] {
+    void* fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      g_encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+  });
+  if (!g_encode) return set_error(PTY_ERR_CUDA, "cuTensorMapEncodeTiled is not available");
+  *out = g_encode;
+  return PTY_OK;
+}
 
 int check_launch(const char* where) {
   cudaError_t e = cudaGetLastError();
@@ -66,6 +103,7 @@ struct pty_plan {
   float2* d_stage = nullptr;     // frame scratch of a staged tile
   uint8_t* d_mask_blk = nullptr; // the mask in the staged tile's column-block order
   int stage_frames = 0;
+  int* d_timeout = nullptr;      // the device's timeout flag (not owned)
   int tile[2] = {1, 1};          // CTAs per frame of the fused frame kernels, per op family
   int eslots = 1;                // error-partial slots per frame (the larger family tile)
   int ndn = 304;                 // diffnorm blocks per array (two per SM)
@@ -127,6 +165,17 @@ extern "C" int64_t pty_launch_count(void) { return (int64_t)launch_total(); }
 
 extern "C" const char* pty_last_error(void) { return g_last_error.c_str(); }
 
+extern "C" int pty_timeout_status(int32_t* timed_out) {
+  if (!timed_out) return set_error(PTY_ERR_ARG, "pty_timeout_status: null argument");
+  int* flag = nullptr;
+  PTY_TRY(device_timeout_flag(&flag));
+  int h = 0;
+  PTY_CUDA(cudaMemcpy(&h, flag, sizeof(int), cudaMemcpyDeviceToHost));
+  if (h) PTY_CUDA(cudaMemset(flag, 0, sizeof(int)));
+  *timed_out = h;
+  return PTY_OK;
+}
+
 extern "C" int pty_plan_destroy(pty_plan* p) {
   if (!p) return PTY_OK;
   for (void* a : p->allocs) cudaFree(a);
@@ -166,8 +215,11 @@ extern "C" int pty_plan_create(const pty_geometry* g, const int64_t* R_host, pty
     R[2 * f] = (int)r0;
     R[2 * f + 1] = (int)r1;
   }
+  int* timeout_flag = nullptr;
+  PTY_TRY(device_timeout_flag(&timeout_flag));
   pty_plan* p = new pty_plan();
   p->n = n; p->N0 = N0; p->N1 = N1; p->U = U; p->V = V;
+  p->d_timeout = timeout_flag;
   static std::atomic<long long> next_serial{1};
   p->serial = next_serial++;
   int rc = PTY_OK;
@@ -280,6 +332,7 @@ static FrameArgs base_args(const pty_plan* p) {
   a.stage = p->d_stage;
   a.stage_frames = p->stage_frames;
   a.mask_blk = p->d_mask_blk;
+  a.timeout = p->d_timeout;
   return a;
 }
 
@@ -542,6 +595,21 @@ static int dm_body(pty_plan* p, const pty_buffers* b, const pty_options* o, int 
   const int n = p->n, N0 = p->N0, N1 = p->N1, U = p->U, V = p->V;
   const int* R = p->d_R;
 
+    // Iteration j's main projection (dm.py:56-85) equals iteration j-1's
+    // metric projection (dm.py:104-134): both project the same exits from the
+    // same O, P (the metric starts from copies), with the same branch.  That
+    // holds for methods 1-3 only (methods 4-6 project pmod_7(exits) in the
+    // main branch, dm.py:171), and needs the same OP branch in both
+    // iterations and no Pmod_P after the metric projection (dm.py:136-137).
+    // Probe centring rolls the metric's Os, Ps by the shift the main branch
+    // then applies to the exits as well (dm.py:68-82, 118-127).
+    auto foldable = [&](int j) -> bool {
+      if (use_bg || j <= 0 || j >= iters) return false;
+      if (j - 1 < o->Pmod_probe) return false;
+      if (upd == 3 && ((j - 1) % o->OP_iters1 == 0) != (j % o->OP_iters1 == 0)) return false;
+      return true;
+    };
+    bool main_done = false;
     // era.py:536: psi = P * O[R]; methods 4-6 form it inside their first Pmod_7 pass
     if (!use_bg || iters == 0) PTY_TRY(launch_make_exits(n, N0, N1, U, V, R, O, P, psi, st));
     if (upd & 1) PTY_TRY(copy_d2d(p->d_bakO, O, nobj * sizeof(float2), st));  // dm.py:35-38
@@ -565,7 +633,19 @@ static int dm_body(pty_plan* p, const pty_buffers* b, const pty_options* o, int 
         }
       }
       // main consistency projection (dm.py:56-85)
-      if (upd == 1) {
+      if (main_done) {
+        // O and P (and the heatmaps) already hold it: the previous iteration's
+        // metric projection was computed into them (see `foldable`).  Only
+        // the centring's roll of the exit waves (dm.py:81-82) remains.
+        if (upd == 3 && i % o->OP_iters1 == 0) {
+          heatP_valid = heatO_valid = true;
+          if (o->probe_centering) {
+            PTY_TRY(launch_roll(psi, p->d_psi_tmp, n, N0, N1, p->d_shift, st));
+            PTY_TRY(copy_d2d(psi, p->d_psi_tmp, (size_t)n * npix * sizeof(float2), st));
+            heatP_valid = heatO_valid = false;
+          }
+        }
+      } else if (upd == 1) {
         PTY_TRY(launch_psup_O(p->tl, n, N0, N1, U, V, R, psi, P, p->d_heatP, !heatP_valid, alpha, O, st));
         heatP_valid = true;
       } else if (upd == 2) {
@@ -606,11 +686,19 @@ static int dm_body(pty_plan* p, const pty_buffers* b, const pty_options* o, int 
           PTY_TRY(frame_op(p, OP_DM1, d, n, st));
         }
       }
-      // metric projection (dm.py:104-137 / 231-271)
-      float2* Os = p->d_Os;
-      float2* Ps = p->d_Ps;
-      PTY_TRY(copy_d2d(Os, O, nobj * sizeof(float2), st));
-      PTY_TRY(copy_d2d(Ps, P, npix * sizeof(float2), st));
+      // metric projection (dm.py:104-137 / 231-271).  When the next
+      // iteration's main projection equals it, it is computed straight into
+      // O and P (the main branch's values are not needed again) and the next
+      // iteration skips its own; otherwise into the scratch Os, Ps.
+      const bool direct = foldable(i + 1);
+      float2* Os = direct ? O : p->d_Os;
+      float2* Ps = direct ? P : p->d_Ps;
+      double* hP2 = direct ? p->d_heatP : p->d_heatP2;
+      double* hO2 = direct ? p->d_heatO : p->d_heatO2;
+      if (!direct) {
+        PTY_TRY(copy_d2d(Os, O, nobj * sizeof(float2), st));
+        PTY_TRY(copy_d2d(Ps, P, npix * sizeof(float2), st));
+      }
       if (upd == 1) {
         PTY_TRY(launch_psup_O(p->tl, n, N0, N1, U, V, R, psi, Ps, p->d_heatP, !heatP_valid, alpha, Os, st));
         heatP_valid = true;
@@ -620,9 +708,9 @@ static int dm_body(pty_plan* p, const pty_buffers* b, const pty_options* o, int 
         heatO_valid = true;
       } else if (i % o->OP_iters1 == 0) {
         for (int j = 0; j < o->OP_iters0; ++j) {
-          PTY_TRY(launch_psup_O(p->tl, n, N0, N1, U, V, R, psi, Ps, p->d_heatP2, true, alpha, Os, st));
+          PTY_TRY(launch_psup_O(p->tl, n, N0, N1, U, V, R, psi, Ps, hP2, true, alpha, Os, st));
           PTY_TRY(launch_psup_P(n, N0, N1, U, V, R, psi, Os, p->d_part_num, p->d_part_den, p->K,
-                                p->d_heatO2, true, alpha, Ps, st));
+                                hO2, true, alpha, Ps, st));
         }
         if (o->probe_centering) PTY_TRY(centre(p, Ps, Os, nullptr, st));
       } else {
@@ -647,6 +735,7 @@ static int dm_body(pty_plan* p, const pty_buffers* b, const pty_options* o, int 
       PTY_TRY(launch_finalize(p->d_err_part, n * p->eslots, p->d_dn_part, ndn, o->I_norm, b->eMod, b->eCon, i, st));
       if (upd & 1) PTY_TRY(copy_d2d(p->d_bakO, Os, nobj * sizeof(float2), st));
       if (upd & 2) PTY_TRY(copy_d2d(p->d_bakP, Ps, npix * sizeof(float2), st));
+      main_done = direct;
     }
     if (b->intensities && iters > 0) {  // dm.py:298-299
       FrameArgs a = base_args(p);

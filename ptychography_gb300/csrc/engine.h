@@ -2,7 +2,9 @@
 #pragma once
 #include <cstddef>
 #include <cstdint>
+#include <cuda.h>
 #include <cuda_runtime.h>
+#include <cudaTypedefs.h>
 
 #include "pty_common.cuh"
 
@@ -46,6 +48,7 @@ struct FrameArgs {
   float2* stage;             // [stage_frames][N0][N1] frame scratch of the staged tiles
   int stage_frames;          // frames the scratch holds (launches run in groups of it)
   uint8_t* mask_blk;         // [N0 * N1] mask in column-block order (staged tiles)
+  int* timeout;              // set when a bounded wait of a kernel runs out
 };
 
 // Frame tiles: how many CTAs transform one frame.  Tile 1 is the single-CTA
@@ -109,6 +112,10 @@ int set_cuda_error(cudaError_t e, const char* where);
     if (_e != cudaSuccess) return pty::set_cuda_error(_e, #x); \
   } while (0)
 int check_launch(const char* where);  // also counts the launch
+// the device's timeout flag (allocated on first use; see pty_timeout_status)
+int device_timeout_flag(int** out);
+// cuTensorMapEncodeTiled from the driver (TMA tensor maps)
+int tensor_map_encoder(PFN_cuTensorMapEncodeTiled_v12000* out);
 void count_launches(long long k);
 long long launch_total();
 

@@ -21,6 +21,7 @@
 // 16-CTA tile 116, so results agree with it to FP32 rounding.
 // Replaces the same reference functions as frame_kernels.cu.
 #include <cstdint>
+#include <cstring>
 
 #include "engine.h"
 #include "fft_line3.cuh"
@@ -38,8 +39,17 @@ constexpr int kCols = kNT / kA;             // columns per column CTA
 constexpr int kBlocksPerFrame = kN / kRows; // = kN / kCols = 64
 constexpr int kRowScr = 542;                // row-exchange slots per warp
 constexpr int kColE1 = 527;                 // column exchange-1 slots (33 k1 + t)
-constexpr size_t kColSmem = (size_t)(kColE1 + kN) * kCols * sizeof(float2) +
-                            (size_t)2 * kN * kCols * sizeof(float) + (size_t)kN * kCols;
+// column-launch shared memory, every region at a 128-byte boundary (TMA
+// destinations): exchange 1, the scratch columns (then exchange 2), the
+// amplitudes, the background, the mask block, the copies' mbarrier
+constexpr size_t kAlign128(size_t b) { return (b + 127) / 128 * 128; }
+constexpr size_t kOffX2 = kAlign128((size_t)kColE1 * kCols * sizeof(float2));
+constexpr size_t kOffA = kOffX2 + (size_t)kN * kCols * sizeof(float2);
+constexpr size_t kOffB = kOffA + (size_t)kN * kCols * sizeof(float);
+constexpr size_t kOffM = kOffB + (size_t)kN * kCols * sizeof(float);
+constexpr size_t kOffBar = kOffM + (size_t)kN * kCols;
+constexpr size_t kColSmem = kOffBar + 128 + 128;   // + the barrier, + base alignment slack
+constexpr unsigned kSpinLimit = 1u << 26;          // mbarrier polls before giving up
 static_assert(kRows == kCols && kBlocksPerFrame == 64, "64 blocks per frame per launch");
 
 // Row slot layouts (a warp is one line; each half-warp touches 16 distinct
@@ -101,11 +111,44 @@ __global__ void __launch_bounds__(kNT, 3) staged_rows_kernel(FrameArgs g, int f0
   }
 }
 
-PTY_DEV void cp_async16(void* smem, const void* gmem) {
-  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(sa), "l"(gmem) : "memory");
+PTY_DEV uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+PTY_DEV void mbar_init(uint64_t* bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
 }
-PTY_DEV void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+PTY_DEV bool mbar_try_wait(uint64_t* bar, unsigned parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_addr(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// 2-D box of a 3-D tensor map (columns, rows, frames) into shared memory
+PTY_DEV void tma_box(void* dst, const CUtensorMap* map, uint64_t* bar, int c, int r, int f) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes "
+      "[%0], [%1, {%3, %4, %5}], [%2];" ::"r"(smem_addr(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(smem_addr(bar)), "r"(c), "r"(r), "r"(f)
+      : "memory");
+}
+// contiguous bytes (a multiple of 16, both addresses 16-byte aligned)
+PTY_DEV void bulk_copy(void* dst, const void* src, unsigned bytes, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          smem_addr(dst)),
+      "l"(src), "r"(bytes), "r"(smem_addr(bar))
+      : "memory");
+}
+
+// The column launch's tensor maps: boxes of 8 columns x 256 rows of one frame
+struct ColMaps {
+  CUtensorMap stage;   // the frame scratch (8-byte elements: complex64)
+  CUtensorMap amp;     // amplitudes
+  CUtensorMap bg;      // the background the operation reads
+};
 
 // The mask in column-block order for the column launch:
 // blk[b][r][c] = mask[r][8 b + c] (64 blocks of 512 rows x 8 columns).
@@ -120,23 +163,26 @@ __global__ void __launch_bounds__(kNT) mask_blocks_kernel(const uint8_t* __restr
 
 // Column launch: 8 columns of one frame per CTA, thread (cw, tc) = line
 // thread tc of column c0 + cw.  Every global input of the CTA -- its scratch
-// columns, amplitudes and background -- is copied into shared memory by
-// cp.async at the start, with its block of the mask (shared by all frames,
+// columns, amplitudes and background -- is copied into shared memory by TMA
+// at the start, with its block of the mask (shared by all frames,
 // L2-resident), so the CTA waits for memory once and holds no registers for
 // loads in flight.
 template <int OP>
-__global__ void __launch_bounds__(kNT, 2) staged_cols_kernel(FrameArgs g, int f0) {
+__global__ void __launch_bounds__(kNT, 2) staged_cols_kernel(FrameArgs g, int f0, const __grid_constant__ ColMaps maps,
+                                                              int amp_frames, int bg_frames) {
   using T = OpTraits<OP>;
   using MI = ModIn<OP, kB>;
   __shared__ float2 tw1[kN];
   __shared__ float2 tw2[32];
   __shared__ double red[32];
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  float2* x1 = reinterpret_cast<float2*>(smem_raw);      // [527][8] exchange 1
-  float2* x2 = x1 + (size_t)kColE1 * kCols;               // [512][8] input, then exchange 2
-  float* sa = reinterpret_cast<float*>(x2 + (size_t)kN * kCols);   // [512][8] amplitudes
-  float* sb = sa + (size_t)kN * kCols;                    // [512][8] background (or DM state)
-  uint8_t* sm = reinterpret_cast<uint8_t*>(sb + (size_t)kN * kCols);   // [512][8] mask
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  unsigned char* base = smem_raw + ((128 - (smem_addr(smem_raw) & 127)) & 127);
+  float2* x1 = reinterpret_cast<float2*>(base);                // [527][8] exchange 1
+  float2* x2 = reinterpret_cast<float2*>(base + kOffX2);       // [512][8] input, then exchange 2
+  float* sa = reinterpret_cast<float*>(base + kOffA);          // [512][8] amplitudes
+  float* sb = reinterpret_cast<float*>(base + kOffB);          // [512][8] background (or DM state)
+  uint8_t* sm = base + kOffM;                                  // [512][8] mask
+  uint64_t* bar = reinterpret_cast<uint64_t*>(base + kOffBar);
   const int fl = blockIdx.x / kBlocksPerFrame, f = f0 + fl;
   const int blk = blockIdx.x % kBlocksPerFrame;
   const int cw = threadIdx.x % kCols, tc = threadIdx.x / kCols;
@@ -147,43 +193,52 @@ __global__ void __launch_bounds__(kNT, 2) staged_cols_kernel(FrameArgs g, int f0
   const float* bsrc = nullptr;
   if constexpr (MI::BG_IN) bsrc = g.bg_in ? g.bg_in + (size_t)g.bg_stride * f : nullptr;
   if constexpr (OP == OP_DM7) bsrc = g.bg_out + fbase;
-  // 16-byte copies: a row segment of the CTA's 8 columns is 64 bytes of
-  // scratch (4 copies) and 32 bytes of amplitude or background (2 copies)
+  // Every global input of the CTA -- its 8 scratch columns, amplitudes and
+  // background (two 8 x 256 boxes each) and its 4 KB block of the mask --
+  // arrives by TMA on one mbarrier: 8 copies instead of ~8000 16-byte
+  // requests, no registers held for loads in flight.
   const int c0 = blk * kCols;
-  const float2* ssrc = g.stage + (size_t)fl * kN * kN + c0;
-#pragma unroll
-  for (int i = 0; i < (kN * kCols / 2) / kNT; ++i) {
-    const int q = threadIdx.x + kNT * i, r = q >> 2, p = q & 3;
-    cp_async16(&x2[r * kCols + 2 * p], ssrc + (size_t)r * kN + 2 * p);
-  }
-  if constexpr (MI::NEEDS) {
-    const float* asrc = g.amp + (size_t)g.amp_stride * f + c0;
-#pragma unroll
-    for (int i = 0; i < (kN * kCols / 4) / kNT; ++i) {
-      const int q = threadIdx.x + kNT * i, r = q >> 1, p = q & 1;
-      cp_async16(&sa[r * kCols + 4 * p], asrc + (size_t)r * kN + 4 * p);
+  const bool want_bg = BG_ST && bsrc != nullptr;
+  if (threadIdx.x == 0) {
+    mbar_init(bar, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    unsigned bytes = 2u * 256u * kCols * sizeof(float2);
+    if constexpr (MI::NEEDS) {
+      bytes += 2u * 256u * kCols * sizeof(float);
+      if (g.mask) bytes += kN * kCols;
+    }
+    if (want_bg) bytes += 2u * 256u * kCols * sizeof(float);
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+                 : "memory");
+    for (int h = 0; h < 2; ++h) tma_box(x2 + h * 256 * kCols, &maps.stage, bar, c0, 256 * h, fl);
+    if constexpr (MI::NEEDS) {
+      const int af = amp_frames > 1 ? f : 0;
+      for (int h = 0; h < 2; ++h) tma_box(sa + h * 256 * kCols, &maps.amp, bar, c0, 256 * h, af);
+      // the mask's column-block copy: this CTA's 512 rows x 8 columns in one piece
+      if (g.mask) bulk_copy(sm, g.mask_blk + (size_t)blk * kN * kCols, kN * kCols, bar);
+    }
+    if (want_bg) {
+      const int bf = bg_frames > 1 ? f : 0;
+      for (int h = 0; h < 2; ++h) tma_box(sb + h * 256 * kCols, &maps.bg, bar, c0, 256 * h, bf);
     }
   }
-  if constexpr (BG_ST) {
-    if (bsrc) {
-#pragma unroll
-      for (int i = 0; i < (kN * kCols / 4) / kNT; ++i) {
-        const int q = threadIdx.x + kNT * i, r = q >> 1, p = q & 1;
-        cp_async16(&sb[r * kCols + 4 * p], bsrc + c0 + (size_t)r * kN + 4 * p);
-      }
-    }
-  }
-  if constexpr (MI::NEEDS) {
-    // the mask's column-block copy: this CTA's 512 rows x 8 columns are 4 KB
-    // in one piece (the natural layout would take 512 separate 8-byte reads)
-    if (g.mask) cp_async16(&sm[16 * threadIdx.x], g.mask_blk + (size_t)blk * kN * kCols + 16 * threadIdx.x);
-  }
+  __syncthreads();   // the barrier's initialisation before anyone polls it
   load_twiddles(g, tw1, tw2);
   auto e1 = [x1, cw](int s) -> float2& { return x1[s * kCols + cw]; };
   auto e2 = [x2, cw](int s) -> float2& { return x2[s * kCols + cw]; };
   auto cta_sync = [] { __syncthreads(); };
-  cp_async_wait_all();
-  __syncthreads();
+  {
+    // bounded wait: past the limit the flag is set and the CTA only waits
+    // (again bounded) for its copies before returning
+    bool ok = false;
+    for (unsigned i = 0; i < kSpinLimit && !ok; ++i) ok = mbar_try_wait(bar, 0);
+    if (__syncthreads_or(!ok)) {
+      if (threadIdx.x == 0 && g.timeout) atomicExch(g.timeout, 1);
+      for (unsigned i = 0; i < kSpinLimit && !mbar_try_wait(bar, 0); ++i) {
+      }
+      return;
+    }
+  }
   float2 v[kB];
   // the transform's first barrier orders these reads before exchange 2
   // overwrites x2
@@ -234,8 +289,44 @@ int set_attr() {
   return PTY_OK;
 }
 
+// A 3-D tensor map (columns, rows, frames) over 512 x 512 frames of `esize`
+// bytes per element, frames `fstride` elements apart (0: one shared frame),
+// with 8 x 256 boxes.
+int frame_map(CUtensorMap* m, const void* base, CUtensorMapDataType type, int esize, long long fstride,
+              int frames) {
+  PFN_cuTensorMapEncodeTiled_v12000 encode;
+  PTY_TRY(tensor_map_encoder(&encode));
+  const bool shared = fstride == 0;
+  const cuuint64_t dims[3] = {(cuuint64_t)kN, (cuuint64_t)kN, (cuuint64_t)(shared ? 1 : frames)};
+  const cuuint64_t strides[2] = {(cuuint64_t)kN * esize,
+                                 (cuuint64_t)(shared ? (long long)kN * kN : fstride) * esize};
+  const cuuint32_t box[3] = {(cuuint32_t)kCols, 256, 1};
+  const cuuint32_t estr[3] = {1, 1, 1};
+  CUresult r = encode(m, type, 3, const_cast<void*>(base), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                      CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                      CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return set_error(PTY_ERR_CUDA, "staged frame tile: tensor map");
+  return PTY_OK;
+}
+
 template <int OP>
 int launch(const FrameArgs& a, int nframes, cudaStream_t st) {
+  using MI = ModIn<OP, kB>;
+  ColMaps maps;
+  std::memset(&maps, 0, sizeof(maps));
+  PTY_TRY(frame_map(&maps.stage, a.stage, CU_TENSOR_MAP_DATA_TYPE_UINT64, 8, (long long)kN * kN, a.stage_frames));
+  int amp_frames = 1, bg_frames = 1;
+  if (MI::NEEDS) {
+    amp_frames = a.amp_stride ? nframes : 1;
+    PTY_TRY(frame_map(&maps.amp, a.amp, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, a.amp_stride, nframes));
+  }
+  if (MI::BG_IN && a.bg_in) {
+    bg_frames = a.bg_stride ? nframes : 1;
+    PTY_TRY(frame_map(&maps.bg, a.bg_in, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, a.bg_stride, nframes));
+  } else if (OP == OP_DM7) {
+    bg_frames = nframes;
+    PTY_TRY(frame_map(&maps.bg, a.bg_out, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, (long long)kN * kN, nframes));
+  }
   if (a.mask) {
     mask_blocks_kernel<<<kBlocksPerFrame, kNT, 0, st>>>(a.mask, a.mask_blk);
     PTY_TRY(check_launch("mask_blocks_kernel"));
@@ -245,7 +336,7 @@ int launch(const FrameArgs& a, int nframes, cudaStream_t st) {
     const dim3 grid(nf * kBlocksPerFrame);
     staged_rows_kernel<OP, false><<<grid, kNT, 0, st>>>(a, f0);
     PTY_TRY(check_launch("staged_rows_kernel"));
-    staged_cols_kernel<OP><<<grid, kNT, kColSmem, st>>>(a, f0);
+    staged_cols_kernel<OP><<<grid, kNT, kColSmem, st>>>(a, f0, maps, amp_frames, bg_frames);
     PTY_TRY(check_launch("staged_cols_kernel"));
     if constexpr (OpTraits<OP>::INVERSE) {
       staged_rows_kernel<OP, true><<<grid, kNT, 0, st>>>(a, f0);

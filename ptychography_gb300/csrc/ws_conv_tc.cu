@@ -377,41 +377,6 @@ __global__ void __launch_bounds__(kThreads, 1)
   }
 }
 
-PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
-std::once_flag g_encode_once;
-int* g_err_flag[64] = {};
-std::mutex g_err_mutex;
-
-int encode_fn(PFN_cuTensorMapEncodeTiled_v12000* out) {
-  std::call_once(g_encode_once, [] {
-    void* fn = nullptr;
-    cudaDriverEntryPointQueryResult q;
-    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) ==
-            cudaSuccess &&
-        q == cudaDriverEntryPointSuccess)
-      g_encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
-  });
-  if (!g_encode) return set_error(PTY_ERR_CUDA, "cuTensorMapEncodeTiled is not available");
-  *out = g_encode;
-  return PTY_OK;
-}
-
-// one int per device, set by a kernel whose bounded wait ran out
-int err_flag(int** out) {
-  int dev = 0;
-  PTY_CUDA(cudaGetDevice(&dev));
-  if (dev < 0 || dev >= 64) return set_error(PTY_ERR_ARG, "device index too large");
-  std::lock_guard<std::mutex> lock(g_err_mutex);
-  if (!g_err_flag[dev]) {
-    void* q = nullptr;
-    PTY_CUDA(cudaMalloc(&q, sizeof(int)));
-    PTY_CUDA(cudaMemset(q, 0, sizeof(int)));
-    g_err_flag[dev] = static_cast<int*>(q);
-  }
-  *out = g_err_flag[dev];
-  return PTY_OK;
-}
-
 int sm_count() {
   int dev = 0, n = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return 1;
@@ -451,9 +416,9 @@ extern "C" int pty_ws_conv3x3_tc(int32_t B, int32_t H, int32_t W, int32_t Cin, i
     if (q && (reinterpret_cast<uintptr_t>(q) & 15))
       return set_error(PTY_ERR_ARG, "pty_ws_conv3x3_tc: arrays must be 16-byte aligned");
   PFN_cuTensorMapEncodeTiled_v12000 encode;
-  PTY_TRY(encode_fn(&encode));
+  PTY_TRY(tensor_map_encoder(&encode));
   int* err = nullptr;
-  PTY_TRY(err_flag(&err));
+  PTY_TRY(device_timeout_flag(&err));
 
   ConvParams p{};
   p.B = B; p.H = H; p.W = W; p.Cin = Cin; p.Cout = Cout;
@@ -504,18 +469,4 @@ extern "C" int pty_ws_conv3x3_tc(int32_t B, int32_t H, int32_t W, int32_t Cin, i
   const int grid = p.tiles < sm_count() ? p.tiles : sm_count();
   ws_conv_tc_kernel<<<grid, kThreads, smem, (cudaStream_t)stream>>>(tmX, tmW, p);
   return check_launch("ws_conv_tc_kernel");
-}
-
-// Reads and clears the flag of a bounded wait that ran out (1) in a
-// pty_ws_conv3x3_tc launch on the current device since the last call.
-// Synchronises the calling thread with the device.
-extern "C" int pty_ws_conv_tc_status(int32_t* timed_out) {
-  if (!timed_out) return set_error(PTY_ERR_ARG, "pty_ws_conv_tc_status: null argument");
-  int* err = nullptr;
-  PTY_TRY(err_flag(&err));
-  int h = 0;
-  PTY_CUDA(cudaMemcpy(&h, err, sizeof(int), cudaMemcpyDeviceToHost));
-  if (h) PTY_CUDA(cudaMemset(err, 0, sizeof(int)));
-  *timed_out = h;
-  return PTY_OK;
 }

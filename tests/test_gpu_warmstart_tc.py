@@ -54,7 +54,7 @@ def bf16(a):
 
 def status_ok():
     t = ctypes.c_int32(-1)
-    _native.check(_native.load().pty_ws_conv_tc_status(ctypes.byref(t)))
+    _native.check(_native.load().pty_timeout_status(ctypes.byref(t)))
     return t.value == 0
 
 
