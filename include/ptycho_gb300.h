@@ -274,6 +274,23 @@ int pty_ws_exits(int32_t nf, int64_t npix, const float* y, const void* P, int32_
  * to 128, W dividing 128 (H a multiple of 128 / W) or a multiple of 128;
  * arrays 16-byte aligned; others are PTY_ERR_UNSUPPORTED.  Its mbarrier waits
  * are bounded (see pty_timeout_status). */
+/* The same convolution on the CUDA cores for layers with few channels
+ * (C_in even, 2..32; C_out 2, 4, 8, 16 or 32: the network's 2-channel first
+ * and last layers), one thread per output pixel, no im2col buffer: out (bf16,
+ * skip added when given) and/or out32 (float, no skip) may be NULL. */
+int pty_ws_conv3x3_direct(int32_t B, int32_t H, int32_t W, int32_t Cin, int32_t Cout, const void* X,
+                          const void* Wt, const float* bias, int32_t relu, const void* skip, void* out,
+                          float* out32, void* stream);
+/* Pieces of the warm start for frames larger than the network's (the frame
+ * at a coarser real-space sampling):
+ *   pty_ws_crop_center: out[f][a][b] = scale * I[f][a + (N0 - M0) / 2][b + (N1 - M1) / 2],
+ *     the central M0 x M1 of each centred pattern (float, device);
+ *   pty_ws_upsample_object: O[u][v] = bilinear sample of Oh (Uh x Vh) at
+ *     (u / f, v / f), clamped at the edges (complex64, device). */
+int pty_ws_crop_center(int32_t nf, int32_t N0, int32_t N1, int32_t M0, int32_t M1, const float* I,
+                       float scale, float* out, void* stream);
+int pty_ws_upsample_object(int32_t Uh, int32_t Vh, const void* Oh, int32_t U, int32_t V, int32_t f,
+                           void* O, void* stream);
 int pty_ws_conv3x3_tc(int32_t B, int32_t H, int32_t W, int32_t Cin, int32_t Cout, const void* X,
                       const void* Wt, const float* bias, int32_t relu, const void* skip, void* out,
                       void* stream);

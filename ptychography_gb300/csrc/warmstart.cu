@@ -719,3 +719,149 @@ extern "C" int pty_ws_exits(int32_t nf, int64_t npix, const float* y, const void
                                                                  (float2*)psi);
   return ws_launched("ws_exits_kernel");
 }
+
+// ---------------------------------------------------------------- direct convolution
+namespace pty {
+namespace {
+
+constexpr int kDirThreads = 128;
+
+// A 3 x 3 convolution (zero padding) for layers with few channels, one thread
+// per output pixel holding all COUT sums: Z[p][co] = sum over taps and input
+// channels of X[p + tap][ci] W[co][tap C_in + ci], in that order, FP32.  Then
+// v = Z + bias (relu when asked), a = bf16(v), out = a (+ skip, rounded to
+// bf16 as ws_bias_act_kernel does) and out32 = v.  The weights sit in shared
+// memory transposed to [k][COUT], so every thread reads the same word.
+template <int COUT>
+__global__ void __launch_bounds__(kDirThreads) ws_conv_direct_kernel(int Bt, int H, int W, int Cin,
+                                                                     const __nv_bfloat16* __restrict__ X,
+                                                                     const __nv_bfloat16* __restrict__ Wt,
+                                                                     const float* __restrict__ bias, int relu,
+                                                                     const __nv_bfloat16* __restrict__ skip,
+                                                                     __nv_bfloat16* __restrict__ out,
+                                                                     float* __restrict__ out32) {
+  extern __shared__ float wsm[];                 // [9 Cin][COUT]
+  const int K = 9 * Cin;
+  for (int i = threadIdx.x; i < K * COUT; i += blockDim.x) {
+    const int co = i / K, k = i - co * K;
+    wsm[k * COUT + co] = __bfloat162float(Wt[i]);
+  }
+  __syncthreads();
+  const long long P = (long long)Bt * H * W;
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < P; p += (long long)gridDim.x * blockDim.x) {
+    const int x = (int)(p % W), y = (int)((p / W) % H);
+    const long long b = p / ((long long)W * H);
+    float acc[COUT];
+#pragma unroll
+    for (int c = 0; c < COUT; ++c) acc[c] = 0.f;
+    for (int tap = 0; tap < 9; ++tap) {
+      const int yy = y + tap / 3 - 1, xx = x + tap % 3 - 1;
+      if (yy < 0 || yy >= H || xx < 0 || xx >= W) continue;
+      const __nv_bfloat16* xp = X + ((b * H + yy) * W + xx) * Cin;
+      const float* wk = wsm + tap * Cin * COUT;
+      for (int ci = 0; ci < Cin; ci += 2) {
+        const float2 v = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(xp + ci));
+#pragma unroll
+        for (int c = 0; c < COUT; ++c) acc[c] = fmaf(v.x, wk[ci * COUT + c], acc[c]);
+#pragma unroll
+        for (int c = 0; c < COUT; ++c) acc[c] = fmaf(v.y, wk[(ci + 1) * COUT + c], acc[c]);
+      }
+    }
+#pragma unroll
+    for (int c = 0; c < COUT; ++c) {
+      float v = acc[c] + bias[c];
+      if (relu) v = fmaxf(v, 0.f);
+      const long long o = p * COUT + c;
+      if (out32) out32[o] = v;
+      if (out) {
+        const __nv_bfloat16 vb = __float2bfloat16(v);
+        out[o] = skip ? __float2bfloat16(__bfloat162float(vb) + __bfloat162float(skip[o])) : vb;
+      }
+    }
+  }
+}
+
+// out[f][a][b] = scale I[f][a + (N0 - M0) / 2][b + (N1 - M1) / 2]: the
+// central M0 x M1 of each centred pattern
+__global__ void ws_crop_center_kernel(long long nf, int N0, int N1, int M0, int M1, const float* __restrict__ I,
+                                      float scale, float* __restrict__ out) {
+  const long long n = nf * M0 * M1;
+  const int o0 = (N0 - M0) / 2, o1 = (N1 - M1) / 2;
+  WS_LOOP(i, n) {
+    const long long f = i / ((long long)M0 * M1);
+    const int r = (int)(i % ((long long)M0 * M1));
+    const int a = r / M1, b = r - a * M1;
+    out[i] = scale * I[(f * N0 + a + o0) * N1 + b + o1];
+  }
+}
+
+// O[u][v] = bilinear sample of Oh at (u / f, v / f), clamped to Oh's edges
+__global__ void ws_upsample_kernel(int Uh, int Vh, const float2* __restrict__ Oh, int U, int V, int f,
+                                   float2* __restrict__ O) {
+  const long long n = (long long)U * V;
+  const float inv = 1.f / (float)f;
+  WS_LOOP(i, n) {
+    const int u = (int)(i / V), v = (int)(i % V);
+    const float su = fminf(u * inv, (float)(Uh - 1)), sv = fminf(v * inv, (float)(Vh - 1));
+    const int u0 = (int)su, v0 = (int)sv;
+    const int u1 = u0 + 1 < Uh ? u0 + 1 : u0, v1 = v0 + 1 < Vh ? v0 + 1 : v0;
+    const float du = su - u0, dv = sv - v0;
+    const float2 a = Oh[(size_t)u0 * Vh + v0], b = Oh[(size_t)u0 * Vh + v1];
+    const float2 c = Oh[(size_t)u1 * Vh + v0], d = Oh[(size_t)u1 * Vh + v1];
+    const float w00 = (1.f - du) * (1.f - dv), w01 = (1.f - du) * dv, w10 = du * (1.f - dv), w11 = du * dv;
+    O[i] = make_float2(w00 * a.x + w01 * b.x + w10 * c.x + w11 * d.x, w00 * a.y + w01 * b.y + w10 * c.y + w11 * d.y);
+  }
+}
+
+template <int COUT>
+int launch_direct(int B, int H, int W, int Cin, const void* X, const void* Wt, const float* bias, int relu,
+                  const void* skip, void* out, float* out32, cudaStream_t st) {
+  const size_t smem = (size_t)9 * Cin * COUT * sizeof(float);
+  const long long P = (long long)B * H * W;
+  long long g = (P + kDirThreads - 1) / kDirThreads;
+  if (g > 16 * 152) g = 16 * 152;
+  ws_conv_direct_kernel<COUT><<<(unsigned)g, kDirThreads, smem, st>>>(
+      B, H, W, Cin, (const __nv_bfloat16*)X, (const __nv_bfloat16*)Wt, bias, relu, (const __nv_bfloat16*)skip,
+      (__nv_bfloat16*)out, out32);
+  return check_launch("ws_conv_direct_kernel");
+}
+
+}  // namespace
+}  // namespace pty
+
+extern "C" int pty_ws_conv3x3_direct(int32_t B, int32_t H, int32_t W, int32_t Cin, int32_t Cout, const void* X,
+                                     const void* Wt, const float* bias, int32_t relu, const void* skip, void* out,
+                                     float* out32, void* stream) {
+  if (B < 1 || H < 1 || W < 1 || !X || !Wt || !bias || (!out && !out32))
+    return set_error(PTY_ERR_ARG, "pty_ws_conv3x3_direct: bad arguments");
+  if (Cin < 2 || Cin > 32 || (Cin & 1)) return set_error(PTY_ERR_UNSUPPORTED, "pty_ws_conv3x3_direct: C_in must be even, 2..32");
+  if (((uintptr_t)X & 3) || ((uintptr_t)Wt & 1))
+    return set_error(PTY_ERR_ARG, "pty_ws_conv3x3_direct: X must be 4-byte aligned");
+  cudaStream_t st = (cudaStream_t)stream;
+  switch (Cout) {
+    case 2: return launch_direct<2>(B, H, W, Cin, X, Wt, bias, relu, skip, out, out32, st);
+    case 4: return launch_direct<4>(B, H, W, Cin, X, Wt, bias, relu, skip, out, out32, st);
+    case 8: return launch_direct<8>(B, H, W, Cin, X, Wt, bias, relu, skip, out, out32, st);
+    case 16: return launch_direct<16>(B, H, W, Cin, X, Wt, bias, relu, skip, out, out32, st);
+    case 32: return launch_direct<32>(B, H, W, Cin, X, Wt, bias, relu, skip, out, out32, st);
+  }
+  return set_error(PTY_ERR_UNSUPPORTED, "pty_ws_conv3x3_direct: C_out must be 2, 4, 8, 16 or 32");
+}
+
+extern "C" int pty_ws_crop_center(int32_t nf, int32_t N0, int32_t N1, int32_t M0, int32_t M1, const float* I,
+                                  float scale, float* out, void* stream) {
+  if (nf < 1 || M0 < 1 || M1 < 1 || M0 > N0 || M1 > N1 || !I || !out)
+    return set_error(PTY_ERR_ARG, "pty_ws_crop_center: bad arguments");
+  const long long n = (long long)nf * M0 * M1;
+  ws_crop_center_kernel<<<grid_for(n), 256, 0, (cudaStream_t)stream>>>(nf, N0, N1, M0, M1, I, scale, out);
+  return ws_launched("ws_crop_center_kernel");
+}
+
+extern "C" int pty_ws_upsample_object(int32_t Uh, int32_t Vh, const void* Oh, int32_t U, int32_t V, int32_t f,
+                                      void* O, void* stream) {
+  if (Uh < 1 || Vh < 1 || U < 1 || V < 1 || f < 1 || !Oh || !O)
+    return set_error(PTY_ERR_ARG, "pty_ws_upsample_object: bad arguments");
+  const long long n = (long long)U * V;
+  ws_upsample_kernel<<<grid_for(n), 256, 0, (cudaStream_t)stream>>>(Uh, Vh, (const float2*)Oh, U, V, f, (float2*)O);
+  return ws_launched("ws_upsample_kernel");
+}

@@ -158,16 +158,32 @@ class WarmStartNet:
                                                  int(relu), _p(skip), _p(out), self._sp()))
         return out
 
+    def _conv_direct(self, i, x, B, H, W, last=False):
+        """Layer i on the CUDA-core direct convolution (the 2-channel first
+        and last layers, too narrow for a tensor-core tile): bf16 activation,
+        or the FP32 output if last."""
+        torch = _torch()
+        cin, cout, relu, _ = LAYERS[i]
+        if last:
+            y = self._buf("y", (B, H, W, cout), torch.float32)
+            _native.check(self.lib.pty_ws_conv3x3_direct(B, H, W, cin, cout, _p(x), _p(self.wb[i]), _p(self.b[i]),
+                                                         int(relu), None, None, _p(y), self._sp()))
+            return y
+        out = self._buf("d%d" % i, (B, H, W, cout), torch.bfloat16)
+        _native.check(self.lib.pty_ws_conv3x3_direct(B, H, W, cin, cout, _p(x), _p(self.wb[i]), _p(self.b[i]),
+                                                     int(relu), None, _p(out), None, self._sp()))
+        return out
+
     def forward_infer(self, x):
         """The forward pass for inference: layers 1-4 (the network's bulk,
-        32-128 channels) on the tensor-core convolution, which writes no
-        im2col buffer and keeps nothing for a backward pass; the 2-channel
-        first and last layers on the im2col path.  Same result as forward()
-        up to FP32 summation order."""
+        32-128 channels) on the tensor-core convolution, the 2-channel first
+        and last layers on the CUDA-core direct convolution; neither writes
+        an im2col buffer or keeps anything for a backward pass.  Same result
+        as forward() up to FP32 summation order."""
         torch = _torch()
         B, H, W = x.shape[0], self.H, self.W
         lib, sp = self.lib, self._sp()
-        h1 = self._conv_fwd(0, x, B, H, W)
+        h1 = self._conv_direct(0, x, B, H, W)
         p1 = self._buf("p1", (B, H // 2, W // 2, 32), torch.bfloat16)
         _native.check(lib.pty_ws_pool2(B, H, W, 32, _p(h1), _p(p1), sp))
         h2 = self._conv_tc(1, p1, B, H // 2, W // 2)
@@ -180,7 +196,7 @@ class WarmStartNet:
         u4 = self._buf("u4", (B, H, W, 64), torch.bfloat16)
         _native.check(lib.pty_ws_up2(B, H // 2, W // 2, 64, _p(h4), _p(u4), sp))
         h5 = self._conv_tc(4, u4, B, H, W, skip=h1)
-        return self._conv_fwd(5, h5, B, H, W, last=True)
+        return self._conv_direct(5, h5, B, H, W, last=True)
 
     def _conv_bwd(self, i, dA, B, H, W, need_dx):
         """dA: gradient (FP32, B x H x W x C_out) at layer i's activation; sets
@@ -283,7 +299,7 @@ class WarmStartNet:
         _native.check(lib.pty_ws_prep_bp(n, H, W, _p(bp), _p(P), 1, _p(x), sp))
         return x
 
-    def predict_exits(self, I, P, plan_h, batch=64, tensor_cores=True):
+    def predict_exits(self, I, P, plan_h, batch=256, tensor_cores=True):
         """Exit waves P exp(i phase) (or |P| exp(i phase)) with the predicted
         phases, for the centred intensities I (n, H, W) float32 of the plan's
         frames and the probe P (H, W) complex64, both on the device."""
@@ -318,10 +334,12 @@ def smooth01(rng, shape, sigma=4.0):
     return (a - a.min()) / (a.max() - a.min())
 
 
-def random_object(rng, U, V=None):
-    """amplitude 0.5 + 0.5 s1, phase pi (s2 - 1/2), s1, s2 smooth random fields."""
+def random_object(rng, U, V=None, sigma=4.0):
+    """amplitude 0.5 + 0.5 s1, phase pi (s2 - 1/2), s1, s2 smooth random
+    fields of smoothing width sigma."""
     V = V or U
-    return (0.5 + 0.5 * smooth01(rng, (U, V))) * np.exp(1j * np.pi * (smooth01(rng, (U, V)) - 0.5))
+    return ((0.5 + 0.5 * smooth01(rng, (U, V), sigma))
+            * np.exp(1j * np.pi * (smooth01(rng, (U, V), sigma) - 0.5)))
 
 
 def aperture_probe(N, radius, edge, quad):
@@ -349,16 +367,21 @@ class _FramePlan:
             self.h = ctypes.c_void_p()
 
 
-def make_training_set(net, n_frames, seed=0, frames_per_object=8, batch=32, pad=64):
-    """Frames of random objects (random_object) under random probes (aperture
-    radius 24-40 px, edge 4 px, quadratic phase 0.001-0.004 rad/px^2) at
-    random positions: the network input (the frames' back-projections,
-    input_from_intensities), the targets (cos, sin of the object phase under
-    the probe) and weights |P|^2 scaled so that `batch` frames sum to 1.  All
-    on the device."""
+def make_training_set(net, n_frames, seed=0, frames_per_object=8, batch=32, pad=64, sigma=(4.0, 4.0),
+                      photons=None):
+    """Frames of random objects (random_object, smoothing width drawn from
+    `sigma`) under random probes (aperture radius 24-40 px, edge 4 px,
+    quadratic phase 0.001-0.004 rad/px^2) at random positions: the network
+    input (the frames' back-projections, input_from_intensities), the
+    targets (cos, sin of the object phase under the probe) and weights |P|^2
+    scaled so that `batch` frames sum to 1.  With photons = (lo, hi) each
+    object's frames get Poisson noise at a photon count per frame drawn
+    log-uniformly from that range.  All on the device."""
     torch = _torch()
     N, dev, lib = net.H, net.dev, net.lib
     rng = np.random.default_rng(seed)
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(int(seed))
     n = (n_frames // frames_per_object) * frames_per_object
     x = torch.empty((n, N, N, LAYERS[0][0]), dtype=torch.bfloat16, device=dev)
     t = torch.empty((n, N, N, 2), dtype=torch.float32, device=dev)
@@ -369,7 +392,8 @@ def make_training_set(net, n_frames, seed=0, frames_per_object=8, batch=32, pad=
     U = N + pad
     sp = net._sp()
     for s in range(0, n, k):
-        O = random_object(rng, U)
+        sg = float(sigma[0]) if sigma[0] == sigma[1] else float(rng.uniform(sigma[0], sigma[1]))
+        O = random_object(rng, U, sigma=sg)
         P = aperture_probe(N, rng.uniform(24, 40), 4.0, rng.uniform(0.001, 0.004))
         R = -rng.integers(0, U - N + 1, (k, 2))
         R[0] = 0                                       # the plan's window starts at R.max() = 0
@@ -378,6 +402,9 @@ def make_training_set(net, n_frames, seed=0, frames_per_object=8, batch=32, pad=
         plan = _FramePlan(k, N, U, U, R)
         try:
             _native.check(lib.pty_intensities(plan.h, _p(Od), _p(Pd), _p(I), sp))
+            if photons is not None:
+                ph = 10.0 ** rng.uniform(np.log10(photons[0]), np.log10(photons[1]))
+                I.copy_(torch.poisson(I * (ph / I.sum(dim=(1, 2), keepdim=True)), generator=gen))
             _native.check(lib.pty_make_exits(plan.h, _p(Od), _p(Pd), _p(psi), sp))
             net.input_from_intensities(plan.h, I, Pd, probe_phasors(P, dev), x[s:s + k])
             wscale = 1.0 / (batch * float(np.sum(np.abs(P) ** 2)))
@@ -451,3 +478,57 @@ def initial_object(net, I, R, P, O_shape=None, alpha=1e-10):
         return O.cpu().numpy()
     finally:
         plan.close()
+
+
+class DownsampledStart:
+    """The warm start for frames larger than the network's, each frame seen
+    at a coarser real-space sampling: the central net.H x net.W part of
+    each centred pattern is the far field of the exit wave low-passed and
+    sampled every f = N / net.H pixels (times f^2), and the probe is
+    resampled the same way, so their ratio, the object, keeps its scale.
+    The coarse frames are stitched at the scan offsets divided by f (to the
+    nearest coarse pixel) into a coarse object, which is bilinearly upsampled
+    by f onto the full object grid.
+
+    Set-up (host work, once per scan: the coarse probe, the coarse plan and
+    buffers) happens here; run() is device work plus the network's batched
+    inference.  n frames of N x N with N = f net.H, the probe P (N, N)
+    (host array), R the plan's scan offsets (n, 2) with maximum 0.
+    """
+
+    def __init__(self, net, n, N0, N1, P, R):
+        torch = _torch()
+        if N0 != N1 or net.H != net.W or N0 % net.H:
+            raise ValueError("frames must be square, a multiple of the network's %d x %d" % (net.H, net.W))
+        self.net, self.n, self.N, self.M = net, int(n), int(N0), int(net.H)
+        self.f = self.N // self.M
+        F = np.fft.fftshift(np.fft.fft2(np.asarray(P, np.complex128)))
+        o = (self.N - self.M) // 2
+        Ps = np.fft.ifft2(np.fft.ifftshift(F[o:o + self.M, o:o + self.M]))
+        self.P_s = torch.from_numpy(Ps.astype(np.complex64)).to(net.dev)
+        Rs = np.rint(np.asarray(R, np.float64)[:, :2] / self.f).astype(np.int64)
+        Rs -= Rs.max(axis=0)
+        self.Us = self.M + int(Rs[:, 0].max() - Rs[:, 0].min())
+        self.Vs = self.M + int(Rs[:, 1].max() - Rs[:, 1].min())
+        self.plan = _FramePlan(self.n, self.M, self.Us, self.Vs, Rs)
+        self.I_s = torch.empty((self.n, self.M, self.M), dtype=torch.float32, device=net.dev)
+        self.heat = torch.empty((self.Us, self.Vs), dtype=torch.float64, device=net.dev)
+
+    def run(self, I_dev, U, V):
+        """The initial object (U, V) complex64 on the device for the centred
+        intensities I_dev (n, N, N) float32 on the device."""
+        torch = _torch()
+        net, sp = self.net, self.net._sp()
+        if tuple(I_dev.shape) != (self.n, self.N, self.N):
+            raise ValueError("expected %d frames of %d x %d" % (self.n, self.N, self.N))
+        _native.check(net.lib.pty_ws_crop_center(self.n, self.N, self.N, self.M, self.M, _p(I_dev), 1.0,
+                                                 _p(self.I_s), sp))
+        O_s = warm_start_object(net, self.I_s, self.P_s, self.plan.h, self.Us, self.Vs, heat=self.heat)
+        if self.f == 1:
+            return O_s
+        O = torch.empty((U, V), dtype=torch.complex64, device=net.dev)
+        _native.check(net.lib.pty_ws_upsample_object(self.Us, self.Vs, _p(O_s), U, V, self.f, _p(O), sp))
+        return O
+
+    def close(self):
+        self.plan.close()

@@ -126,3 +126,105 @@ def test_inference_pass_matches_im2col_network():
     a, b = y_tc.cpu().numpy(), y_old.cpu().numpy()
     assert np.linalg.norm(a - b) / np.linalg.norm(b) < 1e-2
     assert len(LAYERS) == 6
+
+
+@pytest.mark.parametrize("case", [(2, 128, 128, 2, 32, True), (2, 128, 128, 32, 2, False),
+                                  (1, 16, 24, 8, 16, True)], ids=lambda c: "x".join(map(str, c[:5])))
+def test_conv_direct_matches_fp64(case):
+    """The CUDA-core direct convolution (the network's 2-channel layers) against
+    the float64 reference of the same BF16 operands, for both its outputs: the
+    FP32 pre-rounding values (out32) and the BF16 activation with a skip."""
+    B, H, W, cin, cout, relu = case
+    lib = _native.load()
+    rng = np.random.default_rng(H + cin + cout)
+    x = rng.standard_normal((B, H, W, cin)).astype(np.float32)
+    w = (rng.standard_normal((cout, 9 * cin)) * np.sqrt(2.0 / (9 * cin))).astype(np.float32)
+    b = (0.1 * rng.standard_normal(cout)).astype(np.float32)
+    sk = rng.standard_normal((B, H, W, cout)).astype(np.float32)
+    xd, wd, skd = bf16(x), bf16(w), bf16(sk)
+    bd = torch.from_numpy(b).to(dev())
+    out = torch.empty((B, H, W, cout), dtype=torch.bfloat16, device=dev())
+    out32 = torch.empty((B, H, W, cout), dtype=torch.float32, device=dev())
+    _native.check(lib.pty_ws_conv3x3_direct(B, H, W, cin, cout, p(xd), p(wd), p(bd), int(relu), p(skd),
+                                            p(out), p(out32), stream()))
+    xr = xd.float().cpu().numpy().astype(np.float64)
+    wr = wd.float().cpu().numpy().astype(np.float64)
+    skr = skd.float().cpu().numpy().astype(np.float64)
+    # FP32 output: sums of exact BF16 products, FP32 accumulation (~1e-6)
+    B_, H_, W_ = B, H, W
+    xp = np.zeros((B_, H_ + 2, W_ + 2, cin))
+    xp[:, 1:-1, 1:-1] = xr
+    z = np.zeros((B_, H_, W_, cout))
+    wk = wr.reshape(cout, 3, 3, cin)
+    for ky in range(3):
+        for kx in range(3):
+            z += np.einsum("bhwc,oc->bhwo", xp[:, ky:ky + H_, kx:kx + W_], wk[:, ky, kx])
+    z += b
+    if relu:
+        z = np.maximum(z, 0)
+    got32 = out32.cpu().numpy().astype(np.float64)
+    assert np.linalg.norm(got32 - z) / np.linalg.norm(z) < 1e-5
+    ref = conv_ref(xr, wr, b.astype(np.float64), relu, skr)
+    got = out.float().cpu().numpy().astype(np.float64)
+    assert np.linalg.norm(got - ref) / np.linalg.norm(ref) < 3e-3
+
+
+def test_conv_direct_rejects_unsupported_shapes():
+    lib = _native.load()
+    t = torch.zeros(1 << 16, dtype=torch.bfloat16, device=dev())
+    bd = torch.zeros(64, dtype=torch.float32, device=dev())
+    for cin, cout in ((3, 8), (64, 8), (2, 64), (2, 3)):
+        rc = lib.pty_ws_conv3x3_direct(1, 8, 8, cin, cout, p(t), p(t), p(bd), 1, None, p(t), None, stream())
+        assert rc != 0, (cin, cout)
+
+
+def test_crop_and_upsample_match_numpy():
+    lib = _native.load()
+    rng = np.random.default_rng(8)
+    I = rng.random((3, 32, 32)).astype(np.float32)
+    Id = torch.from_numpy(I).to(dev())
+    out = torch.empty((3, 16, 16), dtype=torch.float32, device=dev())
+    _native.check(lib.pty_ws_crop_center(3, 32, 32, 16, 16, p(Id), 0.5, p(out), stream()))
+    np.testing.assert_array_equal(out.cpu().numpy(), 0.5 * I[:, 8:24, 8:24])
+    Oh = (rng.standard_normal((7, 9)) + 1j * rng.standard_normal((7, 9))).astype(np.complex64)
+    Ohd = torch.from_numpy(Oh).to(dev())
+    U, V, f = 15, 20, 2
+    O = torch.empty((U, V), dtype=torch.complex64, device=dev())
+    _native.check(lib.pty_ws_upsample_object(7, 9, p(Ohd), U, V, f, p(O), stream()))
+    su = np.minimum(np.arange(U) / f, 6.0)
+    sv = np.minimum(np.arange(V) / f, 8.0)
+    u0, v0 = np.floor(su).astype(int), np.floor(sv).astype(int)
+    u1, v1 = np.minimum(u0 + 1, 6), np.minimum(v0 + 1, 8)
+    du, dv = (su - u0)[:, None], (sv - v0)[None, :]
+    ref = ((1 - du) * (1 - dv) * Oh[u0][:, v0] + (1 - du) * dv * Oh[u0][:, v1]
+           + du * (1 - dv) * Oh[u1][:, v0] + du * dv * Oh[u1][:, v1])
+    np.testing.assert_allclose(O.cpu().numpy(), ref, rtol=1e-5, atol=1e-6)
+
+
+def test_downsampled_start_sees_the_object():
+    """The warm start for 256^2 frames through a 128^2 network (untrained, so
+    only the geometry is checked): the stitched, upsampled object has the full
+    grid's shape, is finite, and its support follows the scan (non-zero where
+    frames overlap, exactly zero far outside)."""
+    from ptychography_gb300 import warmstart as ws
+    net = WarmStartNet(128, 128, seed=1, device=dev())
+    rng = np.random.default_rng(3)
+    N, U = 256, 384
+    O_true = ws.random_object(rng, U)
+    P = ws.aperture_probe(N, 60, 8, 0.0005)
+    R = -np.array([(i, j) for i in range(0, 129, 32) for j in range(0, 129, 32)], dtype=np.int64)
+    from gpu_util import Plan
+    plan = Plan(len(R), N, N, U, U, R)
+    Od = torch.from_numpy(O_true.astype(np.complex64)).to(dev())
+    Pd = torch.from_numpy(P.astype(np.complex64)).to(dev())
+    I = torch.empty((len(R), N, N), dtype=torch.float32, device=dev())
+    _native.check(_native.load().pty_intensities(plan.h, p(Od), p(Pd), p(I), stream()))
+    st = ws.DownsampledStart(net, len(R), N, N, P, R)
+    O = st.run(I, U, U)
+    torch.cuda.synchronize()
+    st.close()
+    plan.close()
+    o = O.cpu().numpy()
+    assert o.shape == (U, U) and np.all(np.isfinite(o))
+    assert np.abs(o[128:256, 128:256]).min() > 0
+    assert np.all(o[:16, :16] == 0)
