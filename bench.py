@@ -588,16 +588,59 @@ def _era_to_nmse(torch, job, O_init, O_true, heat, target, max_iters):
             "reached": bool(err <= target)}
 
 
-def time_to_nmse(torch, dev, target=1e-3, max_iters=2000, warm_steps=2000, warm_frames=16384):
-    """Time to object NMSE <= target on the 128 x 128 / 100-frame workload
-    (known probe, object update only) against the synthetic ground truth:
-    plain FP32 GPU ERA from ones, and ERA from the learned warm start's
-    stitched object.  The warm start's network is first trained on the GPU
-    (warm_steps Adam steps of 32 frames from warm_frames frames of random
-    objects and probes); its inference + stitching time counts towards its
-    time to NMSE, its training time is reported beside it."""
+def workload_nmse_c1(exits_fn):
+    """The 256^2 / 1024-frame job of workload_c1 -- the same object, probe,
+    32 x 32 raster and Poisson noise at 1e6 photons per frame -- without the
+    additive background and the mask, reconstructed with the true probe (ERA
+    method 1).  With the background and probe retrieval of the full job no
+    start reaches object NMSE 1e-3 against the ground truth (ERA method 4
+    from the known background floors at 1.0e-3), and with the beamstop the
+    unconstrained lowest spatial frequencies drift, so every pixel is used."""
+    rng = np.random.default_rng(1)
+    N, U, side = 256, 1024, 32
+    w = Workload()
+    w.name = "c1n"
+    w.O_true = make_object(rng, U)
+    w.P_true = make_probe(N, 64, 8, 0.0005)
+    w.P0 = w.P_true
+    w.R = raster(rng, side, 24, 3, N, U)
+    I = exits_fn(w.O_true, w.P_true, w.R)
+    I = I * (1e6 / I.sum(axis=(1, 2), keepdims=True))
+    I = rng.poisson(I).astype(np.float32)
+    w.I = np.fft.fftshift(I, axes=(-2, -1))
+    w.M = np.ones((N, N), bool)
+    w.method = 1
+    w.N, w.U = N, U
+    return w
+
+
+def workload_heldout(exits_fn, seed=7):
+    """A held-out 20 x 20 scan of 128^2 frames (the warm start's frame size):
+    an object and a probe drawn like its training frames' (smooth random
+    object, aperture radius 24-40 px, quadratic phase 0.001-0.004) from a
+    seed its training never uses; step 16 px, +-2 px jitter, noise free,
+    known probe (ERA method 1)."""
+    rng = np.random.default_rng(seed)
+    N, side, step = 128, 20, 16
+    U = N + step * (side - 1) + 8
+    w = Workload()
+    w.name = "heldout"
+    w.O_true = make_object(rng, U)
+    w.P_true = make_probe(N, rng.uniform(24, 40), 4, rng.uniform(0.001, 0.004))
+    w.P0 = w.P_true
+    w.R = raster(rng, side, step, 2, N, U)
+    w.I = np.fft.fftshift(exits_fn(w.O_true, w.P_true, w.R), axes=(-2, -1)).astype(np.float32)
+    w.M = np.ones((N, N), bool)
+    w.method = 1
+    w.N, w.U = N, U
+    return w
+
+
+def _nmse_leg(torch, dev, net, w, target, max_iters):
+    """Plain FP32 ERA from the reference's default object of ones
+    (era.py:480-486) against ERA from the learned warm start, both to object
+    NMSE <= target against the synthetic ground truth."""
     from ptychography_gb300 import warmstart as ws
-    w = workload_c0(gpu_intensities)
     job = DeviceJob(w, dev)
     job.run("era", 1, 1)                         # heatmap of the known probe
     torch.cuda.synchronize()
@@ -612,37 +655,93 @@ def time_to_nmse(torch, dev, target=1e-3, max_iters=2000, warm_steps=2000, warm_
         job.O.copy_(ones)
         job.run("era", 1, 1)
     plain = _era_to_nmse(torch, job, ones, O_true, heat, target, max_iters)
-    # the learned warm start
-    net = ws.WarmStartNet(w.N, w.N, seed=0, device=dev)
+    I_dev = torch.from_numpy(np.ascontiguousarray(w.I, dtype=np.float32)).to(dev)
+    R_sh = w.R - w.R.max(axis=0)
+    # set-up (the coarse probe, plan and buffers), like the main plan: untimed
+    st = ws.DownsampledStart(net, I_dev.shape[0], w.N, w.N, w.P0, R_sh)
+    st.run(I_dev, U, V)                          # first call: kernels, tiles, tensor maps
+    torch.cuda.synchronize()
     t0 = time.perf_counter()
-    data = ws.make_training_set(net, warm_frames, seed=1)
+    O_ws = st.run(I_dev, U, V)
+    torch.cuda.synchronize()
+    stitch_s = time.perf_counter() - t0
+    st.close()
+    warm = _era_to_nmse(torch, job, O_ws, O_true, heat, target, max_iters)
+    warm["inference_stitch_seconds"] = round(stitch_s, 5)
+    warm["seconds_total"] = round(stitch_s + warm["seconds"], 5)
+    job.close()
+    return {"plain_era": plain, "warm_start": warm,
+            "iterations": plain["iterations"], "seconds": plain["seconds"], "reached": plain["reached"],
+            "nmse": plain["nmse"],
+            "warm_start_speedup": round(plain["seconds"] / warm["seconds_total"], 3)
+            if warm["seconds_total"] > 0 and warm["reached"] else None}
+
+
+def time_to_nmse(torch, dev, target=1e-3, max_iters=400, warm_steps=3000, warm_frames=50000):
+    """Time to object NMSE <= target (illuminated region, global complex scale
+    removed, against the synthetic ground truth): plain FP32 GPU ERA from
+    ones against ERA from the learned warm start's stitched object.
+
+    The network (128^2 frames) is trained first on the GPU: warm_steps Adam
+    steps of 32 frames from warm_frames simulated frames (random objects with
+    smoothing widths 2-4 px, random probes, Poisson noise at 1e5-1e7
+    photons).  Two scans are then reconstructed: the 256^2 / 1024-frame
+    geometry (workload_nmse_c1; the network sees each frame at half
+    resolution, the central 128^2 of its pattern, and the stitched object is
+    upsampled) and a held-out 20 x 20 scan of 128^2 frames
+    (workload_heldout).  The warm start's inference + stitching is wall clock
+    (host work included) and counts towards its time; its training time is
+    reported beside it."""
+    from ptychography_gb300 import warmstart as ws
+    net = ws.WarmStartNet(128, 128, seed=0, device=dev)
+    t0 = time.perf_counter()
+    data = ws.make_training_set(net, warm_frames, seed=1, sigma=(2.0, 4.0), photons=(1e5, 1e7))
     torch.cuda.synchronize()
     t1 = time.perf_counter()
     losses = ws.train(net, data, warm_steps, batch=32, lr=3e-4)
     t2 = time.perf_counter()
     del data
-    I_dev = torch.from_numpy(w.I.astype(np.float32)).to(dev)
-    ws.warm_start_object(net, I_dev, job.P, job.plan, U, V)        # warm-up
-    holder = {}
-    stitch_s = event_time(torch, lambda: holder.update(O=ws.warm_start_object(net, I_dev, job.P, job.plan,
-                                                                               U, V)), 1)
-    warm = _era_to_nmse(torch, job, holder["O"], O_true, heat, target, max_iters)
-    warm["inference_stitch_seconds"] = round(stitch_s, 5)
-    warm["seconds_total"] = round(stitch_s + warm["seconds"], 5)
-    warm["training"] = {"steps": warm_steps, "batch": 32, "frames": warm_frames,
-                        "data_seconds": round(t1 - t0, 2), "train_seconds": round(t2 - t1, 2),
-                        "loss_first_20": float(np.mean(losses[:20])), "loss_last_20": float(np.mean(losses[-20:])),
-                        "input": "back-projection ifftn(sqrt(I) exp(i angle fftn P)) conj(P), (Re, Im)",
-                        "target": "object phase under the probe (cos, sin), weights |P|^2",
-                        "kernels": "pty_ws_*: im2col + BF16 mma.sync GEMMs, FP32 accumulation"}
+    torch.cuda.empty_cache()
+    c1 = _nmse_leg(torch, dev, net, workload_nmse_c1(gpu_intensities), target, max_iters)
+    held = _nmse_leg(torch, dev, net, workload_heldout(gpu_intensities), target, max_iters)
+    out = {"workload": "ERA m1 (known probe), 1024 frames 256x256, object 1006x1006 (1024x1024 truth), "
+                       "32x32 raster step 24 +-3, Poisson 1e6, no background, no mask",
+           "reference_object": "synthetic ground truth (illuminated region, global scale removed)",
+           "target": target}
+    out.update(c1)
+    out["warm_start"]["downsampling"] = "network at 128x128: central 128^2 of each 256^2 pattern, object upsampled x2"
+    out["warm_start"]["training"] = {
+        "steps": warm_steps, "batch": 32, "frames": warm_frames,
+        "data_seconds": round(t1 - t0, 2), "train_seconds": round(t2 - t1, 2),
+        "loss_first_20": float(np.mean(losses[:20])), "loss_last_20": float(np.mean(losses[-20:])),
+        "input": "back-projection ifftn(sqrt(I) exp(i angle fftn P)) conj(P), (Re, Im)",
+        "target": "object phase under the probe (cos, sin), weights |P|^2",
+        "kernels": "inference: tcgen05 implicit-GEMM convolutions (layers 1-4), direct CUDA-core convolutions "
+                   "(layers 0, 5); training: im2col + mma.sync GEMMs"}
+    out["warm_start"]["timing"] = ("inference + stitching + upsampling wall clock after an untimed set-up of "
+                                   "the coarse plan (as the main plan is set up untimed)")
+    held["workload"] = "held-out 20x20 scan, 400 frames 128x128, ERA m1 (known probe), noise free"
+    out["heldout_20x20"] = held
+    return out
+
+
+def c4_rate(torch, dev, steps=5, warmup=2):
+    """The 4096-frame 512 x 512 DM method-6 job (DeviceWorkload) timed beside
+    the headline: device-resident iterations, CUDA events.  Its error against
+    the chunked FP64 oracle is checked by tests/test_gpu_c4_fp64.py."""
+    w = DeviceWorkload(dev)
+    job = DeviceJob(w, dev)
+    for _ in range(warmup):
+        job.step()
+    t = event_time(torch, job.step, steps) / steps
+    out = {"workload": workload_config("c4")["workload"], "frame_iters_per_s": round(job.n / t, 1),
+           "ms_per_iter": round(t * 1e3, 3), "steps": steps, "warmup": warmup,
+           "error_vs_fp64": "tests/test_gpu_c4_fp64.py: 3 DM iterations against the chunked FP64 oracle; "
+                            "O (illuminated) / P / background within 3e-5"}
     job.close()
-    return {"workload": "ERA m1 (known probe), 100 frames 128x128, object 320x320",
-            "reference_object": "synthetic ground truth (illuminated region, global scale removed)",
-            "target": target, "plain_era": plain, "warm_start": warm,
-            "iterations": plain["iterations"], "seconds": plain["seconds"], "reached": plain["reached"],
-            "nmse": plain["nmse"],
-            "warm_start_speedup": round(plain["seconds"] / warm["seconds_total"], 3)
-            if warm["seconds_total"] > 0 else None}
+    del job, w
+    torch.cuda.empty_cache()
+    return out
 
 
 def e2e_public_api(w, K):
@@ -826,9 +925,11 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-nmse", action="store_true")
+    ap.add_argument("--no-c4", action="store_true",
+                    help="skip the 4096-frame 512x512 DM measurement")
     ap.add_argument("--no-batch", action="store_true",
                     help="skip the 64-reconstruction batched measurement")
-    ap.add_argument("--warm-steps", type=int, default=2000,
+    ap.add_argument("--warm-steps", type=int, default=3000,
                     help="training steps of the warm start's network in the time-to-NMSE measurement")
     ap.add_argument("--frame-tile", type=int, default=0,
                     help="force this frame tile (CTAs per frame; see pty_set_frame_tile) for profiling")
@@ -920,6 +1021,8 @@ def main():
         line["time_to_nmse"] = time_to_nmse(torch, dev, warm_steps=args.warm_steps)
     if args.workload == "c1" and not args.no_batch:
         line["batched"] = batched_rate(dev)
+    if args.workload == "c1" and not args.no_c4:
+        line["c4"] = c4_rate(torch, dev)
     print(json.dumps(line))
     return 0
 
