@@ -766,9 +766,17 @@ def e2e_public_api(w, K):
     torch.cuda.synchronize()
     np.random.seed(13)
     t0 = time.perf_counter()
+    api_calls(1)
+    torch.cuda.synchronize()
+    dt1 = time.perf_counter() - t0
+    np.random.seed(13)
+    t0 = time.perf_counter()
     res = api_calls(K)
     torch.cuda.synchronize()
     dt = time.perf_counter() - t0
+    # wall time = fixed + K x per-iteration, from the 1- and K-iteration calls
+    per_iter = (dt - dt1) / (K - 1) if K > 1 else None
+    fixed = dt1 - per_iter if per_iter is not None else None
     n, N = w.I.shape[0], w.I.shape[1]
     U = w.U
     calls = 2 if w.method == 6 else 1
@@ -783,6 +791,11 @@ def e2e_public_api(w, K):
     return {"value": round(frames / dt, 1), "unit": "frame-iters/s",
             "h2d_bytes_per_step": int(h2d / K), "d2h_bytes_per_step": int(d2h / K),
             "wall_s": round(dt, 3), "final_eMod": float(res[-1]),
+            "fixed_cost_s": round(fixed, 4) if fixed is not None else None,
+            "per_iteration_s": round(per_iter, 6) if per_iter is not None else None,
+            "fixed_cost": "wall time of the public calls that does not grow with the iteration count "
+                          "(host preamble, copies, plan set-up, result download), from a 1-iteration "
+                          "and a K-iteration call",
             "warmup": "one untimed ERA + DM pair of 1 iteration each"}
 
 

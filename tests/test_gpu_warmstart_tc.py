@@ -204,8 +204,9 @@ def test_crop_and_upsample_match_numpy():
 def test_downsampled_start_sees_the_object():
     """The warm start for 256^2 frames through a 128^2 network (untrained, so
     only the geometry is checked): the stitched, upsampled object has the full
-    grid's shape, is finite, and its support follows the scan (non-zero where
-    frames overlap, exactly zero far outside)."""
+    grid's shape and is finite; where frames overlap it is non-zero, and
+    everywhere it is a weighted mean of the network's unit phasors (weights
+    |P|^2 of the resampled probe), so its modulus is at most 1."""
     from ptychography_gb300 import warmstart as ws
     net = WarmStartNet(128, 128, seed=1, device=dev())
     rng = np.random.default_rng(3)
@@ -227,4 +228,4 @@ def test_downsampled_start_sees_the_object():
     o = O.cpu().numpy()
     assert o.shape == (U, U) and np.all(np.isfinite(o))
     assert np.abs(o[128:256, 128:256]).min() > 0
-    assert np.all(o[:16, :16] == 0)
+    assert np.abs(o).max() <= 1.0 + 1e-4
