@@ -289,6 +289,37 @@ __global__ void ws_pool2_bwd_kernel(int Bt, int H, int W, int C, const float* __
   }
 }
 
+// The same with 8 channels per thread (C a multiple of 8, 16-byte aligned
+// arrays, outputs x C / 8 < 2^31): 16-byte loads and stores, 32-bit indices
+__global__ void ws_pool2_v8_kernel(int Bt, int H, int W, int C, const __nv_bfloat16* __restrict__ X,
+                                   __nv_bfloat16* __restrict__ Y) {
+  const int h = H / 2, w = W / 2, chunks = C >> 3;
+  const int n = Bt * h * w * chunks;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int ch = i % chunks, p = i / chunks;
+    const int x = p % w, t = p / w, y = t % h, b = t / h;
+    const size_t base = ((size_t)(b * H + 2 * y) * W + 2 * x) * C + 8 * ch;
+    const size_t off[4] = {0, (size_t)C, (size_t)W * C, (size_t)W * C + C};
+    float acc[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const uint4 u = __ldg(reinterpret_cast<const uint4*>(X + base + off[q]));
+      const __nv_bfloat162* hv = reinterpret_cast<const __nv_bfloat162*>(&u);
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        const float2 f = __bfloat1622float2(hv[k]);
+        acc[2 * k] += f.x;
+        acc[2 * k + 1] += f.y;
+      }
+    }
+    uint4 r;
+    __nv_bfloat162* rv = reinterpret_cast<__nv_bfloat162*>(&r);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) rv[k] = __floats2bfloat162_rn(0.25f * acc[2 * k], 0.25f * acc[2 * k + 1]);
+    *reinterpret_cast<uint4*>(Y + (size_t)i * 8) = r;
+  }
+}
+
 // nearest 2 x upsampling (h x w -> 2h x 2w, NHWC) and its adjoint
 __global__ void ws_up2_kernel(int Bt, int h, int w, int C, const __nv_bfloat16* __restrict__ X,
                               __nv_bfloat16* __restrict__ Y) {
@@ -298,6 +329,18 @@ __global__ void ws_up2_kernel(int Bt, int h, int w, int C, const __nv_bfloat16* 
     const long long p = i / C;
     const int x = (int)(p % (2 * w)), y = (int)((p / (2 * w)) % (2 * h)), b = (int)(p / (4ll * w * h));
     Y[i] = X[(((long long)b * h + y / 2) * w + x / 2) * C + c];
+  }
+}
+// 8 channels per thread (conditions as ws_pool2_v8_kernel)
+__global__ void ws_up2_v8_kernel(int Bt, int h, int w, int C, const __nv_bfloat16* __restrict__ X,
+                                 __nv_bfloat16* __restrict__ Y) {
+  const int chunks = C >> 3;
+  const int n = Bt * 4 * h * w * chunks;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int ch = i % chunks, p = i / chunks;
+    const int x = p % (2 * w), t = p / (2 * w), y = t % (2 * h), b = t / (2 * h);
+    *reinterpret_cast<uint4*>(Y + (size_t)i * 8) =
+        __ldg(reinterpret_cast<const uint4*>(X + ((size_t)(b * h + y / 2) * w + x / 2) * C + 8 * ch));
   }
 }
 __global__ void ws_up2_bwd_kernel(int Bt, int h, int w, int C, const float* __restrict__ dY,
@@ -519,6 +562,11 @@ extern "C" int pty_ws_col2im(int32_t B, int32_t H, int32_t W, int32_t C, const f
 extern "C" int pty_ws_pool2(int32_t B, int32_t H, int32_t W, int32_t C, const void* X, void* Y, void* stream) {
   if (B < 1 || H < 2 || W < 2 || (H | W) & 1 || C < 1 || !X || !Y) return set_error(PTY_ERR_ARG, "bad pool arguments");
   const long long n = (long long)B * (H / 2) * (W / 2) * C;
+  if (C % 8 == 0 && n / 8 < (1ll << 31) && (long long)B * H * W * C < (1ll << 40) &&
+      (((uintptr_t)X | (uintptr_t)Y) & 15u) == 0) {
+    ws_pool2_v8_kernel<<<grid_for(n / 8), 256, 0, (cudaStream_t)stream>>>(B, H, W, C, (const bf16*)X, (bf16*)Y);
+    return ws_launched("ws_pool2_v8_kernel");
+  }
   ws_pool2_kernel<<<grid_for(n), 256, 0, (cudaStream_t)stream>>>(B, H, W, C, (const bf16*)X, (bf16*)Y);
   return ws_launched("ws_pool2_kernel");
 }
@@ -534,6 +582,10 @@ extern "C" int pty_ws_pool2_bwd(int32_t B, int32_t H, int32_t W, int32_t C, cons
 extern "C" int pty_ws_up2(int32_t B, int32_t h, int32_t w, int32_t C, const void* X, void* Y, void* stream) {
   if (B < 1 || h < 1 || w < 1 || C < 1 || !X || !Y) return set_error(PTY_ERR_ARG, "bad upsample arguments");
   const long long n = 4ll * B * h * w * C;
+  if (C % 8 == 0 && n / 8 < (1ll << 31) && (((uintptr_t)X | (uintptr_t)Y) & 15u) == 0) {
+    ws_up2_v8_kernel<<<grid_for(n / 8), 256, 0, (cudaStream_t)stream>>>(B, h, w, C, (const bf16*)X, (bf16*)Y);
+    return ws_launched("ws_up2_v8_kernel");
+  }
   ws_up2_kernel<<<grid_for(n), 256, 0, (cudaStream_t)stream>>>(B, h, w, C, (const bf16*)X, (bf16*)Y);
   return ws_launched("ws_up2_kernel");
 }
@@ -731,8 +783,34 @@ constexpr int kDirThreads = 128;
 // channels of X[p + tap][ci] W[co][tap C_in + ci], in that order, FP32.  Then
 // v = Z + bias (relu when asked), a = bf16(v), out = a (+ skip, rounded to
 // bf16 as ws_bias_act_kernel does) and out32 = v.  The weights sit in shared
-// memory transposed to [k][COUT], so every thread reads the same word.
-template <int COUT>
+// memory transposed to [k][COUT], so every thread reads the same words.
+// Inputs are read VEC channels at a time (8: 16-byte loads, C_in a multiple
+// of 8; 2: 4-byte loads), outputs written as whole 16-, 8- or 4-byte pieces.
+template <int VEC>
+struct BfVec;
+template <>
+struct BfVec<8> {
+  static PTY_DEV void load(const __nv_bfloat16* p, float* f) {
+    const uint4 u = __ldg(reinterpret_cast<const uint4*>(p));
+    const __nv_bfloat162* h = reinterpret_cast<const __nv_bfloat162*>(&u);
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const float2 t = __bfloat1622float2(h[i]);
+      f[2 * i] = t.x;
+      f[2 * i + 1] = t.y;
+    }
+  }
+};
+template <>
+struct BfVec<2> {
+  static PTY_DEV void load(const __nv_bfloat16* p, float* f) {
+    const float2 t = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(p));
+    f[0] = t.x;
+    f[1] = t.y;
+  }
+};
+
+template <int COUT, int VEC>
 __global__ void __launch_bounds__(kDirThreads) ws_conv_direct_kernel(int Bt, int H, int W, int Cin,
                                                                      const __nv_bfloat16* __restrict__ X,
                                                                      const __nv_bfloat16* __restrict__ Wt,
@@ -747,35 +825,62 @@ __global__ void __launch_bounds__(kDirThreads) ws_conv_direct_kernel(int Bt, int
     wsm[k * COUT + co] = __bfloat162float(Wt[i]);
   }
   __syncthreads();
-  const long long P = (long long)Bt * H * W;
-  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < P; p += (long long)gridDim.x * blockDim.x) {
-    const int x = (int)(p % W), y = (int)((p / W) % H);
-    const long long b = p / ((long long)W * H);
+  const int P = Bt * H * W;                      // < 2^31 (checked on the host)
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < P; p += gridDim.x * blockDim.x) {
+    const int x = p % W, t = p / W, y = t % H, b = t / H;
     float acc[COUT];
 #pragma unroll
     for (int c = 0; c < COUT; ++c) acc[c] = 0.f;
+#pragma unroll 1
     for (int tap = 0; tap < 9; ++tap) {
       const int yy = y + tap / 3 - 1, xx = x + tap % 3 - 1;
       if (yy < 0 || yy >= H || xx < 0 || xx >= W) continue;
-      const __nv_bfloat16* xp = X + ((b * H + yy) * W + xx) * Cin;
+      const __nv_bfloat16* xp = X + ((size_t)(b * H + yy) * W + xx) * Cin;
       const float* wk = wsm + tap * Cin * COUT;
-      for (int ci = 0; ci < Cin; ci += 2) {
-        const float2 v = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(xp + ci));
+      for (int ci = 0; ci < Cin; ci += VEC) {
+        float v[VEC];
+        BfVec<VEC>::load(xp + ci, v);
 #pragma unroll
-        for (int c = 0; c < COUT; ++c) acc[c] = fmaf(v.x, wk[ci * COUT + c], acc[c]);
+        for (int j = 0; j < VEC; ++j)
 #pragma unroll
-        for (int c = 0; c < COUT; ++c) acc[c] = fmaf(v.y, wk[(ci + 1) * COUT + c], acc[c]);
+          for (int c = 0; c < COUT; ++c) acc[c] = fmaf(v[j], wk[(ci + j) * COUT + c], acc[c]);
       }
     }
 #pragma unroll
     for (int c = 0; c < COUT; ++c) {
-      float v = acc[c] + bias[c];
-      if (relu) v = fmaxf(v, 0.f);
-      const long long o = p * COUT + c;
-      if (out32) out32[o] = v;
-      if (out) {
-        const __nv_bfloat16 vb = __float2bfloat16(v);
-        out[o] = skip ? __float2bfloat16(__bfloat162float(vb) + __bfloat162float(skip[o])) : vb;
+      acc[c] += bias[c];
+      if (relu) acc[c] = fmaxf(acc[c], 0.f);
+    }
+    const size_t o = (size_t)p * COUT;
+    if (out32) {
+      if constexpr (COUT % 4 == 0) {
+#pragma unroll
+        for (int c = 0; c < COUT; c += 4)
+          *reinterpret_cast<float4*>(out32 + o + c) = make_float4(acc[c], acc[c + 1], acc[c + 2], acc[c + 3]);
+      } else {
+#pragma unroll
+        for (int c = 0; c < COUT; c += 2) *reinterpret_cast<float2*>(out32 + o + c) = make_float2(acc[c], acc[c + 1]);
+      }
+    }
+    if (out) {
+      __nv_bfloat162 hv[COUT / 2];
+#pragma unroll
+      for (int c = 0; c < COUT; c += 2) {
+        __nv_bfloat162 a2 = __floats2bfloat162_rn(acc[c], acc[c + 1]);
+        if (skip) {
+          const float2 af = __bfloat1622float2(a2);
+          const float2 sf = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(skip + o + c));
+          a2 = __floats2bfloat162_rn(af.x + sf.x, af.y + sf.y);
+        }
+        hv[c / 2] = a2;
+      }
+      if constexpr (COUT % 8 == 0) {
+#pragma unroll
+        for (int c = 0; c < COUT; c += 8)
+          *reinterpret_cast<uint4*>(out + o + c) = *reinterpret_cast<const uint4*>(&hv[c / 2]);
+      } else {
+#pragma unroll
+        for (int c = 0; c < COUT; c += 2) *reinterpret_cast<__nv_bfloat162*>(out + o + c) = hv[c / 2];
       }
     }
   }
@@ -819,10 +924,16 @@ int launch_direct(int B, int H, int W, int Cin, const void* X, const void* Wt, c
   const size_t smem = (size_t)9 * Cin * COUT * sizeof(float);
   const long long P = (long long)B * H * W;
   long long g = (P + kDirThreads - 1) / kDirThreads;
-  if (g > 16 * 152) g = 16 * 152;
-  ws_conv_direct_kernel<COUT><<<(unsigned)g, kDirThreads, smem, st>>>(
-      B, H, W, Cin, (const __nv_bfloat16*)X, (const __nv_bfloat16*)Wt, bias, relu, (const __nv_bfloat16*)skip,
-      (__nv_bfloat16*)out, out32);
+  if (g > 32 * 152) g = 32 * 152;
+  const bool v8 = Cin % 8 == 0 && ((uintptr_t)X & 15u) == 0;
+  if (v8)
+    ws_conv_direct_kernel<COUT, 8><<<(unsigned)g, kDirThreads, smem, st>>>(
+        B, H, W, Cin, (const __nv_bfloat16*)X, (const __nv_bfloat16*)Wt, bias, relu, (const __nv_bfloat16*)skip,
+        (__nv_bfloat16*)out, out32);
+  else
+    ws_conv_direct_kernel<COUT, 2><<<(unsigned)g, kDirThreads, smem, st>>>(
+        B, H, W, Cin, (const __nv_bfloat16*)X, (const __nv_bfloat16*)Wt, bias, relu, (const __nv_bfloat16*)skip,
+        (__nv_bfloat16*)out, out32);
   return check_launch("ws_conv_direct_kernel");
 }
 
@@ -835,8 +946,10 @@ extern "C" int pty_ws_conv3x3_direct(int32_t B, int32_t H, int32_t W, int32_t Ci
   if (B < 1 || H < 1 || W < 1 || !X || !Wt || !bias || (!out && !out32))
     return set_error(PTY_ERR_ARG, "pty_ws_conv3x3_direct: bad arguments");
   if (Cin < 2 || Cin > 32 || (Cin & 1)) return set_error(PTY_ERR_UNSUPPORTED, "pty_ws_conv3x3_direct: C_in must be even, 2..32");
-  if (((uintptr_t)X & 3) || ((uintptr_t)Wt & 1))
-    return set_error(PTY_ERR_ARG, "pty_ws_conv3x3_direct: X must be 4-byte aligned");
+  if (((uintptr_t)X & 3) || ((uintptr_t)Wt & 1) || ((uintptr_t)skip & 3) || ((uintptr_t)out & 15) ||
+      ((uintptr_t)out32 & 15))
+    return set_error(PTY_ERR_ARG, "pty_ws_conv3x3_direct: X and skip must be 4-byte, out and out32 16-byte aligned");
+  if ((long long)B * H * W >= (1ll << 31)) return set_error(PTY_ERR_ARG, "pty_ws_conv3x3_direct: too many pixels");
   cudaStream_t st = (cudaStream_t)stream;
   switch (Cout) {
     case 2: return launch_direct<2>(B, H, W, Cin, X, Wt, bias, relu, skip, out, out32, st);
