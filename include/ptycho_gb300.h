@@ -283,12 +283,14 @@ int pty_ws_conv3x3_direct(int32_t B, int32_t H, int32_t W, int32_t Cin, int32_t 
                           float* out32, void* stream);
 /* Pieces of the warm start for frames larger than the network's (the frame
  * at a coarser real-space sampling):
- *   pty_ws_crop_center: out[f][a][b] = scale * I[f][a + (N0 - M0) / 2][b + (N1 - M1) / 2],
- *     the central M0 x M1 of each centred pattern (float, device);
+ *   pty_ws_crop_center: out[f][a][b] = scale * I[g][a + (N0 - M0) / 2][b + (N1 - M1) / 2],
+ *     g = frames[f] (a device int32 list, each entry a frame of I) or f when
+ *     frames is NULL: the central M0 x M1 of each chosen centred pattern
+ *     (float, device);
  *   pty_ws_upsample_object: O[u][v] = bilinear sample of Oh (Uh x Vh) at
  *     (u / f, v / f), clamped at the edges (complex64, device). */
 int pty_ws_crop_center(int32_t nf, int32_t N0, int32_t N1, int32_t M0, int32_t M1, const float* I,
-                       float scale, float* out, void* stream);
+                       const int32_t* frames, float scale, float* out, void* stream);
 int pty_ws_upsample_object(int32_t Uh, int32_t Vh, const void* Oh, int32_t U, int32_t V, int32_t f,
                            void* O, void* stream);
 int pty_ws_conv3x3_tc(int32_t B, int32_t H, int32_t W, int32_t Cin, int32_t Cout, const void* X,

@@ -886,17 +886,18 @@ __global__ void __launch_bounds__(kDirThreads) ws_conv_direct_kernel(int Bt, int
   }
 }
 
-// out[f][a][b] = scale I[f][a + (N0 - M0) / 2][b + (N1 - M1) / 2]: the
-// central M0 x M1 of each centred pattern
+// out[f][a][b] = scale I[g][a + (N0 - M0) / 2][b + (N1 - M1) / 2], g = frames[f]
+// (or f): the central M0 x M1 of each (chosen) centred pattern
 __global__ void ws_crop_center_kernel(long long nf, int N0, int N1, int M0, int M1, const float* __restrict__ I,
-                                      float scale, float* __restrict__ out) {
+                                      const int* __restrict__ frames, float scale, float* __restrict__ out) {
   const long long n = nf * M0 * M1;
   const int o0 = (N0 - M0) / 2, o1 = (N1 - M1) / 2;
   WS_LOOP(i, n) {
     const long long f = i / ((long long)M0 * M1);
     const int r = (int)(i % ((long long)M0 * M1));
     const int a = r / M1, b = r - a * M1;
-    out[i] = scale * I[(f * N0 + a + o0) * N1 + b + o1];
+    const long long g = frames ? (long long)frames[f] : f;
+    out[i] = scale * I[(g * N0 + a + o0) * N1 + b + o1];
   }
 }
 
@@ -962,11 +963,11 @@ extern "C" int pty_ws_conv3x3_direct(int32_t B, int32_t H, int32_t W, int32_t Ci
 }
 
 extern "C" int pty_ws_crop_center(int32_t nf, int32_t N0, int32_t N1, int32_t M0, int32_t M1, const float* I,
-                                  float scale, float* out, void* stream) {
+                                  const int32_t* frames, float scale, float* out, void* stream) {
   if (nf < 1 || M0 < 1 || M1 < 1 || M0 > N0 || M1 > N1 || !I || !out)
     return set_error(PTY_ERR_ARG, "pty_ws_crop_center: bad arguments");
   const long long n = (long long)nf * M0 * M1;
-  ws_crop_center_kernel<<<grid_for(n), 256, 0, (cudaStream_t)stream>>>(nf, N0, N1, M0, M1, I, scale, out);
+  ws_crop_center_kernel<<<grid_for(n), 256, 0, (cudaStream_t)stream>>>(nf, N0, N1, M0, M1, I, frames, scale, out);
   return ws_launched("ws_crop_center_kernel");
 }
 

@@ -480,6 +480,59 @@ def initial_object(net, I, R, P, O_shape=None, alpha=1e-10):
         plan.close()
 
 
+def covering_frames(R, P, frac=0.3, lit=1e-2):
+    """A subset of a scan's frames that still lights the whole object, for a
+    warm start that needs each object pixel seen once, not every time the
+    scan revisits it.  R: (n, 2) scan offsets with maximum 0 (the plan's),
+    P: the probe (N0, N1).  Host work (set-up, once per scan).
+
+    Frames are taken outermost first (distance of their offset from the
+    scan's mean) whenever their offset is at least r from every frame taken,
+    r the radius of the probe's half-maximum intensity disc; then, for every
+    object pixel the full scan lights (sum of |P|^2 over all frames above
+    `lit` of its maximum) where no taken frame's |P|^2 reaches `frac` of the
+    best any frame gives it, the frame giving it most is added.  Returns the
+    sorted frame indices."""
+    R = np.asarray(R, np.int64)[:, :2]
+    n = len(R)
+    p2 = np.abs(np.asarray(P)) ** 2
+    N0, N1 = p2.shape
+    U, V = N0 + int(R[:, 0].max() - R[:, 0].min()), N1 + int(R[:, 1].max() - R[:, 1].min())
+    heat = np.zeros((U, V))
+    best_all = np.zeros((U, V))
+    for r0, r1 in R:
+        w = (slice(-r0, -r0 + N0), slice(-r1, -r1 + N1))
+        heat[w] += p2
+        np.maximum(best_all[w], p2, out=best_all[w])
+    radius = np.sqrt(np.count_nonzero(p2 >= 0.5 * p2.max()) / np.pi)
+    pos = -R.astype(np.float64)
+    order = np.argsort(-np.hypot(*(pos - pos.mean(axis=0)).T), kind="stable")
+    taken = np.zeros(n, bool)
+    kept = np.empty((0, 2))
+    for f in order:
+        if len(kept) == 0 or np.min(np.hypot(*(kept - pos[f]).T)) >= radius:
+            taken[f] = True
+            kept = np.vstack((kept, pos[f]))
+    best = np.zeros((U, V))
+    for f in np.flatnonzero(taken):
+        w = (slice(-R[f, 0], -R[f, 0] + N0), slice(-R[f, 1], -R[f, 1] + N1))
+        np.maximum(best[w], p2, out=best[w])
+    region = heat > lit * heat.max()
+    while True:
+        short = np.flatnonzero((region & (best < frac * best_all)).ravel())
+        if len(short) == 0:
+            break
+        u, v = divmod(int(short[0]), V)
+        a, b = u + R[:, 0], v + R[:, 1]                 # the pixel in each frame
+        inside = (a >= 0) & (a < N0) & (b >= 0) & (b < N1) & ~taken
+        cand = np.flatnonzero(inside)
+        f = int(cand[np.argmax(p2[a[cand], b[cand]])])
+        taken[f] = True
+        w = (slice(-R[f, 0], -R[f, 0] + N0), slice(-R[f, 1], -R[f, 1] + N1))
+        np.maximum(best[w], p2, out=best[w])
+    return np.flatnonzero(taken)
+
+
 class DownsampledStart:
     """The warm start for frames larger than the network's, each frame seen
     at a coarser real-space sampling: the central net.H x net.W part of
@@ -490,13 +543,17 @@ class DownsampledStart:
     nearest coarse pixel) into a coarse object, which is bilinearly upsampled
     by f onto the full object grid.
 
-    Set-up (host work, once per scan: the coarse probe, the coarse plan and
-    buffers) happens here; run() is device work plus the network's batched
-    inference.  n frames of N x N with N = f net.H, the probe P (N, N)
+    With cover (the default) only the frames covering_frames picks go
+    through the network: each object pixel needs one good view for a start,
+    and on a dense scan that is a third to a quarter of the frames.
+
+    Set-up (host work, once per scan: the coarse probe, the frame subset, the
+    coarse plan and buffers) happens here; run() is device work plus the
+    network's batched inference.  n frames of N x N with N = f net.H, the probe P (N, N)
     (host array), R the plan's scan offsets (n, 2) with maximum 0.
     """
 
-    def __init__(self, net, n, N0, N1, P, R):
+    def __init__(self, net, n, N0, N1, P, R, cover=True):
         torch = _torch()
         if N0 != N1 or net.H != net.W or N0 % net.H:
             raise ValueError("frames must be square, a multiple of the network's %d x %d" % (net.H, net.W))
@@ -510,9 +567,19 @@ class DownsampledStart:
         Rs -= Rs.max(axis=0)
         self.Us = self.M + int(Rs[:, 0].max() - Rs[:, 0].min())
         self.Vs = self.M + int(Rs[:, 1].max() - Rs[:, 1].min())
-        self.plan = _FramePlan(self.n, self.M, self.Us, self.Vs, Rs)
-        self.I_s = torch.empty((self.n, self.M, self.M), dtype=torch.float32, device=net.dev)
-        self.heat = torch.empty((self.Us, self.Vs), dtype=torch.float64, device=net.dev)
+        # with cover, only a subset of frames that lights every pixel the scan
+        # lights (covering_frames) goes through the network
+        sel = covering_frames(Rs, Ps) if cover else np.arange(self.n)
+        self.frames = sel
+        self.sel = (torch.from_numpy(sel.astype(np.int32)).to(net.dev) if len(sel) < self.n else None)
+        Rsel = Rs[sel]
+        Rsel = Rsel - Rsel.max(axis=0)
+        self.shift = (Rs[sel].max(axis=0) - Rs.max(axis=0))      # window offset of the subset
+        self.Uc = self.M + int(Rsel[:, 0].max() - Rsel[:, 0].min())
+        self.Vc = self.M + int(Rsel[:, 1].max() - Rsel[:, 1].min())
+        self.plan = _FramePlan(len(sel), self.M, self.Uc, self.Vc, Rsel)
+        self.I_s = torch.empty((len(sel), self.M, self.M), dtype=torch.float32, device=net.dev)
+        self.heat = torch.empty((self.Uc, self.Vc), dtype=torch.float64, device=net.dev)
 
     def run(self, I_dev, U, V):
         """The initial object (U, V) complex64 on the device for the centred
@@ -521,9 +588,18 @@ class DownsampledStart:
         net, sp = self.net, self.net._sp()
         if tuple(I_dev.shape) != (self.n, self.N, self.N):
             raise ValueError("expected %d frames of %d x %d" % (self.n, self.N, self.N))
-        _native.check(net.lib.pty_ws_crop_center(self.n, self.N, self.N, self.M, self.M, _p(I_dev), 1.0,
+        k = self.I_s.shape[0]
+        _native.check(net.lib.pty_ws_crop_center(k, self.N, self.N, self.M, self.M, _p(I_dev), _p(self.sel), 1.0,
                                                  _p(self.I_s), sp))
-        O_s = warm_start_object(net, self.I_s, self.P_s, self.plan.h, self.Us, self.Vs, heat=self.heat)
+        O_c = warm_start_object(net, self.I_s, self.P_s, self.plan.h, self.Uc, self.Vc, heat=self.heat)
+        if (self.Uc, self.Vc) != (self.Us, self.Vs):
+            # the subset's object window inside the full scan's coarse object
+            # (outside it: ones, the default start)
+            O_s = torch.ones((self.Us, self.Vs), dtype=torch.complex64, device=net.dev)
+            a, b = int(-self.shift[0]), int(-self.shift[1])
+            O_s[a:a + self.Uc, b:b + self.Vc] = O_c
+        else:
+            O_s = O_c
         if self.f == 1:
             return O_s
         O = torch.empty((U, V), dtype=torch.complex64, device=net.dev)

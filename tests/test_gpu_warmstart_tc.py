@@ -184,8 +184,12 @@ def test_crop_and_upsample_match_numpy():
     I = rng.random((3, 32, 32)).astype(np.float32)
     Id = torch.from_numpy(I).to(dev())
     out = torch.empty((3, 16, 16), dtype=torch.float32, device=dev())
-    _native.check(lib.pty_ws_crop_center(3, 32, 32, 16, 16, p(Id), 0.5, p(out), stream()))
+    _native.check(lib.pty_ws_crop_center(3, 32, 32, 16, 16, p(Id), None, 0.5, p(out), stream()))
     np.testing.assert_array_equal(out.cpu().numpy(), 0.5 * I[:, 8:24, 8:24])
+    sel = torch.tensor([2, 0], dtype=torch.int32, device=dev())
+    out2 = torch.empty((2, 16, 16), dtype=torch.float32, device=dev())
+    _native.check(lib.pty_ws_crop_center(2, 32, 32, 16, 16, p(Id), p(sel), 1.0, p(out2), stream()))
+    np.testing.assert_array_equal(out2.cpu().numpy(), I[[2, 0], 8:24, 8:24])
     Oh = (rng.standard_normal((7, 9)) + 1j * rng.standard_normal((7, 9))).astype(np.complex64)
     Ohd = torch.from_numpy(Oh).to(dev())
     U, V, f = 15, 20, 2

@@ -43,3 +43,31 @@ def test_c_abi_rejects_bad_arguments_without_a_gpu():
     one = ctypes.c_void_p(16)                                          # never dereferenced: rejected first
     assert lib.pty_ws_prep_bp(1, 8, 7, one, one, 1, one, None) != 0     # odd side with the sign correction
     assert b"even" in lib.pty_last_error()
+
+
+def test_covering_frames_lights_every_pixel():
+    """The warm start's frame subset: on a dense jittered raster (step 12 px,
+    probe radius ~36 px at the network's sampling) it keeps well under half
+    the frames, and every pixel the full scan lights gets at least 30 % of
+    the best |P|^2 any frame gives it from some kept frame."""
+    rng = np.random.default_rng(2)
+    side, step, N = 32, 12, 128
+    pos = np.arange(side) * step
+    R = -np.stack(np.meshgrid(pos, pos, indexing="ij"), -1).reshape(-1, 2)
+    R = R + rng.integers(-1, 2, R.shape)
+    R = R - R.max(axis=0)
+    P = ws.aperture_probe(N, 32, 4.0, 0.002)
+    sel = ws.covering_frames(R, P)
+    assert 0 < len(sel) < 0.45 * len(R)
+    assert np.all(np.diff(sel) > 0)
+    p2 = np.abs(P) ** 2
+    U, V = N + int(R[:, 0].max() - R[:, 0].min()), N + int(R[:, 1].max() - R[:, 1].min())
+    heat, best_all, best = np.zeros((U, V)), np.zeros((U, V)), np.zeros((U, V))
+    for f, (r0, r1) in enumerate(R):
+        w = (slice(-r0, -r0 + N), slice(-r1, -r1 + N))
+        heat[w] += p2
+        best_all[w] = np.maximum(best_all[w], p2)
+        if f in set(sel.tolist()):
+            best[w] = np.maximum(best[w], p2)
+    lit = heat > 1e-2 * heat.max()
+    assert np.all(best[lit] >= 0.3 * best_all[lit])
