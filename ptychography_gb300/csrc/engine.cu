@@ -104,7 +104,6 @@ struct pty_plan {
   uint8_t* d_mask_blk = nullptr; // the mask in the staged tile's column-block order
   int stage_frames = 0;
   int* d_timeout = nullptr;      // the device's timeout flag (not owned)
-  StageLanes lanes;              // the staged tile's two lanes (staged plans only)
   int tile[2] = {1, 1};          // CTAs per frame of the fused frame kernels, per op family
   int eslots = 1;                // error-partial slots per frame (the larger family tile)
   int ndn = 304;                 // diffnorm blocks per array (two per SM)
@@ -187,11 +186,6 @@ extern "C" int pty_plan_destroy(pty_plan* p) {
   if (p->cap) cudaStreamDestroy(p->cap);
   if (p->ev_in) cudaEventDestroy(p->ev_in);
   if (p->ev_out) cudaEventDestroy(p->ev_out);
-  for (int l = 0; l < 2; ++l) {
-    if (p->lanes.s[l]) cudaStreamDestroy(p->lanes.s[l]);
-    if (p->lanes.join[l]) cudaEventDestroy(p->lanes.join[l]);
-  }
-  if (p->lanes.fork) cudaEventDestroy(p->lanes.fork);
   delete p;
   return PTY_OK;
 }
@@ -316,17 +310,6 @@ extern "C" int pty_plan_create(const pty_geometry* g, const int64_t* R_host, pty
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&p->cap, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&p->ev_in, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&p->ev_out, cudaEventDisableTiming);
-  if (e == cudaSuccess && p->d_stage) {
-    const int G = staged_lane_frames(N0, N1);
-    if (G > 0 && p->stage_frames >= 2 * G && n > G) {
-      for (int l = 0; l < 2 && e == cudaSuccess; ++l) {
-        e = cudaStreamCreateWithFlags(&p->lanes.s[l], cudaStreamNonBlocking);
-        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&p->lanes.join[l], cudaEventDisableTiming);
-      }
-      if (e == cudaSuccess) e = cudaEventCreateWithFlags(&p->lanes.fork, cudaEventDisableTiming);
-      if (e == cudaSuccess) p->lanes.frames = G;
-    }
-  }
   if (e != cudaSuccess) return fail(set_cuda_error(e, "pty_plan_create"));
   p->tl = TileLists{TR, T, ntu, ntv, p->d_tile_ptr, p->d_tile_frames};
   *out = p;
@@ -350,7 +333,6 @@ static FrameArgs base_args(const pty_plan* p) {
   a.stage_frames = p->stage_frames;
   a.mask_blk = p->d_mask_blk;
   a.timeout = p->d_timeout;
-  a.lanes = p->lanes.frames > 0 ? &p->lanes : nullptr;
   return a;
 }
 

@@ -24,16 +24,6 @@ enum FrameOp {
   OP_BP = 9,     // mask * sqrt(I) * exp(i arg FFT(P)) -> IFFT -> psi           (Back_projection)
 };
 
-// Two streams over which a staged tile pipelines its frame groups, so that a
-// group's scratch is still in L2 when the group's next launch reads it and the
-// launches of one lane fill the tails of the other's.  Host-only (a plan owns
-// it; kernels never read it).
-struct StageLanes {
-  cudaStream_t s[2] = {nullptr, nullptr};
-  cudaEvent_t fork = nullptr, join[2] = {nullptr, nullptr};
-  int frames = 0;            // frames per group and lane (0: one stream, groups of stage_frames)
-};
-
 struct FrameArgs {
   int U, V;                  // object shape
   const int* R;              // [n][2] scan offsets (<= 0), int32
@@ -59,7 +49,6 @@ struct FrameArgs {
   int stage_frames;          // frames the scratch holds (launches run in groups of it)
   uint8_t* mask_blk;         // [N0 * N1] mask in column-block order (staged tiles)
   int* timeout;              // set when a bounded wait of a kernel runs out
-  const StageLanes* lanes;   // host-only: the plan's lanes for a staged tile, or nullptr
 };
 
 // Frame tiles: how many CTAs transform one frame.  Tile 1 is the single-CTA
@@ -80,8 +69,6 @@ inline int tile_ctas(int tile) { return tile % 100; }
 inline bool tile_staged(int tile) { return tile >= 200; }
 // frames of scratch a staged tile works through at a time
 int staged_group_frames(int N0, int N1);
-// frames per group when a staged tile pipelines groups over two lanes (0: off)
-int staged_lane_frames(int N0, int N1);
 bool frame_shape_supported(int N0, int N1);
 int frame_tile_candidates(int N0, int N1, int* tiles, int cap);   // returns the count
 int max_frame_tile(int N0, int N1);

@@ -218,14 +218,6 @@ int staged_group_frames(int N0, int N1) {
   return g < 1 ? 1 : (int)g;
 }
 
-int staged_lane_frames(int N0, int N1) {
-  // PTY_STAGE_LANE_FRAMES overrides (tuning); 0 turns the two lanes off
-  if (const char* v = getenv("PTY_STAGE_LANE_FRAMES")) return atoi(v) > 0 ? atoi(v) : 0;
-  const long long per = (long long)N0 * N1 * (long long)sizeof(float2);
-  const long long g = ((long long)32 << 20) / per;     // 32 MiB of scratch per group
-  return g < 1 ? 1 : (int)g;
-}
-
 int frame_tile_candidates(int N0, int N1, int* tiles, int cap) {
   const ShapeTiles* s = find_shape(N0, N1);
   if (!s) return 0;

@@ -331,46 +331,6 @@ int launch(const FrameArgs& a, int nframes, cudaStream_t st) {
     mask_blocks_kernel<<<kBlocksPerFrame, kNT, 0, st>>>(a.mask, a.mask_blk);
     PTY_TRY(check_launch("mask_blocks_kernel"));
   }
-  const StageLanes* L = a.lanes;
-  const int G = L ? L->frames : 0;
-  if (G > 0 && nframes > G && a.stage_frames >= 2 * G) {
-    // groups of G frames alternate between two lanes, each with its own
-    // G-frame part of the scratch: a group's three launches run in order on
-    // its lane, the other lane's launches fill their gaps and tails, and a
-    // 32 MiB scratch part is still in L2 when the next launch reads it
-    ColMaps lm[2];
-    for (int l = 0; l < 2; ++l) {
-      lm[l] = maps;
-      PTY_TRY(frame_map(&lm[l].stage, a.stage + (size_t)l * G * kN * kN, CU_TENSOR_MAP_DATA_TYPE_UINT64, 8,
-                        (long long)kN * kN, G));
-    }
-    PTY_CUDA(cudaEventRecord(L->fork, st));
-    for (int l = 0; l < 2; ++l) PTY_CUDA(cudaStreamWaitEvent(L->s[l], L->fork, 0));
-    int rc = PTY_OK;
-    for (int g = 0, f0 = 0; f0 < nframes && rc == PTY_OK; ++g, f0 += G) {
-      const int l = g & 1, nf = nframes - f0 < G ? nframes - f0 : G;
-      cudaStream_t ls = L->s[l];
-      FrameArgs b = a;
-      b.stage = a.stage + (size_t)l * G * kN * kN;
-      const dim3 grid(nf * kBlocksPerFrame);
-      staged_rows_kernel<OP, false><<<grid, kNT, 0, ls>>>(b, f0);
-      rc = check_launch("staged_rows_kernel");
-      if (rc) break;
-      staged_cols_kernel<OP><<<grid, kNT, kColSmem, ls>>>(b, f0, lm[l], amp_frames, bg_frames);
-      rc = check_launch("staged_cols_kernel");
-      if (rc) break;
-      if constexpr (OpTraits<OP>::INVERSE) {
-        staged_rows_kernel<OP, true><<<grid, kNT, 0, ls>>>(b, f0);
-        rc = check_launch("staged_rows_kernel");
-      }
-    }
-    // join both lanes back (also after an error, so a capture stays well formed)
-    for (int l = 0; l < 2; ++l) {
-      PTY_CUDA(cudaEventRecord(L->join[l], L->s[l]));
-      PTY_CUDA(cudaStreamWaitEvent(st, L->join[l], 0));
-    }
-    return rc;
-  }
   for (int f0 = 0; f0 < nframes; f0 += a.stage_frames) {
     const int nf = nframes - f0 < a.stage_frames ? nframes - f0 : a.stage_frames;
     const dim3 grid(nf * kBlocksPerFrame);

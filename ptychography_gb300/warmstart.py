@@ -299,13 +299,14 @@ class WarmStartNet:
         _native.check(lib.pty_ws_prep_bp(n, H, W, _p(bp), _p(P), 1, _p(x), sp))
         return x
 
-    def predict_exits(self, I, P, plan_h, batch=256, tensor_cores=True):
+    def predict_exits(self, I, P, plan_h, batch=256, tensor_cores=True, phasors=None):
         """Exit waves P exp(i phase) (or |P| exp(i phase)) with the predicted
         phases, for the centred intensities I (n, H, W) float32 of the plan's
         frames and the probe P (H, W) complex64, both on the device."""
         torch = _torch()
         n = I.shape[0]
-        phasors = probe_phasors(P.cpu().numpy(), self.dev)
+        if phasors is None:
+            phasors = probe_phasors(P.cpu().numpy(), self.dev)
         x = self.input_from_intensities(plan_h, I, P, phasors)
         psi = torch.empty((n, self.H, self.W), dtype=torch.complex64, device=self.dev)
         for s in range(0, n, batch):
@@ -433,7 +434,7 @@ def train(net, data, steps, batch=32, lr=1e-3, seed=0, log_every=0):
     return hist.sum(dim=1, dtype=torch.float64).cpu().numpy().tolist()
 
 
-def warm_start_object(net, I_dev, P_dev, plan_h, U, V, alpha=1e-10, heat=None):
+def warm_start_object(net, I_dev, P_dev, plan_h, U, V, alpha=1e-10, heat=None, phasors=None):
     """The initial object for ERA: the network's exit waves for the centred
     intensities I_dev (n, N, N) float32, stitched by the overlap update
     (psup_O, era.py:336-369) with the probe P_dev on the plan's U x V grid.
@@ -444,7 +445,7 @@ def warm_start_object(net, I_dev, P_dev, plan_h, U, V, alpha=1e-10, heat=None):
     g = _native.plan_geometry(plan_h)
     if (g.U, g.V) != (U, V):
         raise ValueError("the plan's object is %d x %d, not %d x %d" % (g.U, g.V, U, V))
-    psi = net.predict_exits(I_dev, P_dev, plan_h)
+    psi = net.predict_exits(I_dev, P_dev, plan_h, phasors=phasors)
     O = torch.empty((U, V), dtype=torch.complex64, device=net.dev)
     if heat is None:
         heat = torch.empty((U, V), dtype=torch.float64, device=net.dev)
@@ -480,15 +481,16 @@ def initial_object(net, I, R, P, O_shape=None, alpha=1e-10):
         plan.close()
 
 
-def covering_frames(R, P, frac=0.3, lit=1e-2):
+def covering_frames(R, P, frac=0.3, lit=1e-2, spacing=1.0):
     """A subset of a scan's frames that still lights the whole object, for a
     warm start that needs each object pixel seen once, not every time the
     scan revisits it.  R: (n, 2) scan offsets with maximum 0 (the plan's),
     P: the probe (N0, N1).  Host work (set-up, once per scan).
 
     Frames are taken outermost first (distance of their offset from the
-    scan's mean) whenever their offset is at least r from every frame taken,
-    r the radius of the probe's half-maximum intensity disc; then, for every
+    scan's mean) whenever their offset is at least spacing x r from every
+    frame taken, r the radius of the probe's half-maximum intensity disc;
+    then, for every
     object pixel the full scan lights (sum of |P|^2 over all frames above
     `lit` of its maximum) where no taken frame's |P|^2 reaches `frac` of the
     best any frame gives it, the frame giving it most is added.  Returns the
@@ -504,7 +506,7 @@ def covering_frames(R, P, frac=0.3, lit=1e-2):
         w = (slice(-r0, -r0 + N0), slice(-r1, -r1 + N1))
         heat[w] += p2
         np.maximum(best_all[w], p2, out=best_all[w])
-    radius = np.sqrt(np.count_nonzero(p2 >= 0.5 * p2.max()) / np.pi)
+    radius = spacing * np.sqrt(np.count_nonzero(p2 >= 0.5 * p2.max()) / np.pi)
     pos = -R.astype(np.float64)
     order = np.argsort(-np.hypot(*(pos - pos.mean(axis=0)).T), kind="stable")
     taken = np.zeros(n, bool)
@@ -553,7 +555,7 @@ class DownsampledStart:
     (host array), R the plan's scan offsets (n, 2) with maximum 0.
     """
 
-    def __init__(self, net, n, N0, N1, P, R, cover=True):
+    def __init__(self, net, n, N0, N1, P, R, cover=True, spacing=1.0):
         torch = _torch()
         if N0 != N1 or net.H != net.W or N0 % net.H:
             raise ValueError("frames must be square, a multiple of the network's %d x %d" % (net.H, net.W))
@@ -563,13 +565,14 @@ class DownsampledStart:
         o = (self.N - self.M) // 2
         Ps = np.fft.ifft2(np.fft.ifftshift(F[o:o + self.M, o:o + self.M]))
         self.P_s = torch.from_numpy(Ps.astype(np.complex64)).to(net.dev)
+        self.phasors = probe_phasors(Ps.astype(np.complex64), net.dev)
         Rs = np.rint(np.asarray(R, np.float64)[:, :2] / self.f).astype(np.int64)
         Rs -= Rs.max(axis=0)
         self.Us = self.M + int(Rs[:, 0].max() - Rs[:, 0].min())
         self.Vs = self.M + int(Rs[:, 1].max() - Rs[:, 1].min())
         # with cover, only a subset of frames that lights every pixel the scan
         # lights (covering_frames) goes through the network
-        sel = covering_frames(Rs, Ps) if cover else np.arange(self.n)
+        sel = covering_frames(Rs, Ps, spacing=spacing) if cover else np.arange(self.n)
         self.frames = sel
         self.sel = (torch.from_numpy(sel.astype(np.int32)).to(net.dev) if len(sel) < self.n else None)
         Rsel = Rs[sel]
@@ -591,7 +594,8 @@ class DownsampledStart:
         k = self.I_s.shape[0]
         _native.check(net.lib.pty_ws_crop_center(k, self.N, self.N, self.M, self.M, _p(I_dev), _p(self.sel), 1.0,
                                                  _p(self.I_s), sp))
-        O_c = warm_start_object(net, self.I_s, self.P_s, self.plan.h, self.Uc, self.Vc, heat=self.heat)
+        O_c = warm_start_object(net, self.I_s, self.P_s, self.plan.h, self.Uc, self.Vc, heat=self.heat,
+                                phasors=self.phasors)
         if (self.Uc, self.Vc) != (self.Us, self.Vs):
             # the subset's object window inside the full scan's coarse object
             # (outside it: ones, the default start)
