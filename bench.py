@@ -665,8 +665,9 @@ def _nmse_leg(torch, dev, net, w, target, max_iters):
     O_ws = st.run(I_dev, U, V)
     torch.cuda.synchronize()
     stitch_s = time.perf_counter() - t0
-    st.close()
     warm = _era_to_nmse(torch, job, O_ws, O_true, heat, target, max_iters)
+    warm["frames_through_network"] = int(len(st.frames))
+    st.close()
     warm["inference_stitch_seconds"] = round(stitch_s, 5)
     warm["seconds_total"] = round(stitch_s + warm["seconds"], 5)
     job.close()

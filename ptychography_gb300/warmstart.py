@@ -555,8 +555,10 @@ class DownsampledStart:
     (host array), R the plan's scan offsets (n, 2) with maximum 0.
     """
 
-    def __init__(self, net, n, N0, N1, P, R, cover=True, spacing=1.0):
+    def __init__(self, net, n, N0, N1, P, R, cover=True, spacing=0.75, graph=True):
         torch = _torch()
+        self.graph = bool(graph)
+        self._graph = self._gkey = self._out = None
         if N0 != N1 or net.H != net.W or N0 % net.H:
             raise ValueError("frames must be square, a multiple of the network's %d x %d" % (net.H, net.W))
         self.net, self.n, self.N, self.M = net, int(n), int(N0), int(net.H)
@@ -586,11 +588,33 @@ class DownsampledStart:
 
     def run(self, I_dev, U, V):
         """The initial object (U, V) complex64 on the device for the centred
-        intensities I_dev (n, N, N) float32 on the device."""
+        intensities I_dev (n, N, N) float32 on the device.
+
+        With graph (the default) the first call for a given I_dev buffer and
+        object shape runs the pass once and captures it as a CUDA graph
+        (kernels, tensor maps and buffers fixed); later calls replay it.  The
+        returned tensor then belongs to the graph: the next run() overwrites
+        it, so copy it to keep it."""
         torch = _torch()
-        net, sp = self.net, self.net._sp()
         if tuple(I_dev.shape) != (self.n, self.N, self.N):
             raise ValueError("expected %d frames of %d x %d" % (self.n, self.N, self.N))
+        if not self.graph:
+            return self._run(I_dev, U, V)
+        key = (I_dev.data_ptr(), int(U), int(V))
+        if self._gkey != key:
+            self._graph = self._gkey = self._out = None
+            self._run(I_dev, U, V)                # buffers, kernel attributes, tensor-map encoder
+            torch.cuda.current_stream(self.net.dev).synchronize()
+            g = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(g, capture_error_mode="thread_local"):
+                out = self._run(I_dev, U, V)
+            self._graph, self._gkey, self._out = g, key, out
+        self._graph.replay()
+        return self._out
+
+    def _run(self, I_dev, U, V):
+        torch = _torch()
+        net, sp = self.net, self.net._sp()
         k = self.I_s.shape[0]
         _native.check(net.lib.pty_ws_crop_center(k, self.N, self.N, self.M, self.M, _p(I_dev), _p(self.sel), 1.0,
                                                  _p(self.I_s), sp))
@@ -611,4 +635,5 @@ class DownsampledStart:
         return O
 
     def close(self):
+        self._graph = self._gkey = self._out = None
         self.plan.close()

@@ -226,10 +226,11 @@ def test_downsampled_start_sees_the_object():
     _native.check(_native.load().pty_intensities(plan.h, p(Od), p(Pd), p(I), stream()))
     st = ws.DownsampledStart(net, len(R), N, N, P, R)
     O = st.run(I, U, U)
-    torch.cuda.synchronize()
+    o = O.cpu().numpy()
+    o2 = st.run(I, U, U).cpu().numpy()          # a graph replay gives the same object
     st.close()
     plan.close()
-    o = O.cpu().numpy()
+    np.testing.assert_array_equal(o, o2)
     assert o.shape == (U, U) and np.all(np.isfinite(o))
     assert np.abs(o[128:256, 128:256]).min() > 0
     assert np.abs(o).max() <= 1.0 + 1e-4
