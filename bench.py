@@ -303,6 +303,7 @@ class DeviceJob:
         self.mask = torch.from_numpy(np.fft.ifftshift(w.M).astype(np.uint8)).to(dev)
         b = torch.from_numpy(np.sqrt(np.fft.ifftshift(w.B)).astype(np.float32)).to(dev)
         self.bg = b.expand(n, N, N).contiguous()
+        self.start = (self.P.clone(), b)          # the initial probe and background (reset())
         self.bmean = torch.zeros((N, N), dtype=torch.float32, device=dev)
         self.heat = torch.zeros((U, V), dtype=torch.float64, device=dev)
         self.emod = torch.zeros(4096, dtype=torch.float64, device=dev)
@@ -323,6 +324,14 @@ class DeviceJob:
         hv = ctypes.c_int32(0)
         fn = self.lib.pty_era if kind == "era" else self.lib.pty_dm
         nat.check(fn(self.plan, ctypes.byref(buf), ctypes.byref(opt), iters, ctypes.byref(hv), self.sp()))
+
+    def reset(self, O_init):
+        """Back to the workload's start (initial probe and background, device
+        workloads only) with the object O_init."""
+        self.O.copy_(O_init)
+        P0, b = self.start
+        self.P.copy_(P0)
+        self.bg.copy_(b.expand_as(self.bg))
 
     def step(self):
         if self.w.name == "c4":
@@ -475,6 +484,16 @@ def batched_rate(dev, steps=20):
            "one_by_one_frame_iters_per_s": round(job.frames_per_step() * 2 / t_seq, 1),
            "graph_capture_s": round(capture_s, 3), "data_generation_s": round(gen_s, 1),
            "final_eMod_median": round(statistics.median(eml), 5)}
+    # algorithmic bytes per frame-iteration of ERA method 3: the fused frame
+    # pass reads the amplitudes (4 N^2) and writes the exit waves (8 N^2; the
+    # object window and probe come from L2), the object and probe gathers
+    # read the exit waves once each (8 N^2 + 8 N^2)
+    byts = 28.0 * sum(j["n"] * j["N"] * j["N"] for j in job.jobs) * job.iters * steps
+    pk, kind = peaks()
+    out["roofline"] = {"bound": "hbm", "achieved": round(byts / t / 1e9, 1), "peak": pk, "unit": "GB/s",
+                       "frac": round(byts / t / 1e9 / pk, 4), "peak_kind": kind,
+                       "algorithmic_bytes_per_frame_iter": "28 N^2 (amplitudes 4, exit waves written 8, "
+                                                           "read by the object and probe gathers 8 + 8)"}
     job.close()
     return out
 
@@ -678,21 +697,11 @@ def _nmse_leg(torch, dev, net, w, target, max_iters):
             if warm["seconds_total"] > 0 and warm["reached"] else None}
 
 
-def time_to_nmse(torch, dev, target=1e-3, max_iters=400, warm_steps=3000, warm_frames=50000):
-    """Time to object NMSE <= target (illuminated region, global complex scale
-    removed, against the synthetic ground truth): plain FP32 GPU ERA from
-    ones against ERA from the learned warm start's stitched object.
-
-    The network (128^2 frames) is trained first on the GPU: warm_steps Adam
-    steps of 32 frames from warm_frames simulated frames (random objects with
-    smoothing widths 2-4 px, random probes, Poisson noise at 1e5-1e7
-    photons).  Two scans are then reconstructed: the 256^2 / 1024-frame
-    geometry (workload_nmse_c1; the network sees each frame at half
-    resolution, the central 128^2 of its pattern, and the stitched object is
-    upsampled) and a held-out 20 x 20 scan of 128^2 frames
-    (workload_heldout).  The warm start's inference + stitching is wall clock
-    (host work included) and counts towards its time; its training time is
-    reported beside it."""
+def train_warm_start(torch, dev, warm_steps=3000, warm_frames=50000):
+    """The warm start's network (128^2 frames) trained on the GPU: warm_steps
+    Adam steps of 32 frames from warm_frames simulated frames (random objects
+    with smoothing widths 2-4 px, random probes, Poisson noise at 1e5-1e7
+    photons).  Returns the network and a description of its training."""
     from ptychography_gb300 import warmstart as ws
     net = ws.WarmStartNet(128, 128, seed=0, device=dev)
     t0 = time.perf_counter()
@@ -703,6 +712,28 @@ def time_to_nmse(torch, dev, target=1e-3, max_iters=400, warm_steps=3000, warm_f
     t2 = time.perf_counter()
     del data
     torch.cuda.empty_cache()
+    info = {"steps": warm_steps, "batch": 32, "frames": warm_frames,
+            "data_seconds": round(t1 - t0, 2), "train_seconds": round(t2 - t1, 2),
+            "loss_first_20": float(np.mean(losses[:20])), "loss_last_20": float(np.mean(losses[-20:])),
+            "input": "back-projection ifftn(sqrt(I) exp(i angle fftn P)) conj(P), (Re, Im)",
+            "target": "object phase under the probe (cos, sin), weights |P|^2",
+            "kernels": "inference: tcgen05 implicit-GEMM convolutions (layers 1-4), direct CUDA-core "
+                       "convolutions (layers 0, 5); training: im2col + mma.sync GEMMs"}
+    return net, info
+
+
+def time_to_nmse(torch, dev, net, training, target=1e-3, max_iters=400):
+    """Time to object NMSE <= target (illuminated region, global complex scale
+    removed, against the synthetic ground truth): plain FP32 GPU ERA from
+    ones against ERA from the learned warm start's stitched object.
+
+    Two scans are reconstructed with the trained network (train_warm_start):
+    the 256^2 / 1024-frame geometry (workload_nmse_c1; the network sees a
+    covering subset of the frames at half resolution, the central 128^2 of
+    each pattern, and the stitched object is upsampled) and a held-out
+    20 x 20 scan of 128^2 frames (workload_heldout).  The warm start's
+    inference + stitching is wall clock (host work included) and counts
+    towards its time; its training time is reported beside it."""
     c1 = _nmse_leg(torch, dev, net, workload_nmse_c1(gpu_intensities), target, max_iters)
     held = _nmse_leg(torch, dev, net, workload_heldout(gpu_intensities), target, max_iters)
     out = {"workload": "ERA m1 (known probe), 1024 frames 256x256, object 1006x1006 (1024x1024 truth), "
@@ -711,14 +742,7 @@ def time_to_nmse(torch, dev, target=1e-3, max_iters=400, warm_steps=3000, warm_f
            "target": target}
     out.update(c1)
     out["warm_start"]["downsampling"] = "network at 128x128: central 128^2 of each 256^2 pattern, object upsampled x2"
-    out["warm_start"]["training"] = {
-        "steps": warm_steps, "batch": 32, "frames": warm_frames,
-        "data_seconds": round(t1 - t0, 2), "train_seconds": round(t2 - t1, 2),
-        "loss_first_20": float(np.mean(losses[:20])), "loss_last_20": float(np.mean(losses[-20:])),
-        "input": "back-projection ifftn(sqrt(I) exp(i angle fftn P)) conj(P), (Re, Im)",
-        "target": "object phase under the probe (cos, sin), weights |P|^2",
-        "kernels": "inference: tcgen05 implicit-GEMM convolutions (layers 1-4), direct CUDA-core convolutions "
-                   "(layers 0, 5); training: im2col + mma.sync GEMMs"}
+    out["warm_start"]["training"] = training
     out["warm_start"]["timing"] = ("inference + stitching + upsampling wall clock after an untimed set-up of "
                                    "the coarse plan (as the main plan is set up untimed)")
     held["workload"] = "held-out 20x20 scan, 400 frames 128x128, ERA m1 (known probe), noise free"
@@ -726,10 +750,13 @@ def time_to_nmse(torch, dev, target=1e-3, max_iters=400, warm_steps=3000, warm_f
     return out
 
 
-def c4_rate(torch, dev, steps=5, warmup=2):
+def c4_rate(torch, dev, steps=5, warmup=2, net=None, warm_iters=10):
     """The 4096-frame 512 x 512 DM method-6 job (DeviceWorkload) timed beside
     the headline: device-resident iterations, CUDA events.  Its error against
-    the chunked FP64 oracle is checked by tests/test_gpu_c4_fp64.py."""
+    the chunked FP64 oracle is checked by tests/test_gpu_c4_fp64.py.  With a
+    trained warm-start network, the per-frame warm start (each 512^2 frame
+    seen at 128^2) is timed and warm_iters DM iterations from it are compared
+    with as many from ones (object NMSE against the synthetic truth)."""
     w = DeviceWorkload(dev)
     job = DeviceJob(w, dev)
     for _ in range(warmup):
@@ -739,10 +766,40 @@ def c4_rate(torch, dev, steps=5, warmup=2):
            "ms_per_iter": round(t * 1e3, 3), "steps": steps, "warmup": warmup,
            "error_vs_fp64": "tests/test_gpu_c4_fp64.py: 3 DM iterations against the chunked FP64 oracle; "
                             "O (illuminated) / P / background within 3e-5"}
+    if net is not None:
+        out["warm_start"] = _c4_warm_start(torch, dev, w, job, net, warm_iters)
     job.close()
     del job, w
     torch.cuda.empty_cache()
     return out
+
+
+def _c4_warm_start(torch, dev, w, job, net, iters):
+    from ptychography_gb300 import warmstart as ws
+    torch.cuda.synchronize()
+    heat = job.heat.cpu().numpy()
+    r0, r1 = (-w.R.max(axis=0)).tolist()
+    U, V = job.U, job.V
+    O_true = w.O_true[r0:r0 + U, r1:r1 + V]
+    R_sh = w.R - w.R.max(axis=0)
+    st = ws.DownsampledStart(net, job.n, w.N, w.N, w.P0, R_sh)
+    st.run(w.I_dev, U, V)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    O_ws = st.run(w.I_dev, U, V)
+    torch.cuda.synchronize()
+    t_ws = time.perf_counter() - t0
+    ones = torch.ones((U, V), dtype=torch.complex64, device=dev)
+    res = {"frames_through_network": int(len(st.frames)), "downsampling": "512^2 -> 128^2 (central crop), x4 upsampling",
+           "inference_stitch_seconds": round(t_ws, 5)}
+    for name, O0 in (("ones", ones), ("warm_start", O_ws)):
+        job.reset(O0)
+        e0 = nmse(O0.cpu().numpy(), O_true, heat)
+        t = event_time(torch, lambda: job.run("dm", 6, iters), 1)
+        res[name] = {"initial_nmse": e0, "nmse_after_%d" % iters: nmse(job.O.cpu().numpy(), O_true, heat),
+                     "dm_seconds": round(t, 4)}
+    st.close()
+    return res
 
 
 def e2e_public_api(w, K):
@@ -1031,12 +1088,14 @@ def main():
     }
     if m1:
         line["era_m1"] = m1
+    net = None
     if not args.no_nmse:
-        line["time_to_nmse"] = time_to_nmse(torch, dev, warm_steps=args.warm_steps)
+        net, training = train_warm_start(torch, dev, warm_steps=args.warm_steps)
+        line["time_to_nmse"] = time_to_nmse(torch, dev, net, training)
     if args.workload == "c1" and not args.no_batch:
         line["batched"] = batched_rate(dev)
     if args.workload == "c1" and not args.no_c4:
-        line["c4"] = c4_rate(torch, dev)
+        line["c4"] = c4_rate(torch, dev, net=net)
     print(json.dumps(line))
     return 0
 
