@@ -14,7 +14,10 @@ constexpr int kTileRows = kGatherTileRows;  // tile height (rows)
 constexpr int kRowStep = kTileRows / 2;     // a thread's two pixels are kRowStep rows apart
 constexpr int kGatherNT = 256; // threads per tile, 2 pixels each
 static_assert(kGatherNT * 2 == kTile * kTileRows && kTileRows % 2 == 0, "gather tile split");
-constexpr int kPrefetch = 4;   // frames whose loads are issued together (object gather)
+#ifndef PTY_GATHER_PREFETCH
+#define PTY_GATHER_PREFETCH 4
+#endif
+constexpr int kPrefetch = PTY_GATHER_PREFETCH;   // frames whose loads are issued together (object gather)
 constexpr int kPrefetchP = 4;  // the same for the probe gather
 
 // acc += conj(p) x as four FMAs
