@@ -6,8 +6,9 @@ when given, ``P``, ``O``, ``R``, ``B``; ``output`` holds ``I`` and, when given,
 ``P``, ``O``, ``R``, ``B``, ``eMod``.  ``write_cxi`` replaces an existing file
 and rejects a missing or non-directory parent path with ValueError, as the
 reference does.  ``read_cxi`` returns the same 12-tuple, the intensity stacks
-cut to their first ``maxlen`` frames (the reference's read of a file name
-refers to an unbound name before opening it; a file name works here).
+cut to their first ``maxlen`` frames, and closes the file, also an open h5py
+file it was given, as the reference does (the reference's read of a file
+name refers to an unbound name before opening it; a file name works here).
 
 HDF5 access needs h5py, which is imported when a file is written or read; on
 a machine without it both functions raise ImportError.  The reconstruction
@@ -59,9 +60,8 @@ def write_cxi(I_in, I_out, P_in, P_out, O_in, O_out, R_in, R_out, B_in, B_out, M
 def read_cxi(fnam="output.cxi", maxlen=100):
     """Read a file written by ``write_cxi`` (display.py:61-117): returns
     (I_in, I_out, P_in, P_out, O_in, O_out, R_in, R_out, B_in, B_out, M, eMod)."""
-    h5py = _h5py()
     own = isinstance(fnam, (str, os.PathLike))
-    f = h5py.File(fnam, "r") if own else fnam
+    f = _h5py().File(fnam, "r") if own else fnam
     try:
         gin, gout = f["input"], f["output"]
         get = lambda g, k: g[k][()] if k in g else None  # noqa: E731
@@ -72,5 +72,4 @@ def read_cxi(fnam="output.cxi", maxlen=100):
         return (I_in, I_out, P_in, P_out, O_in, O_out, R_in, R_out, B_in, B_out, gin["M"][()],
                 get(gout, "eMod"))
     finally:
-        if own:
-            f.close()
+        f.close()             # display.py:116 closes the file, also one it was given
