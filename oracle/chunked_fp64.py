@@ -19,9 +19,10 @@ float64 rounding of the transforms (tests/test_chunked_oracle_cpu.py pins
 that on small problems).
 
 Supported: methods 1, 3, 4 and 6 (object, or object and probe, without or
-with a known background), OP_iters = 1, no probe centring and no Pmod_probe
--- the options of the large-reconstruction workload.  Anything else raises
-NotImplementedError.
+with a known background), OP_iters = 1, with or without probe centring
+(era.py:172-186, dm.py:65-82 / 115-127) and the far-field probe constraint
+Pmod_P (era.py:597-610) for the first Pmod_probe iterations.  Anything else
+raises NotImplementedError.
 """
 import numpy as np
 
@@ -64,6 +65,8 @@ class Problem:
         self.mask = torch.fft.ifftshift(mc)                           # era.py:499
         # era.py:495: I_norm = sum(mask * I), accumulated here in float64
         self.I_norm = float(sum(float((self.I[s:e].to(torch.float64) * mc).sum()) for s, e in self.chunks()))
+        F = torch.fft.fftn(self.P0)                                   # era.py:546-547
+        self.Pamp = torch.sqrt((F.conj() * F).real)
         self.bg2d = None
         if background is not None:                                    # era.py:541-544
             b = torch.as_tensor(np.ascontiguousarray(background), device=device).to(torch.float64)
@@ -156,6 +159,41 @@ def _model_error(pb, ex, b, amp):
     return float((pb.mask * (Mag - amp) ** 2).sum())
 
 
+def _pmod_P(pb, P, alpha):
+    """Far-field probe modulus |fftn P| -> Pamp, masked pixels kept (era.py:597-610)."""
+    torch = _torch()
+    F = torch.fft.fftn(P)
+    Mag = torch.sqrt((F.conj() * F).real) + alpha
+    fac = torch.where(pb.mask == 0, torch.ones_like(Mag), pb.Pamp / Mag)
+    return torch.fft.ifftn(F * fac)
+
+
+def _probe_shift(P):
+    """rint(centre of mass of |P|^2) - shape // 2 (era.py:172-176)."""
+    torch = _torch()
+    a = (P.conj() * P).real
+    tot = a.sum()
+    i = torch.arange(a.shape[0], dtype=torch.float64, device=a.device)
+    j = torch.arange(a.shape[1], dtype=torch.float64, device=a.device)
+    c0 = float((a.sum(dim=1) * i).sum() / tot)
+    c1 = float((a.sum(dim=0) * j).sum() / tot)
+    return int(np.rint(c0)) - a.shape[0] // 2, int(np.rint(c1)) - a.shape[1] // 2
+
+
+def _roll2(x, s):
+    """Periodic shift of the last two axes by s (multiroll, era.py:631-740)."""
+    torch = _torch()
+    return torch.roll(x, shifts=(int(s[0]), int(s[1])), dims=(-2, -1))
+
+
+def _pmod_count(Pmod_probe, iters):
+    """The iterations i with i < Pmod_probe (era.py:193)."""
+    if Pmod_probe is None or Pmod_probe is False:
+        return 0
+    x = float(Pmod_probe)
+    return iters if x == float("inf") else max(0, min(iters, int(np.ceil(x))))
+
+
 def _check(method):
     if method not in (1, 3, 4, 6):
         raise NotImplementedError("the chunked oracle restates methods 1, 3, 4 and 6")
@@ -197,7 +235,7 @@ def _op_projection(pb, exits, O, P, update, P_heat, alpha):
     return O, P, P_heat, P_heat
 
 
-def ERA(pb, iters, method, alpha=1e-10):
+def ERA(pb, iters, method, alpha=1e-10, probe_centering=False, Pmod_probe=False):
     """Error reduction (era.py:13-332) for methods 1, 3, 4, 6.  Returns
     (O, P, info) with info keys eMod, eCon, heatmap and, for methods 4 and 6,
     background (fftshift(b)^2 of the frames' common background)."""
@@ -213,6 +251,7 @@ def ERA(pb, iters, method, alpha=1e-10):
         exits[s:e] = pb.make_exits(O, P, s, e)                  # era.py:536
     bg = pb.bg2d.expand(pb.n, pb.N0, pb.N1).clone() if use_bg else None
     P_heat = heat_out = None
+    npm = _pmod_count(Pmod_probe, iters)
     eMods, eCons = [], []
     for i in range(iters):
         bak = _snap(update, O, P)
@@ -224,6 +263,12 @@ def ERA(pb, iters, method, alpha=1e-10):
                 exits[s:e], em = _pmod_1(pb, exits[s:e], pb.amp(s, e), alpha)
             emod += em
         O, P, heat_out, P_heat = _op_projection(pb, exits, O, P, update, P_heat, alpha)
+        if update == "OP" and probe_centering:                  # era.py:172-186
+            cm = _probe_shift(P)
+            P, O = _roll2(P, (-cm[0], -cm[1])), _roll2(O, (-cm[0], -cm[1]))
+            heat_out = None
+        if i < npm:                                             # era.py:193-194
+            P = _pmod_P(pb, P, alpha)
         if use_bg:                                              # era.py:265-270
             bg[:] = _mean_frames(pb, bg)
         for s, e in pb.chunks():                                # era.py:196 / 272
@@ -236,7 +281,7 @@ def ERA(pb, iters, method, alpha=1e-10):
     return O, P, info
 
 
-def DM(pb, iters, method, alpha=1e-10):
+def DM(pb, iters, method, alpha=1e-10, probe_centering=False, Pmod_probe=False):
     """Difference map (dm.py:13-333) for methods 1, 3, 4, 6.  Returns
     (O, P, info) like ERA; info's background is the frames' mean of the last
     metric projection (dm.py:308-318)."""
@@ -253,6 +298,7 @@ def DM(pb, iters, method, alpha=1e-10):
     bg = pb.bg2d.expand(pb.n, pb.N0, pb.N1).clone() if use_bg else None
     P_heat = heat_out = None
     b0 = None
+    npm = _pmod_count(Pmod_probe, iters)
     eMods, eCons = [], []
     bak = _snap(update, O, P)                                   # dm.py:35-38
     for i in range(iters):
@@ -261,6 +307,14 @@ def DM(pb, iters, method, alpha=1e-10):
                 exits[s:e], bg[s:e], _ = _pmod_7(pb, exits[s:e], bg[s:e], pb.amp(s, e), alpha)
         # main consistency projection (dm.py:56-85 / 174-202)
         O, P, heat_out, P_heat = _op_projection(pb, exits, O, P, update, P_heat, alpha)
+        if update == "OP" and probe_centering:                  # dm.py:65-82 / 183-200
+            cm = _probe_shift(P)
+            P, O = _roll2(P, (-cm[0], -cm[1])), _roll2(O, (-cm[0], -cm[1]))
+            heat_out = None
+            for s, e in pb.chunks():
+                exits[s:e] = _roll2(exits[s:e], (-cm[0], -cm[1]))
+        if i < npm:                                             # dm.py:88-89
+            P = _pmod_P(pb, P, alpha)
         # difference-map update (dm.py:91-97 / 203-224), frame chunk by chunk:
         # exits -= ex0; ex0 -= exits (= 2 ex0 - psi); the background likewise
         # against its frame mean; then the modulus projection of the
@@ -282,6 +336,11 @@ def DM(pb, iters, method, alpha=1e-10):
                 exits[s:e] = ps + ex0
         # metric projection (dm.py:104-137 / 231-271)
         Os, Ps, _, P_heat = _op_projection(pb, exits, O.clone(), P.clone(), update, P_heat, alpha)
+        if update == "OP" and probe_centering:                  # dm.py:115-127 / 242-254
+            cm = _probe_shift(Ps)
+            Ps, Os = _roll2(Ps, (-cm[0], -cm[1])), _roll2(Os, (-cm[0], -cm[1]))
+        if i < npm:                                             # dm.py:136-137
+            Ps = _pmod_P(pb, Ps, alpha)
         if use_bg:
             b0 = _mean_frames(pb, bg)
         emod = 0.0
