@@ -541,28 +541,38 @@ int launch_probe_shift(const float2* P, int N0, int N1, int* shift, cudaStream_t
   return check_launch("probe_shift_kernel");
 }
 
-// multiroll(x, -cm) (era.py:631-740): dst[i][j] = src[(i + s0) mod H][(j + s1) mod W]
+// multiroll(x, -cm) (era.py:631-740) per image: dst[r][c] = src[(r + s0) mod H][(c + s1) mod W].
+// Grid: (blocks over one image's rows, images); 32-bit index math inside an
+// image, threads along a row (coalesced writes, reads coalesced up to the one
+// wrap point of the row).
 __global__ void roll_kernel(const float2* __restrict__ src, float2* __restrict__ dst, int nimg,
                             int H, int W, const int* __restrict__ shift) {
-  const long long tot = (long long)nimg * H * W;
   const int s0 = shift[0], s1 = shift[1];
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < tot;
-       i += (long long)gridDim.x * blockDim.x) {
-    const long long img = i / ((long long)H * W);
-    const int r = (int)((i / W) % H), c = (int)(i % W);
-    int rr = (r + s0) % H, cc = (c + s1) % W;
-    if (rr < 0) rr += H;
-    if (cc < 0) cc += W;
-    dst[i] = src[img * H * W + (long long)rr * W + cc];
+  const size_t npix = (size_t)H * W;
+  for (int img = blockIdx.y; img < nimg; img += gridDim.y) {
+    const float2* s = src + (size_t)img * npix;
+    float2* d = dst + (size_t)img * npix;
+    for (int r = blockIdx.x; r < H; r += gridDim.x) {
+      int rr = (r + s0) % H;
+      if (rr < 0) rr += H;
+      const float2* srow = s + (size_t)rr * W;
+      float2* drow = d + (size_t)r * W;
+      for (int c = threadIdx.x; c < W; c += blockDim.x) {
+        int cc = (c + s1) % W;
+        if (cc < 0) cc += W;
+        drow[c] = srow[cc];
+      }
+    }
   }
 }
 
 int launch_roll(const float2* src, float2* dst, int nimg, int H, int W, const int* shift,
                 cudaStream_t st) {
-  long long tot = (long long)nimg * H * W;
-  int blocks = (int)((tot + 255) / 256);
-  if (blocks > 152 * 16) blocks = 152 * 16;
-  roll_kernel<<<blocks, 256, 0, st>>>(src, dst, nimg, H, W, shift);
+  // about 16 CTAs per SM in all: rows split further when there are few images
+  const int gy = nimg < 65535 ? nimg : 65535;
+  int gx = (152 * 16 + gy - 1) / gy;
+  gx = gx < 1 ? 1 : (gx > H ? H : gx);
+  roll_kernel<<<dim3(gx, gy), 256, 0, st>>>(src, dst, nimg, H, W, shift);
   return check_launch("roll_kernel");
 }
 
