@@ -1,7 +1,7 @@
 """Probe centring and the far-field probe constraint at the large-frame scale:
 1024 frames of 512 x 512 (the first 1024 positions of the 4096-frame scan of
 bench.DeviceWorkload, on the staged 512^2 tile), ERA and DM method 3 (object
-and probe) with probe_centering=True and Pmod_probe=2, three iterations,
+and probe) with probe centring and / or Pmod_probe=2, three iterations,
 through the public API, against the chunked FP64 oracle (oracle/chunked_fp64.py,
 pinned to the NumPy oracle by tests/test_chunked_oracle_cpu.py).  The initial
 probe is off centre, so the centring rolls the probe, the object and (DM) the
@@ -33,8 +33,16 @@ def data():
     return w, P0, dev
 
 
-@pytest.mark.parametrize("algo,cent,pmod", [("ERA", True, 2), ("DM", False, 0), ("DM", True, 0),
-                                           ("DM", False, 2), ("DM", True, 2)])
+# DM with Pmod_P is left out here: from this probe (a smooth aperture with a
+# small defocus, whose far field is at rounding level over most of the
+# detector) the probe's far-field constraint makes DM ill-conditioned in FP32:
+# the NumPy oracle's own FP32 and FP64 runs of a 128^2 version of this job
+# (DM method 3, Pmod_probe=2, ones or ones + noise to start) differ by 4-5 % on
+# the probe and 3-9x on eMod, so no FP32 engine can be held to FP64 there.
+# DM + Pmod_P parity rests on the reference-recorded DM_m3_opiters_double run
+# (tests/test_gpu_runs.py), whose bound includes the reference's own FP32/FP64 gap.
+@pytest.mark.parametrize("algo,cent,pmod", [("ERA", True, 2), ("ERA", False, 2), ("DM", False, 0),
+                                           ("DM", True, 0)])
 def test_centring_and_probe_modulus_512(algo, cent, pmod, data):
     w, P0, dev = data
     I = w.I_dev.cpu().numpy()
