@@ -131,8 +131,16 @@ class Preamble:
                     # one frame's pattern; copied to every frame on the device
                     self.background_pattern = np.ascontiguousarray(b.astype(np.float32))
         self.user_background = background
-        Pamp = np.fft.fftn(self.P, axes=(-2, -1))                 # era.py:546-547
-        self.Pamp = np.sqrt((Pamp.conj() * Pamp).real).astype(np.float32)
+        self._Pamp = None
+
+    @property
+    def Pamp(self):
+        """|fftn(P)| of the initial probe (era.py:546-547), formed on first
+        use: only the far-field probe constraint (Pmod_probe) reads it."""
+        if self._Pamp is None:
+            F = np.fft.fftn(self.P, axes=(-2, -1))
+            self._Pamp = np.sqrt((F.conj() * F).real).astype(np.float32)
+        return self._Pamp
 
 
 def _ptr(t):
