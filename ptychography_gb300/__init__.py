@@ -9,6 +9,7 @@ The reconstruction loops run in libptycho_gb300.so (hand-written sm_103a CUDA,
 C ABI in include/ptycho_gb300.h); Python prepares inputs and returns outputs.
 """
 from . import back_projection, cxi, dm, era, forward_models, warmstart  # noqa: F401
+from ._engine import release_plan_cache
 from .back_projection import Back_projection
 from .dm import DM, DM_batch
 from .era import ERA, ERA_batch
@@ -17,5 +18,5 @@ from .forward_models import forward_sim
 from .warmstart import WarmStartNet
 
 __all__ = ["ERA", "DM", "ERA_batch", "DM_batch", "write_cxi", "read_cxi", "forward_sim", "Back_projection",
-           "WarmStartNet", "era", "dm", "forward_models", "back_projection", "warmstart"]
+           "WarmStartNet", "release_plan_cache", "era", "dm", "forward_models", "back_projection", "warmstart"]
 __version__ = "0.1.0"

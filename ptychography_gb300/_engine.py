@@ -12,8 +12,10 @@ the pass that forms the amplitudes.  Everything else (exit waves, FFTs,
 projections, metrics) runs on the GPU in libptycho_gb300.  Bulk arithmetic is
 complex64; ``dtype='double'`` only sets the dtype of the returned arrays.
 """
+import atexit
 import ctypes
 import math
+import threading
 
 import numpy as np
 
@@ -167,13 +169,64 @@ def device_random_background(lib, out, rdt, sp):
     np.random.set_state((st[0], key_out, int(pos_out.value), st[3], st[4]))
 
 
+# The plan of the last public call, kept for the next call with the same
+# geometry and scan (ERA then DM on the same data, or repeated calls): its
+# set-up (tile lists, device scratch) and, when the next call's buffers land at
+# the same addresses, its captured loop are reused.  Only plans of at most
+# 2^27 frame pixels are kept (about 100-300 MB of plan scratch); the tensors a
+# call allocates are torch's and go back to its allocator as usual.
+_PLAN_CACHE = {"key": None, "plan": None}
+_PLAN_LOCK = threading.Lock()
+_PLAN_CACHE_MAX_PIXELS = 1 << 27
+
+
+def release_plan_cache():
+    """Destroy the plan kept from the last public call (frees its device memory)."""
+    with _PLAN_LOCK:
+        plan, _PLAN_CACHE["plan"], _PLAN_CACHE["key"] = _PLAN_CACHE["plan"], None, None
+    if plan:
+        _native.load().pty_plan_destroy(plan)
+
+
+atexit.register(lambda: _PLAN_CACHE.update(plan=None, key=None))   # the context may be gone at exit
+
+
+def _plan_key(dev, geom, R64):
+    return (dev.index, geom.n_frames, geom.N0, geom.N1, geom.U, geom.V, R64.tobytes())
+
+
+def _take_plan(lib, dev, geom, R64):
+    key = _plan_key(dev, geom, R64)
+    with _PLAN_LOCK:
+        if _PLAN_CACHE["key"] == key and _PLAN_CACHE["plan"]:
+            plan = _PLAN_CACHE["plan"]
+            _PLAN_CACHE["plan"], _PLAN_CACHE["key"] = None, None
+            return plan, key
+    plan = ctypes.c_void_p()
+    _native.check(lib.pty_plan_create(ctypes.byref(geom), R64.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)),
+                                      ctypes.byref(plan)))
+    return plan, key
+
+
+def _return_plan(lib, key, plan):
+    """Keep a plan for the next call (when small enough), destroying the one kept before."""
+    if key[1] * key[2] * key[3] > _PLAN_CACHE_MAX_PIXELS:
+        lib.pty_plan_destroy(plan)
+        return
+    with _PLAN_LOCK:
+        old, _PLAN_CACHE["plan"], _PLAN_CACHE["key"] = _PLAN_CACHE["plan"], plan, key
+    if old:
+        lib.pty_plan_destroy(old)
+
+
 class _Job:
     """One reconstruction's plan and device buffers (era.py:435-548 set-up on the GPU)."""
 
     def __init__(self, lib, dev, sp, kind, I, R, P, O, iters, OP_iters, mask, background, method,
-                 Pmod_probe, probe_centering, alpha, dtype, full_output, use_graph):
+                 Pmod_probe, probe_centering, alpha, dtype, full_output, use_graph, reuse_plan=False):
         torch = _torch()
         self.lib, self.kind, self.full_output = lib, kind, full_output
+        self.reuse_plan, self.plan_key, self.ok = reuse_plan, None, False
         pre = self.pre = Preamble(I, R, P, O, OP_iters, mask, background, method, dtype,
                                   host_background_draw=False, host_norm=False)
         self.iters = iters = int(iters)
@@ -181,10 +234,13 @@ class _Job:
         U, V = pre.O.shape
         geom = _native.Geometry(n, N0, N1, U, V)
         R64 = np.ascontiguousarray(pre.R[:, :2], dtype=np.int64)
-        self.plan = ctypes.c_void_p()
-        _native.check(lib.pty_plan_create(ctypes.byref(geom),
-                                          R64.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)),
-                                          ctypes.byref(self.plan)))
+        if reuse_plan:
+            self.plan, self.plan_key = _take_plan(lib, dev, geom, R64)
+        else:
+            self.plan = ctypes.c_void_p()
+            _native.check(lib.pty_plan_create(ctypes.byref(geom),
+                                              R64.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)),
+                                              ctypes.byref(self.plan)))
         try:
             Iin = pre.I
             if Iin.dtype not in (np.float32, np.float64):
@@ -282,7 +338,10 @@ class _Job:
 
     def close(self):
         if self.plan:
-            self.lib.pty_plan_destroy(self.plan)
+            if self.reuse_plan and self.ok:
+                _return_plan(self.lib, self.plan_key, self.plan)
+            else:
+                self.lib.pty_plan_destroy(self.plan)
             self.plan = ctypes.c_void_p()
 
 
@@ -295,7 +354,7 @@ def run(kind, I, R, P, O, iters, OP_iters, mask, background, method, Pmod_probe,
     stream = torch.cuda.current_stream(dev)
     sp = ctypes.c_void_p(stream.cuda_stream)
     job = _Job(lib, dev, sp, kind, I, R, P, O, iters, OP_iters, mask, background, method,
-               Pmod_probe, probe_centering, alpha, dtype, full_output, use_graph)
+               Pmod_probe, probe_centering, alpha, dtype, full_output, use_graph, reuse_plan=True)
     try:
         hv = ctypes.c_int32(0)
         fn = lib.pty_era if kind == "era" else lib.pty_dm
@@ -304,7 +363,9 @@ def run(kind, I, R, P, O, iters, OP_iters, mask, background, method, Pmod_probe,
         job.stage_outputs()            # host work overlapping the GPU loop
         stream.synchronize()
         job.heat_valid = hv.value
-        return job.outputs()
+        out = job.outputs()
+        job.ok = True                  # a plan is kept for the next call only after a clean run
+        return out
     finally:
         job.close()
 

@@ -81,3 +81,30 @@ def test_window_outside_object_is_rejected_before_launch():
     with pytest.raises(ValueError):
         pty.ERA(I, R.copy(), P, O_small, 1, mask=M, method=1)
     assert int(_native.load().pty_launch_count()) == before
+
+
+def test_plan_kept_between_calls_gives_the_same_results():
+    """The public calls keep the last plan for the next call with the same
+    geometry and scan: ERA then DM on the same data reuse it, a call on another
+    scan replaces it, and results equal those of calls on fresh plans."""
+    from ptychography_gb300 import _engine
+    I, R, M, P = _small()
+    lib = _native.load()
+    pty.release_plan_cache()
+    O1, i1 = pty.ERA(I, R.copy(), P, None, 2, mask=M, method=1)
+    kept = _engine._PLAN_CACHE["plan"]
+    assert kept
+    O2, i2 = pty.ERA(I, R.copy(), P, None, 2, mask=M, method=1)      # reuses the kept plan
+    assert _engine._PLAN_CACHE["plan"].value == kept.value
+    np.testing.assert_array_equal(O1, O2)
+    np.testing.assert_array_equal(i1["eMod"], i2["eMod"])
+    pty.release_plan_cache()
+    assert _engine._PLAN_CACHE["plan"] is None
+    O3, i3 = pty.ERA(I, R.copy(), P, None, 2, mask=M, method=1)      # a fresh plan
+    np.testing.assert_array_equal(O1, O3)
+    R2 = R.copy()
+    R2[0] += 1
+    pty.ERA(I, R2, P, None, 1, mask=M, method=1)                    # another scan: replaced
+    assert _engine._PLAN_CACHE["plan"].value != kept.value
+    pty.release_plan_cache()
+    assert lib is _native.load()
