@@ -186,6 +186,14 @@ int pty_psup_P_noalloc(const pty_geometry* geom, const int64_t* R_host, const vo
 int pty_legacy_random_background(const uint32_t* key, int32_t pos, int64_t count,
                                  int32_t rdt_double, float* out, uint32_t* scratch,
                                  uint32_t* key_out, int32_t* pos_out, void* stream);
+/* The same without synchronising: the draw and the copy of the state into
+ * key_out are stream-ordered, so key_out must be page-locked host memory and
+ * is valid once the stream has reached that point (*pos_out is set at once).
+ * The public ERA / DM calls use it to overlap the draw with their uploads.
+ * No reference counterpart beyond the draw itself. */
+int pty_legacy_random_background_async(const uint32_t* key, int32_t pos, int64_t count,
+                                       int32_t rdt_double, float* out, uint32_t* scratch,
+                                       uint32_t* key_out, int32_t* pos_out, void* stream);
 /* Scratch words pty_legacy_random_background needs (-1 for invalid input). */
 int64_t pty_legacy_random_scratch_words(int32_t pos, int64_t count);
 /* Host-side jump-ahead of the same generator (no reference counterpart; it

@@ -169,6 +169,47 @@ def device_random_background(lib, out, rdt, sp):
     np.random.set_state((st[0], key_out, int(pos_out.value), st[3], st[4]))
 
 
+_SIDE = {}
+
+
+def _side_stream(dev):
+    torch = _torch()
+    s = _SIDE.get(dev.index)
+    if s is None:
+        s = _SIDE[dev.index] = torch.cuda.Stream(device=dev)
+    return s
+
+
+def device_random_background_async(lib, out, rdt, main):
+    """device_random_background on a side stream that starts after `main`'s
+    work so far, overlapping the caller's next uploads.  Returns (event,
+    finish): `main` must wait for the event before reading `out`, and
+    finish() -- called once the event has passed, e.g. after a stream
+    synchronisation -- hands the generator's new state to NumPy."""
+    torch = _torch()
+    st = np.random.get_state()
+    if st[0] != "MT19937":
+        raise RuntimeError("NumPy's global generator is not MT19937")
+    key = np.ascontiguousarray(st[1], dtype=np.uint32)
+    key_out = torch.empty(624, dtype=torch.int32, pin_memory=True)     # written by the stream
+    pos_out = ctypes.c_int32(0)
+    u32p = ctypes.POINTER(ctypes.c_uint32)
+    side = _side_stream(out.device)
+    side.wait_stream(main)
+    _native.check(lib.pty_legacy_random_background_async(
+        key.ctypes.data_as(u32p), int(st[2]), int(out.numel()), int(rdt == np.float64), _ptr(out), None,
+        ctypes.cast(key_out.data_ptr(), u32p), ctypes.byref(pos_out), ctypes.c_void_p(side.cuda_stream)))
+    out.record_stream(side)
+    ev = torch.cuda.Event()
+    ev.record(side)
+    pos = int(pos_out.value)
+
+    def finish():
+        ev.synchronize()
+        np.random.set_state((st[0], key_out.numpy().view(np.uint32).copy(), pos, st[3], st[4]))
+    return ev, finish
+
+
 # The plan of the last public call, kept for the next call with the same
 # geometry and scan (ERA then DM on the same data, or repeated calls): its
 # set-up (tile lists, device scratch) and, when the next call's buffers land at
@@ -223,10 +264,12 @@ class _Job:
     """One reconstruction's plan and device buffers (era.py:435-548 set-up on the GPU)."""
 
     def __init__(self, lib, dev, sp, kind, I, R, P, O, iters, OP_iters, mask, background, method,
-                 Pmod_probe, probe_centering, alpha, dtype, full_output, use_graph, reuse_plan=False):
+                 Pmod_probe, probe_centering, alpha, dtype, full_output, use_graph, reuse_plan=False,
+                 overlap_draw=False):
         torch = _torch()
         self.lib, self.kind, self.full_output = lib, kind, full_output
         self.reuse_plan, self.plan_key, self.ok = reuse_plan, None, False
+        self.draw_event, self.finish_draw = None, None
         pre = self.pre = Preamble(I, R, P, O, OP_iters, mask, background, method, dtype,
                                   host_background_draw=False, host_norm=False)
         self.iters = iters = int(iters)
@@ -242,6 +285,12 @@ class _Job:
                                               R64.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)),
                                               ctypes.byref(self.plan)))
         try:
+            bg_d = None
+            if pre.random_background and overlap_draw:              # era.py:539-540
+                # drawn on a side stream while the intensities upload
+                bg_d = torch.empty((n, N0, N1), dtype=torch.float32, device=dev)
+                self.draw_event, self.finish_draw = device_random_background_async(
+                    lib, bg_d, pre.rdt, torch.cuda.current_stream(dev))
             Iin = pre.I
             if Iin.dtype not in (np.float32, np.float64):
                 Iin = Iin.astype(np.float64)
@@ -261,10 +310,11 @@ class _Job:
             self.O_d = torch.from_numpy(np.ascontiguousarray(pre.O.astype(np.complex64))).to(dev)
             self.P_d = torch.from_numpy(np.ascontiguousarray(pre.P.astype(np.complex64))).to(dev)
             psi = torch.empty((n, N0, N1), dtype=torch.complex64, device=dev)
-            bg_d = torch.from_numpy(pre.background).to(dev) if pre.background is not None else None
+            if pre.background is not None:
+                bg_d = torch.from_numpy(pre.background).to(dev)
             if pre.background_pattern is not None:
                 bg_d = torch.from_numpy(pre.background_pattern).to(dev).expand(n, N0, N1).contiguous()
-            if pre.random_background:                               # era.py:539-540
+            if pre.random_background and not overlap_draw:          # era.py:539-540
                 bg_d = torch.empty((n, N0, N1), dtype=torch.float32, device=dev)
                 device_random_background(lib, bg_d, pre.rdt, sp)
             npm = pmod_probe_count(Pmod_probe, iters)
@@ -286,6 +336,7 @@ class _Job:
                                        int(bool(probe_centering)), int(bool(use_graph)),
                                        float(alpha), pre.I_norm)
         except BaseException:
+            self.settle_draw()
             self.close()
             raise
         self.heat_valid = 0
@@ -336,6 +387,13 @@ class _Job:
             return self.inten_host.numpy()
         return self.inten.cpu().numpy().astype(rt, copy=False)
 
+    def settle_draw(self):
+        """Wait for an overlapped background draw and hand NumPy the
+        generator state it leaves (the reference has drawn it by now)."""
+        if self.finish_draw is not None:
+            fin, self.finish_draw = self.finish_draw, None
+            fin()
+
     def close(self):
         if self.plan:
             if self.reuse_plan and self.ok:
@@ -354,8 +412,11 @@ def run(kind, I, R, P, O, iters, OP_iters, mask, background, method, Pmod_probe,
     stream = torch.cuda.current_stream(dev)
     sp = ctypes.c_void_p(stream.cuda_stream)
     job = _Job(lib, dev, sp, kind, I, R, P, O, iters, OP_iters, mask, background, method,
-               Pmod_probe, probe_centering, alpha, dtype, full_output, use_graph, reuse_plan=True)
+               Pmod_probe, probe_centering, alpha, dtype, full_output, use_graph, reuse_plan=True,
+               overlap_draw=True)
     try:
+        if job.draw_event is not None:
+            stream.wait_event(job.draw_event)
         hv = ctypes.c_int32(0)
         fn = lib.pty_era if kind == "era" else lib.pty_dm
         _native.check(fn(job.plan, ctypes.byref(job.buf), ctypes.byref(job.opt), job.iters,
@@ -367,6 +428,7 @@ def run(kind, I, R, P, O, iters, OP_iters, mask, background, method, Pmod_probe,
         job.ok = True                  # a plan is kept for the next call only after a clean run
         return out
     finally:
+        job.settle_draw()
         job.close()
 
 

@@ -62,6 +62,9 @@ SIGNATURES = {
     "pty_legacy_random_background": [ctypes.POINTER(ctypes.c_uint32), c_int32, ctypes.c_int64,
                                      c_int32, c_void_p, c_void_p, ctypes.POINTER(ctypes.c_uint32),
                                      ctypes.POINTER(c_int32), c_void_p],
+    "pty_legacy_random_background_async": [ctypes.POINTER(ctypes.c_uint32), c_int32, ctypes.c_int64,
+                                     c_int32, c_void_p, c_void_p, ctypes.POINTER(ctypes.c_uint32),
+                                     ctypes.POINTER(c_int32), c_void_p],
     "pty_legacy_random_scratch_words": [c_int32, ctypes.c_int64],
     "pty_legacy_random_jump": [ctypes.POINTER(ctypes.c_uint32), ctypes.c_int64,
                                ctypes.POINTER(ctypes.c_uint32)],

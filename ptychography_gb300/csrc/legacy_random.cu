@@ -409,9 +409,8 @@ extern "C" int64_t pty_legacy_random_scratch_words(int32_t pos, int64_t count) {
   return d.total + kMtN + d.segs * kMtN;
 }
 
-extern "C" int pty_legacy_random_background(const uint32_t* key, int32_t pos, int64_t count,
-                                            int32_t rdt_double, float* out, uint32_t* scratch,
-                                            uint32_t* key_out, int32_t* pos_out, void* stream) {
+static int random_background(const uint32_t* key, int32_t pos, int64_t count, int32_t rdt_double, float* out,
+                             uint32_t* scratch, uint32_t* key_out, int32_t* pos_out, void* stream, bool sync) {
   if (!key || !out || !key_out || !pos_out) return set_error(PTY_ERR_ARG, "null argument");
   if (pos < 0 || pos > kMtN) return set_error(PTY_ERR_ARG, "generator position outside 0..624");
   if (count < 1) return set_error(PTY_ERR_ARG, "count must be positive");
@@ -461,7 +460,7 @@ extern "C" int pty_legacy_random_background(const uint32_t* key, int32_t pos, in
     if (e != cudaSuccess) rc = set_cuda_error(e, "generator state copy");
   }
   if (!scratch) cudaFreeAsync(d_x, st);
-  if (rc == PTY_OK) {
+  if (rc == PTY_OK && sync) {
     e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) rc = set_cuda_error(e, "generator state copy");
   }
@@ -470,6 +469,18 @@ extern "C" int pty_legacy_random_background(const uint32_t* key, int32_t pos, in
     *pos_out = (int32_t)((end - 1) % kMtN + 1);
   }
   return rc;
+}
+
+extern "C" int pty_legacy_random_background(const uint32_t* key, int32_t pos, int64_t count,
+                                            int32_t rdt_double, float* out, uint32_t* scratch,
+                                            uint32_t* key_out, int32_t* pos_out, void* stream) {
+  return random_background(key, pos, count, rdt_double, out, scratch, key_out, pos_out, stream, true);
+}
+
+extern "C" int pty_legacy_random_background_async(const uint32_t* key, int32_t pos, int64_t count,
+                                                  int32_t rdt_double, float* out, uint32_t* scratch,
+                                                  uint32_t* key_out, int32_t* pos_out, void* stream) {
+  return random_background(key, pos, count, rdt_double, out, scratch, key_out, pos_out, stream, false);
 }
 
 // The window of 624 words at offset `words` of the raw sequence whose first
