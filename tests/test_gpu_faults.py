@@ -25,17 +25,26 @@ def _small():
     return d["I"], d["R"], d["M"], d["P"]
 
 
+def _start(I, R):
+    # ones plus seeded noise: with this band-limited probe, ones alone leaves
+    # |FFT(P O)| at rounding level outside the pupil (FP32 vs FP64 ill-conditioned)
+    rng = np.random.default_rng(11)
+    shp = (I.shape[1] + R[:, 0].max() - R[:, 0].min(), I.shape[2] + R[:, 1].max() - R[:, 1].min())
+    return np.ones(shp) + 0.1 * (rng.standard_normal(shp) + 1j * rng.standard_normal(shp))
+
+
 def test_nan_intensity_propagates_like_the_reference():
     I, R, M, P = _small()
+    O0 = _start(I, R)
     Ib = I.astype(np.float64).copy()
     Ib[3, 5, 7] = np.nan
-    O, info = pty.ERA(Ib, R.copy(), P, None, 2, mask=M, method=1)
-    O_o, info_o = orc.ERA(Ib, R.copy(), P, None, 2, mask=M, method=1, dtype="double")
+    O, info = pty.ERA(Ib, R.copy(), P, O0, 2, mask=M, method=1)
+    O_o, info_o = orc.ERA(Ib, R.copy(), P, O0, 2, mask=M, method=1, dtype="double")
     assert np.isnan(info["eMod"]).all() == np.isnan(info_o["eMod"]).all()
     assert np.isnan(info["eMod"][0])
-    # a clean call afterwards matches the oracle as usual
-    O2, info2 = pty.ERA(I, R.copy(), P, None, 2, mask=M, method=1)
-    O2o, info2o = orc.ERA(I, R.copy(), P, None, 2, mask=M, method=1, dtype="double")
+    # a clean call afterwards (on the plan the NaN call left) matches the oracle as usual
+    O2, info2 = pty.ERA(I, R.copy(), P, O0, 2, mask=M, method=1)
+    O2o, info2o = orc.ERA(I, R.copy(), P, O0, 2, mask=M, method=1, dtype="double")
     assert np.isfinite(info2["eMod"]).all()
     np.testing.assert_allclose(info2["eMod"], info2o["eMod"], rtol=1e-4)
 
