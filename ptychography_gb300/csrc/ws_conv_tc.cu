@@ -19,8 +19,7 @@
 // reads (64-byte swizzle when C_in = 32).  No im2col buffer is written.
 //
 // Roles (one CTA per SM, persistent over tiles, 192 threads):
-//   warp 4, one lane: TMA producer over a ring of up to 8 stages (as many as
-//     fit about 200 KB of shared memory);
+//   warp 4, one lane: TMA producer over a ring of kStages stages;
 //   warp 5, one lane: MMA issuer; accumulators double-buffered in TMEM so the
 //     epilogue of one tile overlaps the MMAs of the next;
 //   warps 0-3: epilogue, warp w reading TMEM lanes 32w..32w+31 (its 32 pixels).
@@ -43,8 +42,7 @@ namespace {
 
 constexpr int kTileM = 128;
 constexpr int kChunk = 64;            // input channels per stage
-constexpr int kMaxStages = 8;         // TMA ring depth: as many stages as fit, up to this
-constexpr size_t kRingBudget = 200 * 1024;
+constexpr int kStages = 4;
 constexpr int kThreads = 192;
 constexpr int kMaxCout = 128;
 constexpr int kAccCols = 256;         // TMEM columns: two accumulators of up to 128
@@ -60,7 +58,6 @@ struct ConvParams {
   int tiles;               // B * (H / rows) * xtiles
   int chunks;              // ceil(Cin / 64)
   int chunk_ch;            // channels per chunk (64, or Cin when Cin < 64)
-  int stages;              // depth of the TMA stage ring
   int relu;
   const float* bias;       // [Cout]
   const __nv_bfloat16* skip;   // [P][Cout] or nullptr
@@ -192,8 +189,8 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
 }
 
 struct __align__(8) SmemCtl {
-  uint64_t full[kMaxStages];
-  uint64_t empty[kMaxStages];
+  uint64_t full[kStages];
+  uint64_t empty[kStages];
   uint64_t acc_full[2];
   uint64_t acc_empty[2];
   uint64_t drain;
@@ -222,14 +219,13 @@ __global__ void __launch_bounds__(kThreads, 1)
   const int a_bytes = kTileM * p.chunk_ch * 2;            // 16 KB (8 KB when C_in = 32)
   const int b_bytes = p.Cout * p.chunk_ch * 2;
   const int stage_bytes = ((a_bytes + b_bytes + 1023) / 1024) * 1024;
-  const int nst = p.stages;
-  SmemCtl* ctl = reinterpret_cast<SmemCtl*>(base + nst * stage_bytes);
+  SmemCtl* ctl = reinterpret_cast<SmemCtl*>(base + kStages * stage_bytes);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int swz = p.chunk_ch * 2;                         // 128 or 64 bytes per row
 
   for (int i = threadIdx.x; i < p.Cout; i += kThreads) ctl->bias[i] = p.bias[i];
   if (threadIdx.x == 0) {
-    for (int s = 0; s < nst; ++s) {
+    for (int s = 0; s < kStages; ++s) {
       mbar_init(&ctl->full[s], 1);
       mbar_init(&ctl->empty[s], 1);
     }
@@ -267,7 +263,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         int b, y0, x0;
         tile_origin(p, t, b, y0, x0);
         for (int st = 0; st < nstage_per_tile && ok; ++st, ++q) {
-          const int s = q % nst, ph = (q / nst) & 1;
+          const int s = q % kStages, ph = (q / kStages) & 1;
           if (!mbar_wait(&ctl->empty[s], ph ^ 1, abort, p.err)) { ok = false; break; }
           const int tap = st / p.chunks, ch = st % p.chunks;
           const int ky = tap / 3, kx = tap % 3;
@@ -280,10 +276,10 @@ __global__ void __launch_bounds__(kThreads, 1)
       }
       // copies issued but never consumed (after an abort) finish before exit
       if (!ok) {
-        for (int k = 0; k < nst; ++k) {
+        for (int k = 0; k < kStages; ++k) {
           const int qq = q - 1 - k;
           if (qq < 0) break;
-          const int s = qq % nst, ph = (qq / nst) & 1;
+          const int s = qq % kStages, ph = (qq / kStages) & 1;
           for (unsigned i = 0; i < kSpinLimit && !mbar_try_wait(&ctl->full[s], ph); ++i) {
           }
         }
@@ -300,7 +296,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         const uint32_t d = tmem + buf * acc_stride;
         for (int st = 0; st < nstage_per_tile; ++st, ++q) {
-          const int s = q % nst, ph = (q / nst) & 1;
+          const int s = q % kStages, ph = (q / kStages) & 1;
           if (!mbar_wait(&ctl->full[s], ph, abort, p.err)) { ok = false; break; }
           asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
           const uint32_t sa = smem_u32(base + s * stage_bytes);
@@ -390,19 +386,11 @@ int sm_count() {
 
 }  // namespace
 
-// stage ring depth for a layer: as many stages as fit the ring budget (2..8)
-static int conv_tc_stages(int Cin, int Cout) {
-  const int chunk = Cin < kChunk ? Cin : kChunk;
-  const size_t stage = (((size_t)kTileM * chunk * 2 + (size_t)Cout * chunk * 2 + 1023) / 1024) * 1024;
-  size_t n = kRingBudget / stage;
-  return (int)(n < 2 ? 2 : (n > kMaxStages ? kMaxStages : n));
-}
-
 // dynamic shared memory of one CTA for a layer (stage ring + control block + alignment slack)
 static size_t conv_tc_smem(int Cin, int Cout) {
   const int chunk = Cin < kChunk ? Cin : kChunk;
   const size_t stage = (((size_t)kTileM * chunk * 2 + (size_t)Cout * chunk * 2 + 1023) / 1024) * 1024;
-  const size_t need = conv_tc_stages(Cin, Cout) * stage + sizeof(SmemCtl) + 1024;
+  const size_t need = kStages * stage + sizeof(SmemCtl) + 1024;
   return need > kMinSmem ? need : kMinSmem;
 }
 
@@ -440,7 +428,6 @@ extern "C" int pty_ws_conv3x3_tc(int32_t B, int32_t H, int32_t W, int32_t Cin, i
   p.tiles = B * (H / p.rows) * p.xtiles;
   p.chunk_ch = Cin < kChunk ? Cin : kChunk;
   p.chunks = Cin / p.chunk_ch;
-  p.stages = conv_tc_stages(Cin, Cout);
   p.relu = relu != 0;
   p.bias = bias;
   p.skip = static_cast<const __nv_bfloat16*>(skip);
