@@ -1090,6 +1090,14 @@ def main():
                        frame_tile_ctas={"plain": tiles[0], "background": tiles[1]}),
         "gpu_launches": int(launches), "clocks": clk.summary(), "roofline": roof,
         "cpu_baseline": cpu, "e2e": e2e,
+        "error_vs_fp64": ({"test": "tests/test_gpu_geometry_c1.py",
+                           "bound": "one ERA m6 and one DM m6 iteration on this geometry (1024 frames 256x256) "
+                                    "within 1e-5 relative of the FP64 oracle on O, P, background and eMod"}
+                          if args.workload == "c1" else
+                          {"test": "tests/test_gpu_c4_fp64.py",
+                           "bound": "3 DM m6 iterations within 3e-5 of the chunked FP64 oracle (lit object, "
+                                    "probe, background, eMod)"} if args.workload == "c4" else
+                          {"test": "tests/test_gpu_parity_c0.py", "bound": "1e-5 relative per iteration"}),
     }
     if m1:
         line["era_m1"] = m1
