@@ -270,18 +270,6 @@ int pty_ws_targets(int32_t nf, int64_t npix, const void* psi, const void* P, int
                    float wscale, float* target, float* weight, void* stream);
 int pty_ws_exits(int32_t nf, int64_t npix, const float* y, const void* P, int32_t object_phase,
                  void* psi, void* stream);
-/* The network's forward 3 x 3 convolution (zero padding) on the tensor cores
- * (tcgen05, accumulators in tensor memory, operands staged by TMA), with the
- * bias, activation and skip of pty_ws_bias_act fused:
- *   out[p][co] = act(sum_{tap, ci} X[p shifted by tap][ci] Wt[co][tap C_in + ci]
- *                    + bias[co]) (+ skip[p][co]),
- * X, out, skip NHWC bf16 [B][H][W][C] (skip optional), Wt bf16 [C_out][9 C_in]
- * (the im2col path's layout), bias float [C_out], relu != 0 for ReLU.  The
- * same result as pty_ws_im2col + pty_ws_gemm + pty_ws_bias_act up to the FP32
- * summation order.  C_in = 32 or a multiple of 64, C_out a multiple of 32 up
- * to 128, W dividing 128 (H a multiple of 128 / W) or a multiple of 128;
- * arrays 16-byte aligned; others are PTY_ERR_UNSUPPORTED.  Its mbarrier waits
- * are bounded (see pty_timeout_status). */
 /* The same convolution on the CUDA cores for layers with few channels
  * (C_in even, 2..32; C_out 2, 4, 8, 16 or 32: the network's 2-channel first
  * and last layers), one thread per output pixel, no im2col buffer: out (bf16,
@@ -301,9 +289,23 @@ int pty_ws_crop_center(int32_t nf, int32_t N0, int32_t N1, int32_t M0, int32_t M
                        const int32_t* frames, float scale, float* out, void* stream);
 int pty_ws_upsample_object(int32_t Uh, int32_t Vh, const void* Oh, int32_t U, int32_t V, int32_t f,
                            void* O, void* stream);
+/* The network's forward 3 x 3 convolution (zero padding) on the tensor cores
+ * (tcgen05, accumulators in tensor memory, operands staged by TMA), with the
+ * bias, activation and skip of pty_ws_bias_act fused:
+ *   out[p][co] = act(sum_{tap, ci} X[p shifted by tap][ci] Wt[co][tap C_in + ci]
+ *                    + bias[co]) (+ skip[p][co]),
+ * X, out, skip NHWC bf16 [B][H][W][C] (skip optional), Wt bf16 [C_out][9 C_in]
+ * (the im2col path's layout), bias float [C_out], relu != 0 for ReLU.  The
+ * same result as pty_ws_im2col + pty_ws_gemm + pty_ws_bias_act up to the FP32
+ * summation order.  C_in = 32 or a multiple of 64, C_out a multiple of 32 up
+ * to 128, W dividing 128 (H a multiple of 128 / W) or a multiple of 128;
+ * arrays 16-byte aligned; others are PTY_ERR_UNSUPPORTED.  act, when not
+ * NULL, also receives act(sum + bias) before the skip is added (bf16, as out):
+ * the activation a training pass's backward reads.  Its mbarrier waits are
+ * bounded (see pty_timeout_status). */
 int pty_ws_conv3x3_tc(int32_t B, int32_t H, int32_t W, int32_t Cin, int32_t Cout, const void* X,
                       const void* Wt, const float* bias, int32_t relu, const void* skip, void* out,
-                      void* stream);
+                      void* act, void* stream);
 
 /* 1 if the frame shape N0 x N1 has a fused FFT kernel. */
 int pty_shape_supported(int32_t N0, int32_t N1);

@@ -91,7 +91,7 @@ SIGNATURES = {
                        c_void_p],
     "pty_ws_exits": [c_int32, c_int64, c_void_p, c_void_p, c_int32, c_void_p, c_void_p],
     "pty_ws_conv3x3_tc": [c_int32, c_int32, c_int32, c_int32, c_int32, c_void_p, c_void_p, c_void_p,
-                          c_int32, c_void_p, c_void_p, c_void_p],
+                          c_int32, c_void_p, c_void_p, c_void_p, c_void_p],
     "pty_timeout_status": [ctypes.POINTER(c_int32)],
     "pty_ws_conv3x3_direct": [c_int32, c_int32, c_int32, c_int32, c_int32, c_void_p, c_void_p, c_void_p,
                               c_int32, c_void_p, c_void_p, c_void_p, c_void_p],

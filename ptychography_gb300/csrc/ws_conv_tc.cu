@@ -62,6 +62,7 @@ struct ConvParams {
   const float* bias;       // [Cout]
   const __nv_bfloat16* skip;   // [P][Cout] or nullptr
   __nv_bfloat16* out;          // [P][Cout]
+  __nv_bfloat16* act;          // [P][Cout] the activation before the skip, or nullptr
   int* err;                    // device error flag (set on a wait timeout)
 };
 
@@ -340,13 +341,15 @@ __global__ void __launch_bounds__(kThreads, 1)
         }
         const __nv_bfloat16* sk = p.skip ? p.skip + pix * p.Cout + c0 : nullptr;
         __nv_bfloat16* o = p.out + pix * p.Cout + c0;
+        __nv_bfloat16* ao = p.act ? p.act + pix * p.Cout + c0 : nullptr;
 #pragma unroll
         for (int q4 = 0; q4 < 4; ++q4) {
           uint4 skv = make_uint4(0u, 0u, 0u, 0u);
           if (sk) skv = *reinterpret_cast<const uint4*>(sk + 8 * q4);
           const __nv_bfloat162* s2 = reinterpret_cast<const __nv_bfloat162*>(&skv);
-          uint4 ov;
+          uint4 ov, av;
           __nv_bfloat162* o2 = reinterpret_cast<__nv_bfloat162*>(&ov);
+          __nv_bfloat162* a2 = reinterpret_cast<__nv_bfloat162*>(&av);
 #pragma unroll
           for (int e = 0; e < 4; ++e) {
             float a0 = v[8 * q4 + 2 * e] + ctl->bias[c0 + 8 * q4 + 2 * e];
@@ -356,6 +359,7 @@ __global__ void __launch_bounds__(kThreads, 1)
               a1 = fmaxf(a1, 0.f);
             }
             __nv_bfloat162 h = __floats2bfloat162_rn(a0, a1);
+            a2[e] = h;
             if (sk) {
               const float2 sf = __bfloat1622float2(s2[e]);
               const float2 hf = __bfloat1622float2(h);
@@ -364,6 +368,7 @@ __global__ void __launch_bounds__(kThreads, 1)
             o2[e] = h;
           }
           *reinterpret_cast<uint4*>(o + 8 * q4) = ov;
+          if (ao) *reinterpret_cast<uint4*>(ao + 8 * q4) = av;
         }
       }
     }
@@ -400,7 +405,7 @@ using namespace pty;
 
 extern "C" int pty_ws_conv3x3_tc(int32_t B, int32_t H, int32_t W, int32_t Cin, int32_t Cout,
                                  const void* X, const void* Wt, const float* bias, int32_t relu,
-                                 const void* skip, void* out, void* stream) {
+                                 const void* skip, void* out, void* act, void* stream) {
   if (!X || !Wt || !bias || !out) return set_error(PTY_ERR_ARG, "pty_ws_conv3x3_tc: null argument");
   if (B < 1 || H < 1 || W < 1) return set_error(PTY_ERR_ARG, "pty_ws_conv3x3_tc: empty input");
   if (!(Cin == 32 || Cin % 64 == 0) || Cin > 1024)
@@ -411,7 +416,7 @@ extern "C" int pty_ws_conv3x3_tc(int32_t B, int32_t H, int32_t W, int32_t Cin, i
     return set_error(PTY_ERR_UNSUPPORTED,
                      "pty_ws_conv3x3_tc: 128-pixel tiles need W dividing 128 (and H a multiple of 128 / W) "
                      "or W a multiple of 128");
-  const void* arrays[4] = {X, Wt, out, skip};
+  const void* arrays[5] = {X, Wt, out, skip, act};
   for (const void* q : arrays)
     if (q && (reinterpret_cast<uintptr_t>(q) & 15))
       return set_error(PTY_ERR_ARG, "pty_ws_conv3x3_tc: arrays must be 16-byte aligned");
@@ -432,6 +437,7 @@ extern "C" int pty_ws_conv3x3_tc(int32_t B, int32_t H, int32_t W, int32_t Cin, i
   p.bias = bias;
   p.skip = static_cast<const __nv_bfloat16*>(skip);
   p.out = static_cast<__nv_bfloat16*>(out);
+  p.act = static_cast<__nv_bfloat16*>(act);
   p.err = err;
   const CUtensorMapSwizzle swz = p.chunk_ch == 64 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_64B;
 

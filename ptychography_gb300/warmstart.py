@@ -133,6 +133,7 @@ class WarmStartNet:
         B, H, W = x.shape[0], self.H, self.W
         lib, sp = self.lib, self._sp()
         self._x = x
+        self._fwd_inputs = None          # the im2col path keeps its own col buffers
         h1 = self._conv_fwd(0, x, B, H, W)
         p1 = self._buf("p1", (B, H // 2, W // 2, 32), torch.bfloat16)
         _native.check(lib.pty_ws_pool2(B, H, W, 32, _p(h1), _p(p1), sp))
@@ -148,15 +149,64 @@ class WarmStartNet:
         h5 = self._conv_fwd(4, u4, B, H, W, skip=h1)
         return self._conv_fwd(5, h5, B, H, W, last=True)
 
-    def _conv_tc(self, i, x, B, H, W, skip=None):
+    def _conv_tc(self, i, x, B, H, W, skip=None, keep=False):
         """Layer i on the tensor-core implicit-GEMM convolution (bias,
-        activation and skip fused): x (B, H, W, C_in) bf16 -> (B, H, W, C_out) bf16."""
+        activation and skip fused): x (B, H, W, C_in) bf16 -> (B, H, W, C_out) bf16.
+        With keep (a training pass) the activation before the skip goes to the
+        layer's "a%d" buffer for the backward pass."""
         torch = _torch()
         cin, cout, relu, _ = LAYERS[i]
         out = self._buf("t%d" % i, (B, H, W, cout), torch.bfloat16)
+        act = None
+        if keep:
+            act = self._buf("a%d" % i, (B, H, W, cout), torch.bfloat16) if skip is not None else out
+            if skip is None:
+                self._bufs["a%d" % i] = out.view(-1)
         _native.check(self.lib.pty_ws_conv3x3_tc(B, H, W, cin, cout, _p(x), _p(self.wb[i]), _p(self.b[i]),
-                                                 int(relu), _p(skip), _p(out), self._sp()))
+                                                 int(relu), _p(skip), _p(out),
+                                                 _p(act) if skip is not None else None, self._sp()))
         return out
+
+    def _tc_supported(self, B):
+        """Whether layers 1-4 fit the tensor-core convolution's tile rules at
+        this frame size (W at least 8 and dividing 128, H a multiple of
+        128 / W, or W a multiple of 128)."""
+        ok = True
+        for H, W in ((self.H // 2, self.W // 2), (self.H // 4, self.W // 4), (self.H, self.W)):
+            ok = ok and W >= 8 and ((W < 128 and 128 % W == 0 and H % (128 // W) == 0) or W % 128 == 0)
+        return ok
+
+    def forward_train(self, x):
+        """The forward pass of a training step on the tensor cores: layers 1-4
+        on pty_ws_conv3x3_tc (keeping each layer's activation for the
+        backward pass), the 2-channel layers on the direct convolution;
+        backward() then forms the im2col buffers its weight gradients need.
+        Falls back to forward() (im2col + mma.sync) where the frame size does
+        not fit the tensor-core tiles.  x: (B, H, W, 2) bf16; returns y."""
+        torch = _torch()
+        B, H, W = x.shape[0], self.H, self.W
+        if not self._tc_supported(B):
+            self._fwd_inputs = None
+            return self.forward(x)
+        lib, sp = self.lib, self._sp()
+        self._x = x
+        h1 = self._conv_direct(0, x, B, H, W)
+        self._bufs["a0"] = h1.view(-1)
+        p1 = self._buf("p1", (B, H // 2, W // 2, 32), torch.bfloat16)
+        _native.check(lib.pty_ws_pool2(B, H, W, 32, _p(h1), _p(p1), sp))
+        h2 = self._conv_tc(1, p1, B, H // 2, W // 2, keep=True)
+        p2 = self._buf("p2", (B, H // 4, W // 4, 64), torch.bfloat16)
+        _native.check(lib.pty_ws_pool2(B, H // 2, W // 2, 64, _p(h2), _p(p2), sp))
+        h3 = self._conv_tc(2, p2, B, H // 4, W // 4, keep=True)
+        u3 = self._buf("u3", (B, H // 2, W // 2, 128), torch.bfloat16)
+        _native.check(lib.pty_ws_up2(B, H // 4, W // 4, 128, _p(h3), _p(u3), sp))
+        h4 = self._conv_tc(3, u3, B, H // 2, W // 2, skip=h2, keep=True)
+        u4 = self._buf("u4", (B, H, W, 64), torch.bfloat16)
+        _native.check(lib.pty_ws_up2(B, H // 2, W // 2, 64, _p(h4), _p(u4), sp))
+        h5 = self._conv_tc(4, u4, B, H, W, skip=h1, keep=True)
+        # the layer inputs the backward pass's im2col reads
+        self._fwd_inputs = (x, p1, p2, u3, u4, h5)
+        return self._conv_direct(5, h5, B, H, W, last=True)
 
     def _conv_direct(self, i, x, B, H, W, last=False):
         """Layer i on the CUDA-core direct convolution (the 2-channel first
@@ -206,6 +256,10 @@ class WarmStartNet:
         lib, sp = self.lib, self._sp()
         P, K = B * H * W, 9 * cin
         a = self._bufs["a%d" % i] if relu else None
+        if getattr(self, "_fwd_inputs", None) is not None:
+            # a tensor-core forward pass wrote no im2col buffer: form it now
+            col = self._buf("col%d" % i, (P, K), torch.bfloat16)
+            _native.check(lib.pty_ws_im2col(B, H, W, cin, _p(self._fwd_inputs[i]), _p(col), sp))
         dZ = self._buf("dz", (P, cout), torch.bfloat16)
         scr = self._buf("actscr", (int(lib.pty_ws_act_bwd_scratch(P, cout)),), torch.float32)
         _native.check(lib.pty_ws_act_bwd(P, cout, _p(dA), _p(a), int(relu), _p(dZ), _p(self.gb[i]),
@@ -269,8 +323,14 @@ class WarmStartNet:
             _native.check(self.lib.pty_ws_adam(w.numel(), _p(w), _p(wb), _p(g), _p(m), _p(v),
                                                lr, b1, b2, eps, self.step_count, sp))
 
-    def train_step(self, x, target, weight, lr=1e-3):
-        y = self.forward(x)
+    def train_step(self, x, target, weight, lr=1e-3, tensor_cores=True):
+        """One Adam step on a batch; the forward pass on the tensor cores
+        (forward_train) unless tensor_cores is False (forward)."""
+        if tensor_cores:
+            y = self.forward_train(x)
+        else:
+            self._fwd_inputs = None
+            y = self.forward(x)
         parts, dy = self.loss_grad(y, target, weight)
         self.backward(dy)
         self.adam_step(lr)

@@ -79,7 +79,7 @@ def test_conv_tc_matches_fp64_and_im2col_path(case):
     skd = bf16(sk) if has_skip else None
     out = torch.empty((B, H, W, cout), dtype=torch.bfloat16, device=dev())
     _native.check(lib.pty_ws_conv3x3_tc(B, H, W, cin, cout, p(xd), p(wd), p(bd), int(relu), p(skd),
-                                        p(out), stream()))
+                                        p(out), None, stream()))
     assert status_ok()
     got = out.float().cpu().numpy().astype(np.float64)
     xr = xd.float().cpu().numpy().astype(np.float64)
@@ -109,7 +109,7 @@ def test_conv_tc_rejects_unsupported_shapes():
     t = torch.zeros(1 << 16, dtype=torch.bfloat16, device=dev())
     bd = torch.zeros(256, dtype=torch.float32, device=dev())
     for args in ((1, 8, 8, 48, 32), (1, 8, 8, 64, 48), (1, 8, 8, 64, 256), (1, 8, 96, 64, 32)):
-        rc = lib.pty_ws_conv3x3_tc(*args, p(t), p(t), p(bd), 1, None, p(t), stream())
+        rc = lib.pty_ws_conv3x3_tc(*args, p(t), p(t), p(bd), 1, None, p(t), None, stream())
         assert rc == 6, args
 
 
@@ -184,7 +184,7 @@ def test_crop_and_upsample_match_numpy():
     I = rng.random((3, 32, 32)).astype(np.float32)
     Id = torch.from_numpy(I).to(dev())
     out = torch.empty((3, 16, 16), dtype=torch.float32, device=dev())
-    _native.check(lib.pty_ws_crop_center(3, 32, 32, 16, 16, p(Id), None, 0.5, p(out), stream()))
+    _native.check(lib.pty_ws_crop_center(3, 32, 32, 16, 16, p(Id), None, 0.5, p(out), None, stream()))
     np.testing.assert_array_equal(out.cpu().numpy(), 0.5 * I[:, 8:24, 8:24])
     sel = torch.tensor([2, 0], dtype=torch.int32, device=dev())
     out2 = torch.empty((2, 16, 16), dtype=torch.float32, device=dev())
@@ -234,3 +234,32 @@ def test_downsampled_start_sees_the_object():
     assert o.shape == (U, U) and np.all(np.isfinite(o))
     assert np.abs(o[128:256, 128:256]).min() > 0
     assert np.abs(o).max() <= 1.0 + 1e-4
+
+
+def test_training_forward_on_tensor_cores_gives_the_same_gradients():
+    """A training step whose forward pass runs on the tensor cores
+    (forward_train: layers 1-4 on pty_ws_conv3x3_tc keeping their
+    activations, the backward pass forming its own im2col buffers) gives the
+    weight and bias gradients of the im2col + mma.sync forward pass, up to
+    the FP32 summation order of the forward sums (one BF16 rounding step on
+    some activations): within 3e-2 norm-wise per layer."""
+    net = WarmStartNet(128, 128, seed=4, device=dev())
+    rng = np.random.default_rng(9)
+    B = 8
+    x = bf16(rng.standard_normal((B, 128, 128, 2)) * 0.5)
+    t = torch.from_numpy(rng.standard_normal((B, 128, 128, 2)).astype(np.float32)).to(dev())
+    wgt = torch.full((B, 128, 128), 1.0 / (B * 128 * 128), dtype=torch.float32, device=dev())
+    grads = []
+    for train in (False, True):
+        y = net.forward_train(x) if train else net.forward(x)
+        parts, dy = net.loss_grad(y, t, wgt)
+        net.backward(dy)
+        torch.cuda.synchronize()
+        grads.append(([g.clone() for g in net.gw], [g.clone() for g in net.gb], float(parts.sum().cpu())))
+    assert status_ok()
+    (gw0, gb0, l0), (gw1, gb1, l1) = grads
+    assert abs(l1 - l0) < 1e-2 * abs(l0)
+    for i in range(len(LAYERS)):
+        ew = float((gw1[i] - gw0[i]).norm() / gw0[i].norm())
+        eb = float((gb1[i] - gb0[i]).norm() / (gb0[i].norm() + 1e-30))
+        assert ew < 3e-2 and eb < 3e-2, (i, ew, eb)
