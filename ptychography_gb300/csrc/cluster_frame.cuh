@@ -46,36 +46,6 @@ PTY_DEV void cluster_sync_relaxed() {
 PTY_DEV void cluster_arrive_release() { asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory"); }
 PTY_DEV void cluster_wait_acquire() { asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory"); }
 
-#ifndef PTY_ASYNC_PUSH
-#define PTY_ASYNC_PUSH 0
-#endif
-// The row pass's pushes as asynchronous remote stores (st.async) that count
-// their bytes on the receiving CTA's mbarrier: the receiver starts its column
-// pass when its own barrier has seen all N x CPC elements, with no cluster-wide
-// release / acquire barrier in between.
-PTY_DEV uint32_t cl_smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
-PTY_DEV uint32_t cl_mapa(uint32_t local, int rank) {
-  uint32_t r;
-  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(local), "r"(rank));
-  return r;
-}
-PTY_DEV void cl_st_async(uint32_t remote, float2 v, uint32_t remote_bar) {
-  asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.v2.f32 [%0], {%1, %2}, [%3];" ::"r"(remote),
-               "f"(v.x), "f"(v.y), "r"(remote_bar)
-               : "memory");
-}
-PTY_DEV bool cl_try_wait_cluster(uint32_t bar, unsigned parity) {
-  uint32_t ok;
-  asm volatile(
-      "{\n\t.reg .pred p;\n\t"
-      "mbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2;\n\t"
-      "selp.u32 %0, 1, 0, p;\n\t}"
-      : "=r"(ok)
-      : "r"(bar), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-
 template <int N, int C>
 struct ClusterCfg {
   static constexpr int A = LineGeom<N>::A, B = LineGeom<N>::B;  // rows and columns alike
@@ -91,7 +61,7 @@ struct ClusterCfg {
   static constexpr int JPC = CPC / A;        // row registers per destination CTA
   static constexpr size_t CBUF = (size_t)N * CP + N / A;  // + one skew slot per A rows
   static constexpr size_t RSCR = (size_t)RF * ROWLEN;
-  static constexpr size_t SMEM = (CBUF + RSCR + N) * sizeof(float2) + 32 * sizeof(double) + 16;
+  static constexpr size_t SMEM = (CBUF + RSCR + N) * sizeof(float2) + 32 * sizeof(double);
   static_assert(RPC % RF == 0 && CPC % CW == 0 && CPC % A == 0 && CW >= 8, "cluster split");
   static_assert(SMEM <= 227 * 1024, "shared memory budget");
   // the column pass exchanges through the (then idle) row scratch
@@ -121,19 +91,6 @@ __global__ void __launch_bounds__(ClusterCfg<N, C>::NT, ClusterCfg<N, C>::MINB)
   float2* tw = rscr + K::RSCR;                            // [N]
   double* red = reinterpret_cast<double*>(tw + N);
   for (int i = tid; i < N; i += K::NT) tw[i] = g.tw0[i];
-#if PTY_ASYNC_PUSH
-  uint64_t* pbar = reinterpret_cast<uint64_t*>(red + 32);
-  constexpr unsigned kPushBytes = (unsigned)N * CPC * sizeof(float2);
-  if (tid == 0) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(cl_smem_u32(pbar)) : "memory");
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(cl_smem_u32(pbar)), "r"(kPushBytes)
-                 : "memory");
-  }
-  // every barrier initialised before any peer pushes into it (waited for
-  // just before the first push)
-  asm volatile("barrier.cluster.arrive.relaxed.aligned;" ::: "memory");
-#endif
 
   // Column buffer: element (row r, owned column cl) at r * CP + cl + r / A.
   // With CP odd and the skew of one slot per A rows, both the natural walk
@@ -169,36 +126,15 @@ __global__ void __launch_bounds__(ClusterCfg<N, C>::NT, ClusterCfg<N, C>::MINB)
     __syncwarp();
     line_stage2<N, OpTraits<OP>::FIRST_DIR>(v, t, [&](int tt, int k1) { return rs[k1 * (A + 1) + tt]; });
     // v[j] = X[a][t + A j]; column t + A j belongs to CTA j / JPC
-#if PTY_ASYNC_PUSH
-    if (s == 0) asm volatile("barrier.cluster.wait.aligned;" ::: "memory");
-#pragma unroll
-    for (int j = 0; j < B; ++j) {
-      const int q = j / JPC;
-      cl_st_async(cl_mapa(cl_smem_u32(&cbuf[cidx(a, t + A * (j % JPC))]), q), v[j], cl_mapa(cl_smem_u32(pbar), q));
-    }
-#else
 #pragma unroll
     for (int j = 0; j < B; ++j) rc(j / JPC)[cidx(a, t + A * (j % JPC))] = v[j];
-#endif
   }
   // the modulus inputs of the first column sub-pass are loaded while the
-  // cluster barrier (or the pushes into this CTA) completes
+  // cluster barrier completes
   ModIn<OP, B> m;
-#if PTY_ASYNC_PUSH
-  modulus_load<N, N, OP, A, B>(g, f, fbase, tid / CW, rank * CPC + tid % CW, m);
-  {
-    // bounded: past the limit the flag is set and the pass runs on whatever
-    // arrived (outputs invalid); every CTA still meets the cluster barriers
-    // below, so none exits while a peer may push into it
-    bool ok = false;
-    for (unsigned i = 0; i < (1u << 26) && !ok; ++i) ok = cl_try_wait_cluster(cl_smem_u32(pbar), 0);
-    if (!ok && g.timeout) atomicExch(g.timeout, 1);
-  }
-#else
   cluster_arrive_release();
   modulus_load<N, N, OP, A, B>(g, f, fbase, tid / CW, rank * CPC + tid % CW, m);
   cluster_wait_acquire();
-#endif
 
   // ---------------- 3. column pass on the owned columns
   // Lanes of a warp run along a row (coalesced amp / mask / background
@@ -262,9 +198,6 @@ __global__ void __launch_bounds__(ClusterCfg<N, C>::NT, ClusterCfg<N, C>::MINB)
     // barrier suffices to keep the column buffers alive until every pull is done
     cluster_sync_relaxed();
   }
-#if PTY_ASYNC_PUSH
-  if constexpr (!INVERSE) cluster_sync_relaxed();   // no CTA leaves while peers may push into it
-#endif
 
   if (g.err_part) {
     const double sum = block_sum_d(ff_to_double(err), red);
