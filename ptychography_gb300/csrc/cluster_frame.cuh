@@ -234,19 +234,12 @@ static cudaLaunchConfig_t cluster_config(int nframes, cudaStream_t st, cudaLaunc
   attr[0].val.clusterDim.z = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-#if defined(PTY_CLUSTER_POLICY) && PTY_CLUSTER_POLICY > 0
-  // tuning builds: the cluster scheduling preference (1 spread, 2 load balancing)
-  attr[1].id = cudaLaunchAttributeClusterSchedulingPolicyPreference;
-  attr[1].val.clusterSchedulingPolicyPreference =
-      PTY_CLUSTER_POLICY == 1 ? cudaClusterSchedulingPolicySpread : cudaClusterSchedulingPolicyLoadBalancing;
-  cfg.numAttrs = 2;
-#endif
   return cfg;
 }
 
 template <int N, int C, int OP>
 static int launch_cluster(const FrameArgs& a, int nframes, cudaStream_t st) {
-  cudaLaunchAttribute attr[2];
+  cudaLaunchAttribute attr[1];
   cudaLaunchConfig_t cfg = cluster_config<N, C>(nframes, st, attr);
   cudaError_t e = cudaLaunchKernelEx(&cfg, cluster_frame_kernel<N, C, OP>, a);
   if (e != cudaSuccess) return set_cuda_error(e, "cluster_frame_kernel launch");
@@ -269,7 +262,7 @@ static int prepare_cluster_tile() {
   if (!rc) rc = set_cluster_attr<N, C, OP_MERR_PSI>();
   if (!rc) rc = set_cluster_attr<N, C, OP_BP>();
   if (rc) return rc;
-  cudaLaunchAttribute attr[2];
+  cudaLaunchAttribute attr[1];
   cudaLaunchConfig_t cfg = cluster_config<N, C>(1, nullptr, attr);
   int nclusters = 0;
   cudaError_t e = cudaOccupancyMaxActiveClusters(&nclusters, cluster_frame_kernel<N, C, OP_PSI7>, &cfg);
