@@ -346,13 +346,6 @@ const char* pty_last_error(void);
  * counterpart. */
 int pty_timeout_status(int32_t* timed_out);
 int pty_version(void);
-/* *yes = 1 when the current device reads ordinary (pageable) host memory
- * coherently through the host's page tables (Grace-Blackwell NVLink-C2C), so
- * that a kernel may be handed a host pointer to data the host has written;
- * 0 otherwise.  The public ERA / DM calls then read the intensities straight
- * from the caller's array instead of uploading a copy.  No reference
- * counterpart. */
-int pty_device_reads_pageable_memory(int32_t* yes);
 /* Kernels this library has launched in the process so far (direct launches
  * plus the kernel nodes of replayed CUDA graphs).  No reference counterpart:
  * it lets a caller confirm the GPU path ran. */

@@ -149,16 +149,6 @@ def _ptr(t):
     return ctypes.c_void_p(t.data_ptr()) if t is not None else None
 
 
-class _HostArray:
-    """A host NumPy array handed to a kernel as a pointer (see device_reads_host)."""
-
-    def __init__(self, a):
-        self.a = a
-
-    def data_ptr(self):
-        return self.a.ctypes.data
-
-
 def device_random_background(lib, out, rdt, sp):
     """np.random.random(out.shape).astype(rdt) + 0.1 (as float32) into the
     device tensor `out`, drawn on the GPU from NumPy's global legacy generator,
@@ -180,21 +170,6 @@ def device_random_background(lib, out, rdt, sp):
 
 
 _SIDE = {}
-_HOST_READ = {}          # per device: kernels may read pageable host memory
-HOST_READ_ENABLED = True
-
-
-def device_reads_host(lib, dev):
-    """Whether kernels on `dev` may read the caller's host arrays in place
-    (coherent pageable-memory access through the host's page tables)."""
-    if not HOST_READ_ENABLED:
-        return False
-    v = _HOST_READ.get(dev.index)
-    if v is None:
-        yes = ctypes.c_int32(0)
-        _native.check(lib.pty_device_reads_pageable_memory(ctypes.byref(yes)))
-        v = _HOST_READ[dev.index] = bool(yes.value)
-    return v
 
 
 def _side_stream(dev):
@@ -319,15 +294,7 @@ class _Job:
             Iin = pre.I
             if Iin.dtype not in (np.float32, np.float64):
                 Iin = Iin.astype(np.float64)
-            Iin = np.ascontiguousarray(Iin)
-            if device_reads_host(lib, dev):
-                # the amplitude kernel reads the caller's array over the
-                # coherent host link (no staging copy); the array outlives
-                # the kernel: the job holds it until the run has synchronised
-                self._I_host = Iin
-                I_d = _HostArray(Iin)
-            else:
-                I_d = torch.from_numpy(Iin).to(dev, non_blocking=False)
+            I_d = torch.from_numpy(np.ascontiguousarray(Iin)).to(dev, non_blocking=False)
             amp = torch.empty((n, N0, N1), dtype=torch.float32, device=dev)
             mask_d = torch.from_numpy(pre.mask).to(dev) if pre.mask is not None else None
             if pre.I_norm is None:

@@ -105,7 +105,6 @@ SIGNATURES = {
     "pty_set_frame_tile": [c_int32, c_int32, c_int32, c_int32],
     "pty_last_error": [],
     "pty_version": [],
-    "pty_device_reads_pageable_memory": [ctypes.POINTER(c_int32)],
     "pty_launch_count": [],
 }
 _RESTYPES = {"pty_last_error": ctypes.c_char_p, "pty_launch_count": ctypes.c_int64,

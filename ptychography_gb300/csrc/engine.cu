@@ -163,16 +163,6 @@ extern "C" int pty_version(void) { return 100; }
 
 extern "C" int64_t pty_launch_count(void) { return (int64_t)launch_total(); }
 
-extern "C" int pty_device_reads_pageable_memory(int32_t* yes) {
-  if (!yes) return set_error(PTY_ERR_ARG, "pty_device_reads_pageable_memory: null argument");
-  int dev = 0, pageable = 0, host_tables = 0;
-  PTY_CUDA(cudaGetDevice(&dev));
-  PTY_CUDA(cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, dev));
-  PTY_CUDA(cudaDeviceGetAttribute(&host_tables, cudaDevAttrPageableMemoryAccessUsesHostPageTables, dev));
-  *yes = (pageable && host_tables) ? 1 : 0;
-  return PTY_OK;
-}
-
 extern "C" const char* pty_last_error(void) { return g_last_error.c_str(); }
 
 extern "C" int pty_timeout_status(int32_t* timed_out) {
