@@ -810,7 +810,7 @@ struct BfVec<2> {
   }
 };
 
-template <int COUT, int VEC>
+template <int COUT, int VEC, int PX>
 __global__ void __launch_bounds__(kDirThreads) ws_conv_direct_kernel(int Bt, int H, int W, int Cin,
                                                                      const __nv_bfloat16* __restrict__ X,
                                                                      const __nv_bfloat16* __restrict__ Wt,
@@ -818,6 +818,8 @@ __global__ void __launch_bounds__(kDirThreads) ws_conv_direct_kernel(int Bt, int
                                                                      const __nv_bfloat16* __restrict__ skip,
                                                                      __nv_bfloat16* __restrict__ out,
                                                                      float* __restrict__ out32) {
+  // a thread owns PX consecutive pixels of a row (W a multiple of PX), so
+  // every weight read from shared memory feeds PX multiply-adds
   extern __shared__ float wsm[];                 // [9 Cin][COUT]
   const int K = 9 * Cin;
   for (int i = threadIdx.x; i < K * COUT; i += blockDim.x) {
@@ -825,62 +827,84 @@ __global__ void __launch_bounds__(kDirThreads) ws_conv_direct_kernel(int Bt, int
     wsm[k * COUT + co] = __bfloat162float(Wt[i]);
   }
   __syncthreads();
-  const int P = Bt * H * W;                      // < 2^31 (checked on the host)
-  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < P; p += gridDim.x * blockDim.x) {
-    const int x = p % W, t = p / W, y = t % H, b = t / H;
-    float acc[COUT];
+  const int Wq = W / PX;
+  const int Q = Bt * H * Wq;                     // pixel groups (< 2^31, checked on the host)
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < Q; q += gridDim.x * blockDim.x) {
+    const int x0 = (q % Wq) * PX, t = q / Wq, y = t % H, b = t / H;
+    float acc[PX][COUT];
 #pragma unroll
-    for (int c = 0; c < COUT; ++c) acc[c] = 0.f;
+    for (int u = 0; u < PX; ++u)
+#pragma unroll
+      for (int c = 0; c < COUT; ++c) acc[u][c] = 0.f;
 #pragma unroll 1
     for (int tap = 0; tap < 9; ++tap) {
-      const int yy = y + tap / 3 - 1, xx = x + tap % 3 - 1;
-      if (yy < 0 || yy >= H || xx < 0 || xx >= W) continue;
-      const __nv_bfloat16* xp = X + ((size_t)(b * H + yy) * W + xx) * Cin;
+      const int yy = y + tap / 3 - 1;
+      if (yy < 0 || yy >= H) continue;
+      const int dx = tap % 3 - 1;
+      const __nv_bfloat16* xrow = X + (size_t)(b * H + yy) * W * Cin;
       const float* wk = wsm + tap * Cin * COUT;
       for (int ci = 0; ci < Cin; ci += VEC) {
-        float v[VEC];
-        BfVec<VEC>::load(xp + ci, v);
+        float v[PX][VEC];
+#pragma unroll
+        for (int u = 0; u < PX; ++u) {
+          const int xx = x0 + u + dx;
+          if (xx >= 0 && xx < W) {
+            BfVec<VEC>::load(xrow + (size_t)xx * Cin + ci, v[u]);
+          } else {
+#pragma unroll
+            for (int j = 0; j < VEC; ++j) v[u][j] = 0.f;
+          }
+        }
 #pragma unroll
         for (int j = 0; j < VEC; ++j)
 #pragma unroll
-          for (int c = 0; c < COUT; ++c) acc[c] = fmaf(v[j], wk[(ci + j) * COUT + c], acc[c]);
+          for (int c = 0; c < COUT; ++c) {
+            const float wv = wk[(ci + j) * COUT + c];
+#pragma unroll
+            for (int u = 0; u < PX; ++u) acc[u][c] = fmaf(v[u][j], wv, acc[u][c]);
+          }
       }
     }
 #pragma unroll
-    for (int c = 0; c < COUT; ++c) {
-      acc[c] += bias[c];
-      if (relu) acc[c] = fmaxf(acc[c], 0.f);
-    }
-    const size_t o = (size_t)p * COUT;
-    if (out32) {
-      if constexpr (COUT % 4 == 0) {
+    for (int u = 0; u < PX; ++u) {
 #pragma unroll
-        for (int c = 0; c < COUT; c += 4)
-          *reinterpret_cast<float4*>(out32 + o + c) = make_float4(acc[c], acc[c + 1], acc[c + 2], acc[c + 3]);
-      } else {
-#pragma unroll
-        for (int c = 0; c < COUT; c += 2) *reinterpret_cast<float2*>(out32 + o + c) = make_float2(acc[c], acc[c + 1]);
+      for (int c = 0; c < COUT; ++c) {
+        acc[u][c] += bias[c];
+        if (relu) acc[u][c] = fmaxf(acc[u][c], 0.f);
       }
-    }
-    if (out) {
-      __nv_bfloat162 hv[COUT / 2];
+      const size_t o = ((size_t)(b * H + y) * W + x0 + u) * COUT;
+      if (out32) {
+        if constexpr (COUT % 4 == 0) {
 #pragma unroll
-      for (int c = 0; c < COUT; c += 2) {
-        __nv_bfloat162 a2 = __floats2bfloat162_rn(acc[c], acc[c + 1]);
-        if (skip) {
-          const float2 af = __bfloat1622float2(a2);
-          const float2 sf = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(skip + o + c));
-          a2 = __floats2bfloat162_rn(af.x + sf.x, af.y + sf.y);
+          for (int c = 0; c < COUT; c += 4)
+            *reinterpret_cast<float4*>(out32 + o + c) =
+                make_float4(acc[u][c], acc[u][c + 1], acc[u][c + 2], acc[u][c + 3]);
+        } else {
+#pragma unroll
+          for (int c = 0; c < COUT; c += 2)
+            *reinterpret_cast<float2*>(out32 + o + c) = make_float2(acc[u][c], acc[u][c + 1]);
         }
-        hv[c / 2] = a2;
       }
-      if constexpr (COUT % 8 == 0) {
+      if (out) {
+        __nv_bfloat162 hv[COUT / 2];
 #pragma unroll
-        for (int c = 0; c < COUT; c += 8)
-          *reinterpret_cast<uint4*>(out + o + c) = *reinterpret_cast<const uint4*>(&hv[c / 2]);
-      } else {
+        for (int c = 0; c < COUT; c += 2) {
+          __nv_bfloat162 a2 = __floats2bfloat162_rn(acc[u][c], acc[u][c + 1]);
+          if (skip) {
+            const float2 af = __bfloat1622float2(a2);
+            const float2 sf = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(skip + o + c));
+            a2 = __floats2bfloat162_rn(af.x + sf.x, af.y + sf.y);
+          }
+          hv[c / 2] = a2;
+        }
+        if constexpr (COUT % 8 == 0) {
 #pragma unroll
-        for (int c = 0; c < COUT; c += 2) *reinterpret_cast<__nv_bfloat162*>(out + o + c) = hv[c / 2];
+          for (int c = 0; c < COUT; c += 8)
+            *reinterpret_cast<uint4*>(out + o + c) = *reinterpret_cast<const uint4*>(&hv[c / 2]);
+        } else {
+#pragma unroll
+          for (int c = 0; c < COUT; c += 2) *reinterpret_cast<__nv_bfloat162*>(out + o + c) = hv[c / 2];
+        }
       }
     }
   }
@@ -919,22 +943,31 @@ __global__ void ws_upsample_kernel(int Uh, int Vh, const float2* __restrict__ Oh
   }
 }
 
+template <int COUT, int VEC, int PX>
+void direct_grid(int B, int H, int W, int Cin, const void* X, const void* Wt, const float* bias, int relu,
+                 const void* skip, void* out, float* out32, size_t smem, cudaStream_t st) {
+  const long long Q = (long long)B * H * (W / PX);
+  long long g = (Q + kDirThreads - 1) / kDirThreads;
+  if (g > 32 * 152) g = 32 * 152;
+  ws_conv_direct_kernel<COUT, VEC, PX><<<(unsigned)g, kDirThreads, smem, st>>>(
+      B, H, W, Cin, (const __nv_bfloat16*)X, (const __nv_bfloat16*)Wt, bias, relu, (const __nv_bfloat16*)skip,
+      (__nv_bfloat16*)out, out32);
+}
+
 template <int COUT>
 int launch_direct(int B, int H, int W, int Cin, const void* X, const void* Wt, const float* bias, int relu,
                   const void* skip, void* out, float* out32, cudaStream_t st) {
   const size_t smem = (size_t)9 * Cin * COUT * sizeof(float);
-  const long long P = (long long)B * H * W;
-  long long g = (P + kDirThreads - 1) / kDirThreads;
-  if (g > 32 * 152) g = 32 * 152;
   const bool v8 = Cin % 8 == 0 && ((uintptr_t)X & 15u) == 0;
-  if (v8)
-    ws_conv_direct_kernel<COUT, 8><<<(unsigned)g, kDirThreads, smem, st>>>(
-        B, H, W, Cin, (const __nv_bfloat16*)X, (const __nv_bfloat16*)Wt, bias, relu, (const __nv_bfloat16*)skip,
-        (__nv_bfloat16*)out, out32);
-  else
-    ws_conv_direct_kernel<COUT, 2><<<(unsigned)g, kDirThreads, smem, st>>>(
-        B, H, W, Cin, (const __nv_bfloat16*)X, (const __nv_bfloat16*)Wt, bias, relu, (const __nv_bfloat16*)skip,
-        (__nv_bfloat16*)out, out32);
+  // pixels per thread: more for narrow outputs (fewer accumulators)
+  constexpr int PXW = COUT <= 4 ? 4 : 2;
+  if (W % PXW == 0) {
+    if (v8) direct_grid<COUT, 8, PXW>(B, H, W, Cin, X, Wt, bias, relu, skip, out, out32, smem, st);
+    else direct_grid<COUT, 2, PXW>(B, H, W, Cin, X, Wt, bias, relu, skip, out, out32, smem, st);
+  } else {
+    if (v8) direct_grid<COUT, 8, 1>(B, H, W, Cin, X, Wt, bias, relu, skip, out, out32, smem, st);
+    else direct_grid<COUT, 2, 1>(B, H, W, Cin, X, Wt, bias, relu, skip, out, out32, smem, st);
+  }
   return check_launch("ws_conv_direct_kernel");
 }
 

@@ -129,7 +129,8 @@ def test_inference_pass_matches_im2col_network():
 
 
 @pytest.mark.parametrize("case", [(2, 128, 128, 2, 32, True), (2, 128, 128, 32, 2, False),
-                                  (1, 16, 24, 8, 16, True)], ids=lambda c: "x".join(map(str, c[:5])))
+                                  (1, 16, 24, 8, 16, True), (1, 9, 15, 4, 8, True), (1, 6, 10, 32, 2, False)],
+                         ids=lambda c: "x".join(map(str, c[:5])))
 def test_conv_direct_matches_fp64(case):
     """The CUDA-core direct convolution (the network's 2-channel layers) against
     the float64 reference of the same BF16 operands, for both its outputs: the
