@@ -818,8 +818,9 @@ __global__ void __launch_bounds__(kDirThreads) ws_conv_direct_kernel(int Bt, int
                                                                      const __nv_bfloat16* __restrict__ skip,
                                                                      __nv_bfloat16* __restrict__ out,
                                                                      float* __restrict__ out32) {
-  // a thread owns PX consecutive pixels of a row (W a multiple of PX), so
-  // every weight read from shared memory feeds PX multiply-adds
+  // a thread owns PX pixels of a row, 32 apart (W a multiple of 32 PX when
+  // PX > 1), so that every weight read from shared memory feeds PX
+  // multiply-adds while the lanes of a warp still read neighbouring pixels
   extern __shared__ float wsm[];                 // [9 Cin][COUT]
   const int K = 9 * Cin;
   for (int i = threadIdx.x; i < K * COUT; i += blockDim.x) {
@@ -830,7 +831,8 @@ __global__ void __launch_bounds__(kDirThreads) ws_conv_direct_kernel(int Bt, int
   const int Wq = W / PX;
   const int Q = Bt * H * Wq;                     // pixel groups (< 2^31, checked on the host)
   for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < Q; q += gridDim.x * blockDim.x) {
-    const int x0 = (q % Wq) * PX, t = q / Wq, y = t % H, b = t / H;
+    const int xi = q % Wq, t = q / Wq, y = t % H, b = t / H;
+    const int x0 = PX > 1 ? (xi >> 5) * 32 * PX + (xi & 31) : xi;   // pixel u at x0 + 32 u
     float acc[PX][COUT];
 #pragma unroll
     for (int u = 0; u < PX; ++u)
@@ -847,7 +849,7 @@ __global__ void __launch_bounds__(kDirThreads) ws_conv_direct_kernel(int Bt, int
         float v[PX][VEC];
 #pragma unroll
         for (int u = 0; u < PX; ++u) {
-          const int xx = x0 + u + dx;
+          const int xx = x0 + 32 * u + dx;
           if (xx >= 0 && xx < W) {
             BfVec<VEC>::load(xrow + (size_t)xx * Cin + ci, v[u]);
           } else {
@@ -872,7 +874,7 @@ __global__ void __launch_bounds__(kDirThreads) ws_conv_direct_kernel(int Bt, int
         acc[u][c] += bias[c];
         if (relu) acc[u][c] = fmaxf(acc[u][c], 0.f);
       }
-      const size_t o = ((size_t)(b * H + y) * W + x0 + u) * COUT;
+      const size_t o = ((size_t)(b * H + y) * W + x0 + 32 * u) * COUT;
       if (out32) {
         if constexpr (COUT % 4 == 0) {
 #pragma unroll
@@ -961,7 +963,7 @@ int launch_direct(int B, int H, int W, int Cin, const void* X, const void* Wt, c
   const bool v8 = Cin % 8 == 0 && ((uintptr_t)X & 15u) == 0;
   // pixels per thread: more for narrow outputs (fewer accumulators)
   constexpr int PXW = COUT <= 4 ? 4 : 2;
-  if (W % PXW == 0) {
+  if (W % (32 * PXW) == 0) {
     if (v8) direct_grid<COUT, 8, PXW>(B, H, W, Cin, X, Wt, bias, relu, skip, out, out32, smem, st);
     else direct_grid<COUT, 2, PXW>(B, H, W, Cin, X, Wt, bias, relu, skip, out, out32, smem, st);
   } else {
