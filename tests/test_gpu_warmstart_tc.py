@@ -206,7 +206,8 @@ def test_crop_and_upsample_match_numpy():
     np.testing.assert_allclose(O.cpu().numpy(), ref, rtol=1e-5, atol=1e-6)
 
 
-def test_downsampled_start_sees_the_object():
+@pytest.mark.parametrize("cover,graph", [(True, True), (False, False)])
+def test_downsampled_start_sees_the_object(cover, graph):
     """The warm start for 256^2 frames through a 128^2 network (untrained, so
     only the geometry is checked): the stitched, upsampled object has the full
     grid's shape and is finite; where frames overlap it is non-zero, and
@@ -225,7 +226,8 @@ def test_downsampled_start_sees_the_object():
     Pd = torch.from_numpy(P.astype(np.complex64)).to(dev())
     I = torch.empty((len(R), N, N), dtype=torch.float32, device=dev())
     _native.check(_native.load().pty_intensities(plan.h, p(Od), p(Pd), p(I), stream()))
-    st = ws.DownsampledStart(net, len(R), N, N, P, R)
+    st = ws.DownsampledStart(net, len(R), N, N, P, R, cover=cover, graph=graph)
+    assert (len(st.frames) < len(R)) == cover
     O = st.run(I, U, U)
     o = O.cpu().numpy()
     o2 = st.run(I, U, U).cpu().numpy()          # a graph replay gives the same object
