@@ -717,8 +717,9 @@ def train_warm_start(torch, dev, warm_steps=6000, warm_frames=50000):
             "loss_first_20": float(np.mean(losses[:20])), "loss_last_20": float(np.mean(losses[-20:])),
             "input": "back-projection ifftn(sqrt(I) exp(i angle fftn P)) conj(P), (Re, Im)",
             "target": "object phase under the probe (cos, sin), weights |P|^2",
-            "kernels": "inference: tcgen05 implicit-GEMM convolutions (layers 1-4), direct CUDA-core "
-                       "convolutions (layers 0, 5); training: im2col + mma.sync GEMMs"}
+            "kernels": "inference and the training forward pass: tcgen05 implicit-GEMM convolutions "
+                       "(layers 1-4), direct CUDA-core convolutions (layers 0, 5); training backward: "
+                       "im2col + mma.sync GEMMs"}
     return net, info
 
 
