@@ -227,7 +227,9 @@ int pty_legacy_random_jump(const uint32_t* key, int64_t words, uint32_t* window_
  *     w[P] summing to 1: dY = 2 w (Y - T); loss_parts[256] partial sums.
  *   pty_ws_adam: one Adam step (Kingma and Ba) on float weights w with
  *     moments m, v (step counts from 1); wb (optional) gets a bf16 copy.
- *   pty_ws_to_bf16, pty_ws_add: element-wise conversion and sum. */
+ *   pty_ws_to_bf16, pty_ws_add: element-wise conversion and sum;
+ *   pty_ws_flip_weights: Wf[ci][t C_out + co] = W[co][(8 - t) C_in + ci] (bf16),
+ *     the weights of the input-gradient convolution dX = conv3x3(dZ, Wf). */
 int pty_ws_gemm(int32_t M, int32_t N, int32_t K, const void* A, int64_t sam, int64_t sak,
                 const void* B, int64_t sbk, int64_t sbn, float* C, int64_t scm, int64_t scn,
                 int32_t splits, float* partial, void* stream);
@@ -248,6 +250,7 @@ int pty_ws_adam(int64_t n, float* w, void* wb, const float* g, float* m, float* 
                 float b1, float b2, float eps, int32_t step, void* stream);
 int pty_ws_to_bf16(int64_t n, const float* x, void* y, void* stream);
 int pty_ws_add(int64_t n, const float* a, const float* b, float* out, void* stream);
+int pty_ws_flip_weights(int32_t Cin, int32_t Cout, const void* W, void* Wf, void* stream);
 /* Data for the network, nf frames of npix pixels:
  *   pty_ws_prep_bp: the network's input from back-projected exit waves bp
  *     (complex64 [nf][N0][N1]) under the probe P (complex64 [N0][N1]):
@@ -306,6 +309,11 @@ int pty_ws_upsample_object(int32_t Uh, int32_t Vh, const void* Oh, int32_t U, in
 int pty_ws_conv3x3_tc(int32_t B, int32_t H, int32_t W, int32_t Cin, int32_t Cout, const void* X,
                       const void* Wt, const float* bias, int32_t relu, const void* skip, void* out,
                       void* act, void* stream);
+/* The same convolution without bias, activation or skip, FP32 output out32
+ * [B][H][W][C_out] (16-byte aligned): a training pass's input gradient,
+ * conv3x3(dZ, Wf) with Wf from pty_ws_flip_weights.  Same shape rules. */
+int pty_ws_conv3x3_tc_f32(int32_t B, int32_t H, int32_t W, int32_t Cin, int32_t Cout, const void* X,
+                          const void* Wt, float* out32, void* stream);
 
 /* 1 if the frame shape N0 x N1 has a fused FFT kernel. */
 int pty_shape_supported(int32_t N0, int32_t N1);

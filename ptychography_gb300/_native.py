@@ -86,12 +86,15 @@ SIGNATURES = {
                     ctypes.c_float, ctypes.c_float, ctypes.c_float, c_int32, c_void_p],
     "pty_ws_to_bf16": [c_int64, c_void_p, c_void_p, c_void_p],
     "pty_ws_add": [c_int64, c_void_p, c_void_p, c_void_p, c_void_p],
+    "pty_ws_flip_weights": [c_int32, c_int32, c_void_p, c_void_p, c_void_p],
     "pty_ws_prep_bp": [c_int32, c_int32, c_int32, c_void_p, c_void_p, c_int32, c_void_p, c_void_p],
     "pty_ws_targets": [c_int32, c_int64, c_void_p, c_void_p, c_int32, ctypes.c_float, c_void_p, c_void_p,
                        c_void_p],
     "pty_ws_exits": [c_int32, c_int64, c_void_p, c_void_p, c_int32, c_void_p, c_void_p],
     "pty_ws_conv3x3_tc": [c_int32, c_int32, c_int32, c_int32, c_int32, c_void_p, c_void_p, c_void_p,
                           c_int32, c_void_p, c_void_p, c_void_p, c_void_p],
+    "pty_ws_conv3x3_tc_f32": [c_int32, c_int32, c_int32, c_int32, c_int32, c_void_p, c_void_p, c_void_p,
+                              c_void_p],
     "pty_timeout_status": [ctypes.POINTER(c_int32)],
     "pty_ws_conv3x3_direct": [c_int32, c_int32, c_int32, c_int32, c_int32, c_void_p, c_void_p, c_void_p,
                               c_int32, c_void_p, c_void_p, c_void_p, c_void_p],

@@ -464,6 +464,19 @@ __global__ void ws_add_kernel(long long n, const float* __restrict__ a, const fl
   WS_LOOP(i, n) out[i] = a[i] + b[i];
 }
 
+// The input-gradient convolution's weights: Wf[ci][t C_out + co] = W[co][(8 - t) C_in + ci],
+// the forward weights with C_in and C_out exchanged and the 3 x 3 taps turned
+// by 180 degrees, so that dX = conv3x3(dZ, Wf) in the forward layout
+__global__ void ws_flip_weights_kernel(int cin, int cout, const __nv_bfloat16* __restrict__ w,
+                                       __nv_bfloat16* __restrict__ wf) {
+  const long long n = 9LL * cin * cout;
+  WS_LOOP(i, n) {
+    const int ci = (int)(i / (9 * cout)), r = (int)(i % (9 * cout));
+    const int t = r / cout, co = r % cout;
+    wf[i] = w[(size_t)co * 9 * cin + (size_t)(8 - t) * cin + ci];
+  }
+}
+
 inline unsigned grid_for(long long n) {
   long long g = (n + 255) / 256;
   if (g > 8 * 152) g = 8 * 152;
@@ -646,6 +659,13 @@ extern "C" int pty_ws_to_bf16(int64_t n, const float* x, void* y, void* stream) 
   if (n < 1 || !x || !y) return set_error(PTY_ERR_ARG, "bad conversion arguments");
   ws_to_bf16_kernel<<<grid_for(n), 256, 0, (cudaStream_t)stream>>>(n, x, (bf16*)y);
   return ws_launched("ws_to_bf16_kernel");
+}
+
+extern "C" int pty_ws_flip_weights(int32_t Cin, int32_t Cout, const void* W, void* Wf, void* stream) {
+  if (Cin < 1 || Cout < 1 || !W || !Wf) return set_error(PTY_ERR_ARG, "bad weight-flip arguments");
+  ws_flip_weights_kernel<<<grid_for(9LL * Cin * Cout), 256, 0, (cudaStream_t)stream>>>(Cin, Cout, (const bf16*)W,
+                                                                                      (bf16*)Wf);
+  return ws_launched("ws_flip_weights_kernel");
 }
 
 extern "C" int pty_ws_add(int64_t n, const float* a, const float* b, float* out, void* stream) {

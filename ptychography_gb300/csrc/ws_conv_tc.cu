@@ -63,6 +63,7 @@ struct ConvParams {
   const __nv_bfloat16* skip;   // [P][Cout] or nullptr
   __nv_bfloat16* out;          // [P][Cout]
   __nv_bfloat16* act;          // [P][Cout] the activation before the skip, or nullptr
+  float* out32;                // [P][Cout] raw FP32 sums instead of out (no bias, activation, skip)
   int* err;                    // device error flag (set on a wait timeout)
 };
 
@@ -224,7 +225,7 @@ __global__ void __launch_bounds__(kThreads, 1)
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int swz = p.chunk_ch * 2;                         // 128 or 64 bytes per row
 
-  for (int i = threadIdx.x; i < p.Cout; i += kThreads) ctl->bias[i] = p.bias[i];
+  for (int i = threadIdx.x; i < p.Cout; i += kThreads) ctl->bias[i] = p.bias ? p.bias[i] : 0.f;
   if (threadIdx.x == 0) {
     for (int s = 0; s < kStages; ++s) {
       mbar_init(&ctl->full[s], 1);
@@ -339,6 +340,13 @@ __global__ void __launch_bounds__(kThreads, 1)
           __syncwarp();
           if (lane == 0) mbar_arrive(&ctl->acc_empty[buf]);
         }
+        if (p.out32) {
+          float* o32 = p.out32 + pix * p.Cout + c0;
+#pragma unroll
+          for (int q4 = 0; q4 < 8; ++q4)
+            *reinterpret_cast<float4*>(o32 + 4 * q4) = make_float4(v[4 * q4], v[4 * q4 + 1], v[4 * q4 + 2], v[4 * q4 + 3]);
+          continue;
+        }
         const __nv_bfloat16* sk = p.skip ? p.skip + pix * p.Cout + c0 : nullptr;
         __nv_bfloat16* o = p.out + pix * p.Cout + c0;
         __nv_bfloat16* ao = p.act ? p.act + pix * p.Cout + c0 : nullptr;
@@ -403,10 +411,26 @@ static size_t conv_tc_smem(int Cin, int Cout) {
 
 using namespace pty;
 
+static int conv_tc(int32_t B, int32_t H, int32_t W, int32_t Cin, int32_t Cout, const void* X, const void* Wt,
+                   const float* bias, int32_t relu, const void* skip, void* out, void* act, float* out32,
+                   void* stream);
+
 extern "C" int pty_ws_conv3x3_tc(int32_t B, int32_t H, int32_t W, int32_t Cin, int32_t Cout,
                                  const void* X, const void* Wt, const float* bias, int32_t relu,
                                  const void* skip, void* out, void* act, void* stream) {
   if (!X || !Wt || !bias || !out) return set_error(PTY_ERR_ARG, "pty_ws_conv3x3_tc: null argument");
+  return conv_tc(B, H, W, Cin, Cout, X, Wt, bias, relu, skip, out, act, nullptr, stream);
+}
+
+extern "C" int pty_ws_conv3x3_tc_f32(int32_t B, int32_t H, int32_t W, int32_t Cin, int32_t Cout, const void* X,
+                                     const void* Wt, float* out32, void* stream) {
+  if (!X || !Wt || !out32) return set_error(PTY_ERR_ARG, "pty_ws_conv3x3_tc_f32: null argument");
+  return conv_tc(B, H, W, Cin, Cout, X, Wt, nullptr, 0, nullptr, nullptr, nullptr, out32, stream);
+}
+
+static int conv_tc(int32_t B, int32_t H, int32_t W, int32_t Cin, int32_t Cout, const void* X, const void* Wt,
+                   const float* bias, int32_t relu, const void* skip, void* out, void* act, float* out32,
+                   void* stream) {
   if (B < 1 || H < 1 || W < 1) return set_error(PTY_ERR_ARG, "pty_ws_conv3x3_tc: empty input");
   if (!(Cin == 32 || Cin % 64 == 0) || Cin > 1024)
     return set_error(PTY_ERR_UNSUPPORTED, "pty_ws_conv3x3_tc: C_in must be 32 or a multiple of 64");
@@ -416,7 +440,7 @@ extern "C" int pty_ws_conv3x3_tc(int32_t B, int32_t H, int32_t W, int32_t Cin, i
     return set_error(PTY_ERR_UNSUPPORTED,
                      "pty_ws_conv3x3_tc: 128-pixel tiles need W dividing 128 (and H a multiple of 128 / W) "
                      "or W a multiple of 128");
-  const void* arrays[5] = {X, Wt, out, skip, act};
+  const void* arrays[6] = {X, Wt, out, skip, act, out32};
   for (const void* q : arrays)
     if (q && (reinterpret_cast<uintptr_t>(q) & 15))
       return set_error(PTY_ERR_ARG, "pty_ws_conv3x3_tc: arrays must be 16-byte aligned");
@@ -438,6 +462,7 @@ extern "C" int pty_ws_conv3x3_tc(int32_t B, int32_t H, int32_t W, int32_t Cin, i
   p.skip = static_cast<const __nv_bfloat16*>(skip);
   p.out = static_cast<__nv_bfloat16*>(out);
   p.act = static_cast<__nv_bfloat16*>(act);
+  p.out32 = out32;
   p.err = err;
   const CUtensorMapSwizzle swz = p.chunk_ch == 64 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_64B;
 

@@ -74,6 +74,7 @@ class WarmStartNet:
         self.step_count = 0
         self._sync_bf16()
         self._bufs = {}
+        self._zero_bias = torch.zeros(128, dtype=torch.float32, device=self.dev)
 
     def _sp(self):
         torch = _torch()
@@ -180,7 +181,9 @@ class WarmStartNet:
         """The forward pass of a training step on the tensor cores: layers 1-4
         on pty_ws_conv3x3_tc (keeping each layer's activation for the
         backward pass), the 2-channel layers on the direct convolution;
-        backward() then forms the im2col buffers its weight gradients need.
+        backward() then forms the im2col buffers its weight gradients need
+        and computes the input gradients on the same convolutions (flipped
+        weights, FP32 output).
         Falls back to forward() (im2col + mma.sync) where the frame size does
         not fit the tensor-core tiles.  x: (B, H, W, 2) bf16; returns y."""
         torch = _torch()
@@ -272,6 +275,19 @@ class WarmStartNet:
                                       _p(self.gw[i]), K, 1, splits, _p(part), sp))
         if not need_dx:
             return None
+        if getattr(self, "_fwd_inputs", None) is not None:
+            # input gradient as a convolution of dZ with the flipped weights:
+            # the tensor-core kernel for layers 1-4, the direct one for the
+            # 2-channel layer 5; no dcol buffer, no col2im
+            wf = self._buf("wf%d" % i, (cin, 9 * cout), torch.bfloat16)
+            _native.check(lib.pty_ws_flip_weights(cin, cout, _p(self.wb[i]), _p(wf), sp))
+            dX = self._buf("dx%d" % i, (B, H, W, cin), torch.float32)
+            if cout < 32:
+                _native.check(lib.pty_ws_conv3x3_direct(B, H, W, cout, cin, _p(dZ), _p(wf), _p(self._zero_bias),
+                                                        0, None, None, _p(dX), sp))
+            else:
+                _native.check(lib.pty_ws_conv3x3_tc_f32(B, H, W, cout, cin, _p(dZ), _p(wf), _p(dX), sp))
+            return dX
         dcol = self._buf("dcol", (P, K), torch.float32)
         _native.check(lib.pty_ws_gemm(P, K, cout, _p(dZ), cout, 1, _p(self.wb[i]), K, 1,
                                       _p(dcol), K, 1, 1, None, sp))

@@ -104,6 +104,53 @@ def test_conv_tc_matches_fp64_and_im2col_path(case):
     assert np.all(d <= 2 ** -6 * np.maximum(np.abs(old), np.abs(got)) + 1e-6)
 
 
+def dgrad_ref(dz, w):
+    """float64 input gradient of the 3 x 3 convolution: dX[b, y, x, ci] =
+    sum_{ky, kx, co} dZ[b, y - ky + 1, x - kx + 1, co] w[co][(ky*3+kx) C_in + ci]."""
+    B, H, W, co = dz.shape
+    cin = w.shape[1] // 9
+    dzp = np.zeros((B, H + 2, W + 2, co))
+    dzp[:, 1:-1, 1:-1] = dz
+    wk = w.reshape(co, 3, 3, cin)
+    dx = np.zeros((B, H, W, cin))
+    for ky in range(3):
+        for kx in range(3):
+            dx += np.einsum("bhwo,oc->bhwc", dzp[:, 2 - ky:2 - ky + H, 2 - kx:2 - kx + W], wk[:, ky, kx])
+    return dx
+
+
+# (B, H, W, C_in, C_out) of the forward layer whose input gradient is taken:
+# the network's layers 1-5 at 128^2 frames (layer 5, C_out 2, on the direct kernel)
+DGRAD_CASES = [(2, 64, 64, 32, 64), (2, 32, 32, 64, 128), (2, 64, 64, 128, 64), (2, 128, 128, 64, 32),
+               (2, 128, 128, 32, 2)]
+
+
+@pytest.mark.parametrize("case", DGRAD_CASES, ids=lambda c: "x".join(map(str, c)))
+def test_input_gradient_convolution_matches_fp64(case):
+    """dX = conv3x3(dZ, Wf), Wf from pty_ws_flip_weights, on the tensor-core
+    kernel's FP32 output mode (the direct kernel for a 2-channel dZ), against
+    the float64 adjoint of the forward convolution on the same BF16 operands:
+    the products are exact in FP32, so within 1e-5 norm-wise."""
+    B, H, W, cin, cout = case
+    lib = _native.load()
+    rng = np.random.default_rng(B + H + cin + cout)
+    dz = bf16(rng.standard_normal((B, H, W, cout)))
+    wd = bf16(rng.standard_normal((cout, 9 * cin)) * np.sqrt(2.0 / (9 * cin)))
+    wf = torch.empty((cin, 9 * cout), dtype=torch.bfloat16, device=dev())
+    _native.check(lib.pty_ws_flip_weights(cin, cout, p(wd), p(wf), stream()))
+    dx = torch.empty((B, H, W, cin), dtype=torch.float32, device=dev())
+    if cout < 32:
+        zb = torch.zeros(cin, dtype=torch.float32, device=dev())
+        _native.check(lib.pty_ws_conv3x3_direct(B, H, W, cout, cin, p(dz), p(wf), p(zb), 0, None, None, p(dx),
+                                                stream()))
+    else:
+        _native.check(lib.pty_ws_conv3x3_tc_f32(B, H, W, cout, cin, p(dz), p(wf), p(dx), stream()))
+    assert status_ok()
+    ref = dgrad_ref(dz.float().cpu().numpy().astype(np.float64), wd.float().cpu().numpy().astype(np.float64))
+    got = dx.cpu().numpy().astype(np.float64)
+    assert np.linalg.norm(got - ref) / np.linalg.norm(ref) < 1e-5
+
+
 def test_conv_tc_rejects_unsupported_shapes():
     lib = _native.load()
     t = torch.zeros(1 << 16, dtype=torch.bfloat16, device=dev())
@@ -245,7 +292,8 @@ def test_training_forward_on_tensor_cores_gives_the_same_gradients():
     activations, the backward pass forming its own im2col buffers) gives the
     weight and bias gradients of the im2col + mma.sync forward pass, up to
     the FP32 summation order of the forward sums (one BF16 rounding step on
-    some activations): within 3e-2 norm-wise per layer."""
+    some activations) and of the input gradients (flipped-weight
+    convolutions instead of GEMM + col2im): within 3e-2 norm-wise per layer."""
     net = WarmStartNet(128, 128, seed=4, device=dev())
     rng = np.random.default_rng(9)
     B = 8
