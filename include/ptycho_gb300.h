@@ -314,6 +314,24 @@ int pty_ws_conv3x3_tc(int32_t B, int32_t H, int32_t W, int32_t Cin, int32_t Cout
  * conv3x3(dZ, Wf) with Wf from pty_ws_flip_weights.  Same shape rules. */
 int pty_ws_conv3x3_tc_f32(int32_t B, int32_t H, int32_t W, int32_t Cin, int32_t Cout, const void* X,
                           const void* Wt, float* out32, void* stream);
+/* The weight gradient of that convolution on the tensor cores:
+ *   dW[co][tap C_in + ci] = sum_p dZ[p][co] X[p shifted by tap][ci]
+ * (dW float [C_out][9 C_in], the im2col path's layout), from XS, the layer
+ * input in three x-shifted channel-major copies, and dZT, the gradient at the
+ * pre-activation sums channel-major, both made by pty_ws_shift_transpose:
+ *   pty_ws_shift_transpose: XS[s][c][p] = X[p shifted by s - 1 along x][c]
+ *     (zero past the row ends) for S = 3; XS[0][c][p] = X[p][c] for S = 1;
+ *     X bf16 [P][C] (P = B H W, W even, C <= 256), XS bf16 [S][C][P];
+ *   pty_ws_wgrad_tc: XS [3][C_in][P], dZT [C_out][P], C_in 32, 64 or 128,
+ *     C_out 1..128, W 32 or a multiple of 64; scratch of at least
+ *     pty_ws_wgrad_tc_scratch(...) floats (-1: shape unsupported) holds the
+ *     per-split partial sums, added in split order (deterministic); arrays
+ *     16-byte aligned.  Its mbarrier waits are bounded (pty_timeout_status). */
+int pty_ws_shift_transpose(int32_t B, int32_t H, int32_t W, int32_t C, int32_t S, const void* X, void* XS,
+                           void* stream);
+int64_t pty_ws_wgrad_tc_scratch(int32_t B, int32_t H, int32_t W, int32_t Cin, int32_t Cout);
+int pty_ws_wgrad_tc(int32_t B, int32_t H, int32_t W, int32_t Cin, int32_t Cout, const void* XS,
+                    const void* dZT, float* dW, float* scratch, int64_t scratch_floats, void* stream);
 
 /* 1 if the frame shape N0 x N1 has a fused FFT kernel. */
 int pty_shape_supported(int32_t N0, int32_t N1);

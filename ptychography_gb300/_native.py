@@ -95,6 +95,10 @@ SIGNATURES = {
                           c_int32, c_void_p, c_void_p, c_void_p, c_void_p],
     "pty_ws_conv3x3_tc_f32": [c_int32, c_int32, c_int32, c_int32, c_int32, c_void_p, c_void_p, c_void_p,
                               c_void_p],
+    "pty_ws_shift_transpose": [c_int32, c_int32, c_int32, c_int32, c_int32, c_void_p, c_void_p, c_void_p],
+    "pty_ws_wgrad_tc_scratch": [c_int32, c_int32, c_int32, c_int32, c_int32],
+    "pty_ws_wgrad_tc": [c_int32, c_int32, c_int32, c_int32, c_int32, c_void_p, c_void_p, c_void_p, c_void_p,
+                        c_int64, c_void_p],
     "pty_timeout_status": [ctypes.POINTER(c_int32)],
     "pty_ws_conv3x3_direct": [c_int32, c_int32, c_int32, c_int32, c_int32, c_void_p, c_void_p, c_void_p,
                               c_int32, c_void_p, c_void_p, c_void_p, c_void_p],
@@ -112,7 +116,7 @@ SIGNATURES = {
 }
 _RESTYPES = {"pty_last_error": ctypes.c_char_p, "pty_launch_count": ctypes.c_int64,
              "pty_legacy_random_scratch_words": ctypes.c_int64,
-             "pty_ws_act_bwd_scratch": ctypes.c_int64}
+             "pty_ws_act_bwd_scratch": ctypes.c_int64, "pty_ws_wgrad_tc_scratch": ctypes.c_int64}
 
 
 class PtyError(RuntimeError):

@@ -390,6 +390,249 @@ __global__ void __launch_bounds__(kThreads, 1)
   }
 }
 
+
+// ---------------------------------------------------------------- weight gradient
+//
+//   dW[co][tap C_in + ci] = sum_p dZ[p][co] X[p shifted by tap][ci]
+//
+// as a GEMM with the pixels on K: D[k][co] with k = tap C_in + ci on the MMA's
+// M (128 rows: 128 / C_in taps per M tile) and co on N.  Both operands are
+// K-major, i.e. pixel-contiguous: XS[s][ci][p] = X[p shifted by s - 1 along
+// x][ci] (three copies, so that the TMA's innermost coordinate, a pixel
+// column, never carries the +-1 tap offset: it stays a multiple of the
+// chunk) and dZT[co][p].  A stage is one chunk of 64 pixels of an image row
+// (32 when W = 32): per tap of the M tile one box (chunk, 1 row, 1 image,
+// C_in channels, 1 copy) at row y + ky - 1 of copy kx (rows outside the
+// image read the zero fill), and one box (chunk, N) of dZT (rows past C_out
+// read zeros, so C_out < 16 runs as N = 16).  Work items are (M tile, pixel
+// range) pairs; each accumulates its range in tensor memory and writes an
+// FP32 partial [split][k][co]; ws_wgrad_reduce_kernel sums the splits in
+// order (deterministic).
+struct WgradParams {
+  int B, H, W, Cin, Cout, npad;  // npad: B-operand rows (C_out rounded up to 16)
+  int kchunk;                    // pixels per stage
+  int xtiles;                    // W / kchunk
+  int tpt, mtiles;               // taps per M tile, M tiles
+  int nchunks, cps, splits;      // pixel chunks, chunks per split, splits
+  int items;                     // mtiles * splits
+  int kpad;                      // mtiles * 128
+  float* partial;                // [splits][kpad][Cout]
+  int* err;
+};
+
+__device__ __forceinline__ void tma_load_5d(void* dst, const CUtensorMap* map, uint64_t* bar, int c0,
+                                            int c1, int c2, int c3, int c4) {
+  asm volatile(
+      "cp.async.bulk.tensor.5d.shared::cluster.global.tile.mbarrier::complete_tx::bytes "
+      "[%0], [%1, {%3, %4, %5, %6, %7}], [%2];" ::"r"(smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(smem_u32(bar)), "r"(c0), "r"(c1), "r"(c2), "r"(c3),
+      "r"(c4)
+      : "memory");
+}
+
+__global__ void __launch_bounds__(kThreads, 1)
+    ws_wgrad_tc_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constant__ CUtensorMap tmD,
+                       const WgradParams p) {
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  const uint32_t raw = smem_u32(smem_raw);
+  unsigned char* base = smem_raw + ((1024 - (raw & 1023)) & 1023);
+  const int row_bytes = p.kchunk * 2;                     // 128 or 64: the swizzle span
+  const int a_bytes = kTileM * row_bytes;
+  const int b_bytes = p.npad * row_bytes;
+  const int stage_bytes = ((a_bytes + b_bytes + 1023) / 1024) * 1024;
+  SmemCtl* ctl = reinterpret_cast<SmemCtl*>(base + kStages * stage_bytes);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < kStages; ++s) {
+      mbar_init(&ctl->full[s], 1);
+      mbar_init(&ctl->empty[s], 1);
+    }
+    for (int i = 0; i < 2; ++i) {
+      mbar_init(&ctl->acc_full[i], 1);
+      mbar_init(&ctl->acc_empty[i], 4);
+    }
+    mbar_init(&ctl->drain, 1);
+    ctl->abort = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(&ctl->tmem_base)),
+                 "r"(kAccCols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = ctl->tmem_base;
+  volatile int* abort = &ctl->abort;
+  const int ksteps = p.kchunk / 16;
+  const uint32_t idesc = instr_desc(kTileM, p.npad);
+  const uint32_t acc_stride = 128u;
+
+  if (warp == 4) {
+    // ------------------------------------------------ TMA producer
+    if (lane == 0) {
+      int q = 0;
+      bool ok = true;
+      for (int t = blockIdx.x; t < p.items && ok; t += gridDim.x) {
+        const int mt = t % p.mtiles, sp = t / p.mtiles;
+        const int c0 = sp * p.cps, c1 = min(c0 + p.cps, p.nchunks);
+        const int tap0 = mt * p.tpt, ntap = min(p.tpt, 9 - tap0);
+        const unsigned tx = (unsigned)(ntap * p.Cin * row_bytes + b_bytes);
+        for (int c = c0; c < c1 && ok; ++c, ++q) {
+          const int s = q % kStages, ph = (q / kStages) & 1;
+          if (!mbar_wait(&ctl->empty[s], ph ^ 1, abort, p.err)) { ok = false; break; }
+          const int xt = c % p.xtiles, row = c / p.xtiles;
+          const int y = row % p.H, b = row / p.H, x0 = xt * p.kchunk;
+          unsigned char* sa = base + s * stage_bytes;
+          unsigned char* sb = sa + a_bytes;
+          mbar_expect_tx(&ctl->full[s], tx);
+          for (int j = 0; j < ntap; ++j) {
+            const int tap = tap0 + j, ky = tap / 3, kx = tap % 3;
+            tma_load_5d(sa + j * p.Cin * row_bytes, &tmX, &ctl->full[s], x0, y + ky - 1, b, 0, kx);
+          }
+          tma_load_2d(sb, &tmD, &ctl->full[s], c * p.kchunk, 0);
+        }
+      }
+      if (!ok) {
+        for (int k = 0; k < kStages; ++k) {
+          const int qq = q - 1 - k;
+          if (qq < 0) break;
+          const int s = qq % kStages, ph = (qq / kStages) & 1;
+          for (unsigned i = 0; i < kSpinLimit && !mbar_try_wait(&ctl->full[s], ph); ++i) {
+          }
+        }
+      }
+    }
+  } else if (warp == 5) {
+    // ------------------------------------------------ MMA issuer
+    if (lane == 0) {
+      int q = 0, local = 0;
+      bool ok = true;
+      for (int t = blockIdx.x; t < p.items && ok; t += gridDim.x, ++local) {
+        const int sp = t / p.mtiles;
+        const int c0 = sp * p.cps, c1 = min(c0 + p.cps, p.nchunks);
+        const int buf = local & 1, use = local >> 1;
+        if (!mbar_wait(&ctl->acc_empty[buf], (use & 1) ^ 1, abort, p.err)) { ok = false; break; }
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const uint32_t d = tmem + buf * acc_stride;
+        for (int c = c0; c < c1; ++c, ++q) {
+          const int s = q % kStages, ph = (q / kStages) & 1;
+          if (!mbar_wait(&ctl->full[s], ph, abort, p.err)) { ok = false; break; }
+          asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+          const uint32_t sa = smem_u32(base + s * stage_bytes);
+          const uint32_t sb = sa + a_bytes;
+          for (int k = 0; k < ksteps; ++k)
+            mma_bf16(d, smem_desc(sa + 32 * k, row_bytes), smem_desc(sb + 32 * k, row_bytes), idesc,
+                     (c > c0 || k > 0) ? 1u : 0u);
+          mma_commit(&ctl->empty[s]);
+        }
+        if (!ok) break;
+        mma_commit(&ctl->acc_full[buf]);
+      }
+      mma_commit(&ctl->drain);
+      for (unsigned i = 0; i < kSpinLimit && !mbar_try_wait(&ctl->drain, 0); ++i) {
+      }
+    }
+  } else {
+    // ------------------------------------------------ epilogue (warps 0-3)
+    int local = 0;
+    const int nvalid = 9 * p.Cin;
+    for (int t = blockIdx.x; t < p.items; t += gridDim.x, ++local) {
+      const int buf = local & 1, use = local >> 1;
+      if (!mbar_wait_warp(&ctl->acc_full[buf], use & 1, abort, p.err)) break;
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const int mt = t % p.mtiles, sp = t / p.mtiles;
+      const int k = mt * kTileM + warp * 32 + lane;          // this lane's row: tap C_in + ci
+      float* dst = p.partial + ((size_t)sp * p.kpad + k) * p.Cout;
+      const uint32_t tbase = tmem + buf * acc_stride + ((uint32_t)(warp * 32) << 16);
+      for (int c0 = 0; c0 < p.npad; c0 += 32) {
+        float v[32];
+        tmem_ld32(tbase + c0, v);
+        if (c0 + 32 >= p.npad) {
+          asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+          __syncwarp();
+          if (lane == 0) mbar_arrive(&ctl->acc_empty[buf]);
+        }
+        if (k < nvalid) {
+          if (c0 + 32 <= p.Cout) {
+#pragma unroll
+            for (int q4 = 0; q4 < 8; ++q4)
+              *reinterpret_cast<float4*>(dst + c0 + 4 * q4) =
+                  make_float4(v[4 * q4], v[4 * q4 + 1], v[4 * q4 + 2], v[4 * q4 + 3]);
+          } else {
+#pragma unroll
+            for (int e = 0; e < 32; ++e)
+              if (c0 + e < p.Cout) dst[c0 + e] = v[e];
+          }
+        }
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0) {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kAccCols)
+                 : "memory");
+  }
+}
+
+// dW[co][k] = sum over s < splits of partial[s][k][co], in split order
+__global__ void ws_wgrad_reduce_kernel(int splits, int kpad, int K9, int Cout, const float* __restrict__ part,
+                                       float* __restrict__ dW) {
+  const long long n = (long long)Cout * K9;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const int co = (int)(i / K9), k = (int)(i % K9);
+    float s = 0.f;
+    for (int sp = 0; sp < splits; ++sp) s += part[((size_t)sp * kpad + k) * Cout + co];
+    dW[i] = s;
+  }
+}
+
+// XS[s][c][p] = X[p shifted by s - 1 along x][c] (zero past either end of the
+// image row) for s < 3 when S = 3; XS[0][c][p] = X[p][c] when S = 1.  X is
+// [P][C] bf16 (P = B H W pixels); one block per 64 pixels, staged through
+// shared memory with a one-pixel halo so both sides are coalesced.
+constexpr int kTrPix = 64;
+__global__ void __launch_bounds__(256) ws_shift_transpose_kernel(long long P, int W, int C, int S,
+                                                                 const __nv_bfloat16* __restrict__ X,
+                                                                 __nv_bfloat16* __restrict__ XS) {
+  extern __shared__ __nv_bfloat16 tr_s[];          // [kTrPix + 2][C + 2]
+  const int pitch = C + 2;
+  const long long p0 = (long long)blockIdx.x * kTrPix;
+  const int n = (kTrPix + 2) * C;
+  for (int e = threadIdx.x; e < n; e += blockDim.x) {
+    const int i = e / C, c = e % C;
+    const long long pp = p0 - 1 + i;
+    tr_s[i * pitch + c] = (pp >= 0 && pp < P) ? X[pp * C + c] : __float2bfloat16(0.f);
+  }
+  __syncthreads();
+  const int i2 = threadIdx.x & 31, r = threadIdx.x >> 5;
+  const long long p = p0 + 2 * i2;
+  if (p >= P) return;
+  const bool two = p + 1 < P;
+  const int x = (int)(p % W);                      // W even: p and p + 1 share a row
+  for (int sc = r; sc < S * C; sc += 8) {
+    const int s = sc / C, c = sc % C;
+    const int sh = S == 3 ? s - 1 : 0;
+    const int xa = x + sh, xb = x + 1 + sh;
+    const __nv_bfloat16 z = __float2bfloat16(0.f);
+    const __nv_bfloat16 va = (xa >= 0 && xa < W) ? tr_s[(2 * i2 + 1 + sh) * pitch + c] : z;
+    const __nv_bfloat16 vb = (xb >= 0 && xb < W) ? tr_s[(2 * i2 + 2 + sh) * pitch + c] : z;
+    __nv_bfloat16* o = XS + ((size_t)s * C + c) * P + p;
+    if (two) {
+      *reinterpret_cast<__nv_bfloat162*>(o) = __halves2bfloat162(va, vb);
+    } else {
+      o[0] = va;
+    }
+  }
+}
+
 int sm_count() {
   int dev = 0, n = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return 1;
@@ -500,4 +743,136 @@ static int conv_tc(int32_t B, int32_t H, int32_t W, int32_t Cin, int32_t Cout, c
   const int grid = p.tiles < sm_count() ? p.tiles : sm_count();
   ws_conv_tc_kernel<<<grid, kThreads, smem, (cudaStream_t)stream>>>(tmX, tmW, p);
   return check_launch("ws_conv_tc_kernel");
+}
+
+
+// ------------------------------------------------------------ weight gradient: host side
+namespace pty {
+namespace {
+
+struct WgradShape {
+  int kchunk, npad, tpt, mtiles, nchunks, cps, splits, kpad;
+};
+
+int wgrad_shape(int B, int H, int W, int Cin, int Cout, WgradShape& w) {
+  if (B < 1 || H < 1 || W < 1) return set_error(PTY_ERR_ARG, "pty_ws_wgrad_tc: empty input");
+  if (!(Cin == 32 || Cin == 64 || Cin == 128))
+    return set_error(PTY_ERR_UNSUPPORTED, "pty_ws_wgrad_tc: C_in must be 32, 64 or 128");
+  if (Cout < 1 || Cout > kMaxCout) return set_error(PTY_ERR_UNSUPPORTED, "pty_ws_wgrad_tc: C_out must be 1..128");
+  if (!(W == 32 || W % 64 == 0))
+    return set_error(PTY_ERR_UNSUPPORTED, "pty_ws_wgrad_tc: W must be 32 or a multiple of 64");
+  const long long P = (long long)B * H * W;
+  if (P >= (1ll << 31)) return set_error(PTY_ERR_UNSUPPORTED, "pty_ws_wgrad_tc: too many pixels");
+  w.kchunk = W == 32 ? 32 : 64;
+  w.npad = Cout < 16 ? 16 : ((Cout + 15) / 16) * 16;
+  w.tpt = kTileM / Cin;
+  w.mtiles = (9 + w.tpt - 1) / w.tpt;
+  w.nchunks = (int)(P / w.kchunk);
+  // at most two items per SM, every split non-empty
+  const int want = 2 * sm_count() / w.mtiles > 0 ? 2 * sm_count() / w.mtiles : 1;
+  int splits = want < w.nchunks ? want : w.nchunks;
+  w.cps = (w.nchunks + splits - 1) / splits;
+  w.splits = (w.nchunks + w.cps - 1) / w.cps;
+  w.kpad = w.mtiles * kTileM;
+  return PTY_OK;
+}
+
+size_t wgrad_smem(const WgradShape& w) {
+  const size_t stage = (((size_t)kTileM * w.kchunk * 2 + (size_t)w.npad * w.kchunk * 2 + 1023) / 1024) * 1024;
+  const size_t need = kStages * stage + sizeof(SmemCtl) + 1024;
+  return need > kMinSmem ? need : kMinSmem;
+}
+
+}  // namespace
+}  // namespace pty
+
+extern "C" int64_t pty_ws_wgrad_tc_scratch(int32_t B, int32_t H, int32_t W, int32_t Cin, int32_t Cout) {
+  WgradShape w;
+  if (wgrad_shape(B, H, W, Cin, Cout, w) != PTY_OK) return -1;
+  return (int64_t)w.splits * w.kpad * Cout;
+}
+
+extern "C" int pty_ws_shift_transpose(int32_t B, int32_t H, int32_t W, int32_t C, int32_t S, const void* X,
+                                      void* XS, void* stream) {
+  if (B < 1 || H < 1 || W < 2 || (W & 1) || C < 1 || C > 256 || !(S == 1 || S == 3) || !X || !XS)
+    return set_error(PTY_ERR_ARG, "pty_ws_shift_transpose: bad arguments");
+  if ((reinterpret_cast<uintptr_t>(XS) & 3) != 0)
+    return set_error(PTY_ERR_ARG, "pty_ws_shift_transpose: XS must be 4-byte aligned");
+  const long long P = (long long)B * H * W;
+  const long long blocks = (P + kTrPix - 1) / kTrPix;
+  if (blocks >= (1ll << 31)) return set_error(PTY_ERR_UNSUPPORTED, "pty_ws_shift_transpose: too many pixels");
+  const size_t smem = (size_t)(kTrPix + 2) * (C + 2) * sizeof(__nv_bfloat16);
+  ws_shift_transpose_kernel<<<(unsigned)blocks, 256, smem, (cudaStream_t)stream>>>(
+      P, W, C, S, static_cast<const __nv_bfloat16*>(X), static_cast<__nv_bfloat16*>(XS));
+  return check_launch("ws_shift_transpose_kernel");
+}
+
+extern "C" int pty_ws_wgrad_tc(int32_t B, int32_t H, int32_t W, int32_t Cin, int32_t Cout, const void* XS,
+                               const void* dZT, float* dW, float* scratch, int64_t scratch_floats,
+                               void* stream) {
+  if (!XS || !dZT || !dW || !scratch) return set_error(PTY_ERR_ARG, "pty_ws_wgrad_tc: null argument");
+  WgradShape w;
+  PTY_TRY(wgrad_shape(B, H, W, Cin, Cout, w));
+  if (scratch_floats < (int64_t)w.splits * w.kpad * Cout)
+    return set_error(PTY_ERR_ARG, "pty_ws_wgrad_tc: scratch smaller than pty_ws_wgrad_tc_scratch");
+  const void* arrays[4] = {XS, dZT, dW, scratch};
+  for (const void* q : arrays)
+    if (reinterpret_cast<uintptr_t>(q) & 15)
+      return set_error(PTY_ERR_ARG, "pty_ws_wgrad_tc: arrays must be 16-byte aligned");
+  PFN_cuTensorMapEncodeTiled_v12000 encode;
+  PTY_TRY(tensor_map_encoder(&encode));
+  int* err = nullptr;
+  PTY_TRY(device_timeout_flag(&err));
+  const long long P = (long long)B * H * W;
+  const CUtensorMapSwizzle swz = w.kchunk == 64 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_64B;
+  CUtensorMap tmX, tmD;
+  {
+    // XS: dims (W, H, B, C_in, 3 copies), box (chunk, 1, 1, C_in, 1)
+    const cuuint64_t dims[5] = {(cuuint64_t)W, (cuuint64_t)H, (cuuint64_t)B, (cuuint64_t)Cin, 3};
+    const cuuint64_t strides[4] = {(cuuint64_t)W * 2, (cuuint64_t)H * W * 2, (cuuint64_t)P * 2,
+                                   (cuuint64_t)Cin * P * 2};
+    const cuuint32_t box[5] = {(cuuint32_t)w.kchunk, 1, 1, (cuuint32_t)Cin, 1};
+    const cuuint32_t estr[5] = {1, 1, 1, 1, 1};
+    CUresult r = encode(&tmX, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 5, const_cast<void*>(XS), dims, strides, box,
+                        estr, CU_TENSOR_MAP_INTERLEAVE_NONE, swz, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return set_error(PTY_ERR_CUDA, "pty_ws_wgrad_tc: input tensor map");
+  }
+  {
+    // dZT: dims (P, C_out), box (chunk, npad): rows past C_out read zeros
+    const cuuint64_t dims[2] = {(cuuint64_t)P, (cuuint64_t)Cout};
+    const cuuint64_t strides[1] = {(cuuint64_t)P * 2};
+    const cuuint32_t box[2] = {(cuuint32_t)w.kchunk, (cuuint32_t)w.npad};
+    const cuuint32_t estr[2] = {1, 1};
+    CUresult r = encode(&tmD, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(dZT), dims, strides, box,
+                        estr, CU_TENSOR_MAP_INTERLEAVE_NONE, swz, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return set_error(PTY_ERR_CUDA, "pty_ws_wgrad_tc: gradient tensor map");
+  }
+  WgradParams p{};
+  p.B = B; p.H = H; p.W = W; p.Cin = Cin; p.Cout = Cout; p.npad = w.npad;
+  p.kchunk = w.kchunk;
+  p.xtiles = W / w.kchunk;
+  p.tpt = w.tpt; p.mtiles = w.mtiles;
+  p.nchunks = w.nchunks; p.cps = w.cps; p.splits = w.splits;
+  p.items = w.mtiles * w.splits;
+  p.kpad = w.kpad;
+  p.partial = scratch;
+  p.err = err;
+  const size_t smem = wgrad_smem(w);
+  static std::once_flag attr_once;
+  static cudaError_t attr_err = cudaSuccess;
+  std::call_once(attr_once, [] {
+    WgradShape big{64, kMaxCout, 1, 9, 1, 1, 1, 9 * kTileM};
+    attr_err = cudaFuncSetAttribute(ws_wgrad_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)wgrad_smem(big));
+  });
+  if (attr_err != cudaSuccess) return set_cuda_error(attr_err, "pty_ws_wgrad_tc: smem attribute");
+  const int grid = p.items < sm_count() ? p.items : sm_count();
+  ws_wgrad_tc_kernel<<<grid, kThreads, smem, (cudaStream_t)stream>>>(tmX, tmD, p);
+  PTY_TRY(check_launch("ws_wgrad_tc_kernel"));
+  const long long n = (long long)Cout * 9 * Cin;
+  ws_wgrad_reduce_kernel<<<(unsigned)((n + 255) / 256), 256, 0, (cudaStream_t)stream>>>(w.splits, w.kpad, 9 * Cin,
+                                                                                       Cout, scratch, dW);
+  return check_launch("ws_wgrad_reduce_kernel");
 }

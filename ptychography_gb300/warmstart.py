@@ -181,9 +181,11 @@ class WarmStartNet:
         """The forward pass of a training step on the tensor cores: layers 1-4
         on pty_ws_conv3x3_tc (keeping each layer's activation for the
         backward pass), the 2-channel layers on the direct convolution;
-        backward() then forms the im2col buffers its weight gradients need
-        and computes the input gradients on the same convolutions (flipped
-        weights, FP32 output).
+        backward() then takes the weight gradients of layers 1-5 on the
+        tensor cores too (pty_ws_wgrad_tc, from channel-major copies of the
+        layer inputs; layer 0's 2-channel input through im2col + mma.sync)
+        and the input gradients on the same convolutions (flipped weights,
+        FP32 output).
         Falls back to forward() (im2col + mma.sync) where the frame size does
         not fit the tensor-core tiles.  x: (B, H, W, 2) bf16; returns y."""
         torch = _torch()
@@ -259,7 +261,9 @@ class WarmStartNet:
         lib, sp = self.lib, self._sp()
         P, K = B * H * W, 9 * cin
         a = self._bufs["a%d" % i] if relu else None
-        if getattr(self, "_fwd_inputs", None) is not None:
+        tc = getattr(self, "_fwd_inputs", None) is not None
+        wscr_n = int(lib.pty_ws_wgrad_tc_scratch(B, H, W, cin, cout)) if tc else -1
+        if tc and wscr_n < 0:
             # a tensor-core forward pass wrote no im2col buffer: form it now
             col = self._buf("col%d" % i, (P, K), torch.bfloat16)
             _native.check(lib.pty_ws_im2col(B, H, W, cin, _p(self._fwd_inputs[i]), _p(col), sp))
@@ -267,12 +271,25 @@ class WarmStartNet:
         scr = self._buf("actscr", (int(lib.pty_ws_act_bwd_scratch(P, cout)),), torch.float32)
         _native.check(lib.pty_ws_act_bwd(P, cout, _p(dA), _p(a), int(relu), _p(dZ), _p(self.gb[i]),
                                          _p(scr), sp))
-        # wgrad: dW[co][k] = sum_p dZ[p][co] col[p][k], split over pixels
-        splits = max(1, min(64, P // 4096))
-        part = self._buf("wpart", (splits, cout, K), torch.float32)
-        col = self._bufs["col%d" % i]
-        _native.check(lib.pty_ws_gemm(cout, K, P, _p(dZ), 1, cout, _p(col), K, 1,
-                                      _p(self.gw[i]), K, 1, splits, _p(part), sp))
+        if wscr_n >= 0:
+            # wgrad on the tensor cores from channel-major copies of the layer
+            # input (three x-shifted) and of dZ; no im2col buffer
+            xs = self._buf("xs", (3, cin, P), torch.bfloat16)
+            _native.check(lib.pty_ws_shift_transpose(B, H, W, cin, 3, _p(self._fwd_inputs[i]), _p(xs), sp))
+            dzt = self._buf("dzt", (cout, P), torch.bfloat16)
+            _native.check(lib.pty_ws_shift_transpose(B, H, W, cout, 1, _p(dZ), _p(dzt), sp))
+            wscr = self._buf("wscr", (wscr_n,), torch.float32)
+            _native.check(lib.pty_ws_wgrad_tc(B, H, W, cin, cout, _p(xs), _p(dzt), _p(self.gw[i]), _p(wscr),
+                                              wscr_n, sp))
+        else:
+            # wgrad: dW[co][k] = sum_p dZ[p][co] col[p][k], split over pixels
+            # (about two CTAs per SM: tiles x splits ~ 304)
+            tiles = ((cout + 63) // 64) * ((K + 63) // 64)
+            splits = max(1, min(512, P // 1024, (304 + tiles - 1) // tiles))
+            part = self._buf("wpart", (splits, cout, K), torch.float32)
+            col = self._bufs["col%d" % i]
+            _native.check(lib.pty_ws_gemm(cout, K, P, _p(dZ), 1, cout, _p(col), K, 1,
+                                          _p(self.gw[i]), K, 1, splits, _p(part), sp))
         if not need_dx:
             return None
         if getattr(self, "_fwd_inputs", None) is not None:

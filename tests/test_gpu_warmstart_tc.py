@@ -151,6 +151,96 @@ def test_input_gradient_convolution_matches_fp64(case):
     assert np.linalg.norm(got - ref) / np.linalg.norm(ref) < 1e-5
 
 
+def shift_ref(x, S):
+    """XS[s][c][p] of pty_ws_shift_transpose for NHWC x (float64)."""
+    B, H, W, C = x.shape
+    out = np.zeros((S, C, B, H, W))
+    for s in range(S):
+        sh = s - 1 if S == 3 else 0
+        src = np.zeros_like(x)
+        if sh < 0:
+            src[:, :, 1:] = x[:, :, :-1]
+        elif sh > 0:
+            src[:, :, :-1] = x[:, :, 1:]
+        else:
+            src = x
+        out[s] = np.transpose(src, (3, 0, 1, 2))
+    return out.reshape(S, C, B * H * W)
+
+
+@pytest.mark.parametrize("S,C", [(3, 64), (1, 2), (3, 32), (1, 128)])
+def test_shift_transpose_matches_numpy(S, C):
+    B, H, W = 2, 8, 32
+    rng = np.random.default_rng(S * 100 + C)
+    x = bf16(rng.standard_normal((B, H, W, C)))
+    xs = torch.empty((S, C, B * H * W), dtype=torch.bfloat16, device=dev())
+    _native.check(_native.load().pty_ws_shift_transpose(B, H, W, C, S, p(x), p(xs), stream()))
+    ref = shift_ref(x.float().cpu().numpy().astype(np.float64), S)
+    np.testing.assert_array_equal(xs.float().cpu().numpy(), ref)
+
+
+def wgrad_ref(x, dz):
+    """float64 dW[co][(ky*3+kx) C_in + ci] = sum_p dZ[p][co] X[p + (ky-1, kx-1)][ci]."""
+    B, H, W, cin = x.shape
+    co = dz.shape[-1]
+    xp = np.zeros((B, H + 2, W + 2, cin))
+    xp[:, 1:-1, 1:-1] = x
+    dw = np.zeros((co, 3, 3, cin))
+    for ky in range(3):
+        for kx in range(3):
+            dw[:, ky, kx] = np.einsum("bhwo,bhwc->oc", dz, xp[:, ky:ky + H, kx:kx + W])
+    return dw.reshape(co, 9 * cin)
+
+
+# (B, H, W, C_in, C_out): the network's layers 1-5 at 128^2 frames, plus a
+# 192-wide image (three chunks per row) with C_out 48 (N = 48: a partial
+# 32-column accumulator read)
+WGRAD_CASES = [(2, 64, 64, 32, 64), (2, 32, 32, 64, 128), (2, 64, 64, 128, 64), (2, 128, 128, 64, 32),
+               (2, 128, 128, 32, 2), (1, 16, 192, 64, 48)]
+
+
+@pytest.mark.parametrize("case", WGRAD_CASES, ids=lambda c: "x".join(map(str, c)))
+def test_wgrad_tc_matches_fp64(case):
+    """pty_ws_wgrad_tc (tcgen05, pixels on K, split partial sums added in
+    order) against the float64 weight gradient of the same BF16 operands:
+    the products are exact in FP32, the sums run over up to 2^15 pixels per
+    split, so within 1e-5 norm-wise; and the same bits on a second call."""
+    B, H, W, cin, cout = case
+    lib = _native.load()
+    rng = np.random.default_rng(B + H + W + cin + cout)
+    x = bf16(rng.standard_normal((B, H, W, cin)))
+    dz = bf16(rng.standard_normal((B, H, W, cout)))
+    P = B * H * W
+    xs = torch.empty((3, cin, P), dtype=torch.bfloat16, device=dev())
+    dzt = torch.empty((cout, P), dtype=torch.bfloat16, device=dev())
+    _native.check(lib.pty_ws_shift_transpose(B, H, W, cin, 3, p(x), p(xs), stream()))
+    _native.check(lib.pty_ws_shift_transpose(B, H, W, cout, 1, p(dz), p(dzt), stream()))
+    n = int(lib.pty_ws_wgrad_tc_scratch(B, H, W, cin, cout))
+    assert n > 0
+    scr = torch.empty(n, dtype=torch.float32, device=dev())
+    dws = []
+    for _ in range(2):
+        dw = torch.full((cout, 9 * cin), float("nan"), dtype=torch.float32, device=dev())
+        _native.check(lib.pty_ws_wgrad_tc(B, H, W, cin, cout, p(xs), p(dzt), p(dw), p(scr), n, stream()))
+        dws.append(dw.cpu().numpy())
+    assert status_ok()
+    ref = wgrad_ref(x.float().cpu().numpy().astype(np.float64), dz.float().cpu().numpy().astype(np.float64))
+    got = dws[0].astype(np.float64)
+    assert np.all(np.isfinite(got))
+    assert np.linalg.norm(got - ref) / np.linalg.norm(ref) < 1e-5
+    np.testing.assert_array_equal(dws[0], dws[1])
+
+
+def test_wgrad_tc_rejects_unsupported_shapes():
+    lib = _native.load()
+    for args in ((1, 8, 64, 2, 32), (1, 8, 64, 48, 32), (1, 8, 16, 32, 32), (1, 8, 96, 32, 32),
+                 (1, 8, 64, 32, 256)):
+        assert lib.pty_ws_wgrad_tc_scratch(*args) == -1, args
+    t = torch.zeros(1 << 16, dtype=torch.float32, device=dev())
+    rc = lib.pty_ws_wgrad_tc(1, 8, 16, 32, 32, p(t), p(t), p(t), p(t), 1 << 16, stream())
+    assert rc == 6
+
+
 def test_conv_tc_rejects_unsupported_shapes():
     lib = _native.load()
     t = torch.zeros(1 << 16, dtype=torch.bfloat16, device=dev())
@@ -292,8 +382,9 @@ def test_training_forward_on_tensor_cores_gives_the_same_gradients():
     activations, the backward pass forming its own im2col buffers) gives the
     weight and bias gradients of the im2col + mma.sync forward pass, up to
     the FP32 summation order of the forward sums (one BF16 rounding step on
-    some activations) and of the input gradients (flipped-weight
-    convolutions instead of GEMM + col2im): within 3e-2 norm-wise per layer."""
+    some activations) and of the input and weight gradients (flipped-weight
+    convolutions instead of GEMM + col2im; the tensor-core weight gradient
+    for layers 1-5): within 3e-2 norm-wise per layer."""
     net = WarmStartNet(128, 128, seed=4, device=dev())
     rng = np.random.default_rng(9)
     B = 8
