@@ -697,7 +697,7 @@ def _nmse_leg(torch, dev, net, w, target, max_iters):
             if warm["seconds_total"] > 0 and warm["reached"] else None}
 
 
-def train_warm_start(torch, dev, warm_steps=6000, warm_frames=50000):
+def train_warm_start(torch, dev, warm_steps=20000, warm_frames=50000):
     """The warm start's network (128^2 frames) trained on the GPU: warm_steps
     Adam steps of 32 frames from warm_frames simulated frames (random objects
     with smoothing widths 2-4 px, random probes, Poisson noise at 1e5-1e7
@@ -719,7 +719,9 @@ def train_warm_start(torch, dev, warm_steps=6000, warm_frames=50000):
             "target": "object phase under the probe (cos, sin), weights |P|^2",
             "kernels": "inference and the training forward pass: tcgen05 implicit-GEMM convolutions "
                        "(layers 1-4), direct CUDA-core convolutions (layers 0, 5); training backward: "
-                       "im2col + mma.sync GEMMs"}
+                       "input gradients as tcgen05 convolutions with flipped weights (layers 1-4; "
+                       "layer 5 direct), weight gradients as tcgen05 GEMMs over the pixels (layers "
+                       "1-5; layer 0 im2col + mma.sync)"}
     return net, info
 
 
@@ -1006,7 +1008,7 @@ def main():
                     help="skip the 4096-frame 512x512 DM measurement")
     ap.add_argument("--no-batch", action="store_true",
                     help="skip the 64-reconstruction batched measurement")
-    ap.add_argument("--warm-steps", type=int, default=6000,
+    ap.add_argument("--warm-steps", type=int, default=20000,
                     help="training steps of the warm start's network in the time-to-NMSE measurement")
     ap.add_argument("--frame-tile", type=int, default=0,
                     help="force this frame tile (CTAs per frame; see pty_set_frame_tile) for profiling")
