@@ -321,7 +321,7 @@ int pty_ws_conv3x3_tc_f32(int32_t B, int32_t H, int32_t W, int32_t Cin, int32_t 
  * pre-activation sums channel-major, both made by pty_ws_shift_transpose:
  *   pty_ws_shift_transpose: XS[s][c][p] = X[p shifted by s - 1 along x][c]
  *     (zero past the row ends) for S = 3; XS[0][c][p] = X[p][c] for S = 1;
- *     X bf16 [P][C] (P = B H W, W even, C <= 256), XS bf16 [S][C][P];
+ *     X bf16 [P][C] (P = B H W, W even, C <= 128), XS bf16 [S][C][P];
  *   pty_ws_wgrad_tc: XS [3][C_in][P], dZT [C_out][P], C_in 32, 64 or 128,
  *     C_out 1..128, W 32 or a multiple of 64; scratch of at least
  *     pty_ws_wgrad_tc_scratch(...) floats (-1: shape unsupported) holds the

@@ -596,39 +596,75 @@ __global__ void ws_wgrad_reduce_kernel(int splits, int kpad, int K9, int Cout, c
 
 // XS[s][c][p] = X[p shifted by s - 1 along x][c] (zero past either end of the
 // image row) for s < 3 when S = 3; XS[0][c][p] = X[p][c] when S = 1.  X is
-// [P][C] bf16 (P = B H W pixels); one block per 64 pixels, staged through
-// shared memory with a one-pixel halo so both sides are coalesced.
-constexpr int kTrPix = 64;
-__global__ void __launch_bounds__(256) ws_shift_transpose_kernel(long long P, int W, int C, int S,
+// [P][C] bf16 (P = B H W pixels, C <= 128); one block per 128 pixels, staged
+// through shared memory as [c][pixel] with a one-pixel halo: 16-byte loads
+// (all of a thread's issued before any is stored, so their latencies
+// overlap), odd row pitch (the 8 channels of a load land in distinct banks),
+// and each warp writes 128 contiguous bytes of one output row at a time.
+constexpr int kTrPix = 128;
+constexpr int kTrPitch = kTrPix + 3;     // odd
+constexpr int kTrBatch = 9;              // 16-byte loads in flight per thread (130 x 16 <= 9 x 256)
+__global__ void __launch_bounds__(256) ws_shift_transpose_kernel(long long P, int W, int C, int S, int vec,
                                                                  const __nv_bfloat16* __restrict__ X,
                                                                  __nv_bfloat16* __restrict__ XS) {
-  extern __shared__ __nv_bfloat16 tr_s[];          // [kTrPix + 2][C + 2]
-  const int pitch = C + 2;
+  extern __shared__ __nv_bfloat16 tr_s[];          // [C][kTrPitch]: pixel p0 - 1 + i at column i
   const long long p0 = (long long)blockIdx.x * kTrPix;
-  const int n = (kTrPix + 2) * C;
-  for (int e = threadIdx.x; e < n; e += blockDim.x) {
-    const int i = e / C, c = e % C;
-    const long long pp = p0 - 1 + i;
-    tr_s[i * pitch + c] = (pp >= 0 && pp < P) ? X[pp * C + c] : __float2bfloat16(0.f);
+  constexpr int rows = kTrPix + 2;
+  const int tid = threadIdx.x;
+  if (vec) {
+    const int c8n = C / 8, n = rows * c8n;
+    for (int base = 0; base < n; base += kTrBatch * 256) {
+      uint4 v[kTrBatch];
+#pragma unroll
+      for (int r = 0; r < kTrBatch; ++r) {
+        const int e = base + tid + 256 * r;
+        v[r] = make_uint4(0u, 0u, 0u, 0u);
+        if (e < n) {
+          const long long pp = p0 - 1 + e / c8n;
+          if (pp >= 0 && pp < P) v[r] = __ldg(reinterpret_cast<const uint4*>(X + pp * C + 8 * (e % c8n)));
+        }
+      }
+#pragma unroll
+      for (int r = 0; r < kTrBatch; ++r) {
+        const int e = base + tid + 256 * r;
+        if (e < n) {
+          const int i = e / c8n, c = 8 * (e % c8n);
+          const __nv_bfloat16* h = reinterpret_cast<const __nv_bfloat16*>(&v[r]);
+#pragma unroll
+          for (int k = 0; k < 8; ++k) tr_s[(c + k) * kTrPitch + i] = h[k];
+        }
+      }
+    }
+  } else {
+    const int n = rows * C;
+    for (int e = tid; e < n; e += 256) {
+      const int i = e / C, c = e % C;
+      const long long pp = p0 - 1 + i;
+      tr_s[c * kTrPitch + i] = (pp >= 0 && pp < P) ? X[pp * C + c] : __float2bfloat16(0.f);
+    }
   }
   __syncthreads();
-  const int i2 = threadIdx.x & 31, r = threadIdx.x >> 5;
-  const long long p = p0 + 2 * i2;
-  if (p >= P) return;
-  const bool two = p + 1 < P;
-  const int x = (int)(p % W);                      // W even: p and p + 1 share a row
-  for (int sc = r; sc < S * C; sc += 8) {
+  const int lane = tid & 31, w = tid >> 5;
+  const __nv_bfloat16 z = __float2bfloat16(0.f);
+  for (int sc = w; sc < S * C; sc += 8) {
     const int s = sc / C, c = sc % C;
     const int sh = S == 3 ? s - 1 : 0;
-    const int xa = x + sh, xb = x + 1 + sh;
-    const __nv_bfloat16 z = __float2bfloat16(0.f);
-    const __nv_bfloat16 va = (xa >= 0 && xa < W) ? tr_s[(2 * i2 + 1 + sh) * pitch + c] : z;
-    const __nv_bfloat16 vb = (xb >= 0 && xb < W) ? tr_s[(2 * i2 + 2 + sh) * pitch + c] : z;
-    __nv_bfloat16* o = XS + ((size_t)s * C + c) * P + p;
-    if (two) {
-      *reinterpret_cast<__nv_bfloat162*>(o) = __halves2bfloat162(va, vb);
-    } else {
-      o[0] = va;
+    const __nv_bfloat16* row = tr_s + c * kTrPitch;
+    __nv_bfloat16* orow = XS + ((size_t)s * C + c) * P;
+#pragma unroll
+    for (int h = 0; h < kTrPix / 64; ++h) {
+      const int i = 2 * lane + 64 * h;             // even pixel offset in the tile
+      const long long p = p0 + i;
+      if (p >= P) break;
+      const int x = (int)(p % W);                  // W even: p and p + 1 share a row
+      const int xa = x + sh, xb = x + 1 + sh;
+      const __nv_bfloat16 va = (xa >= 0 && xa < W) ? row[i + 1 + sh] : z;
+      const __nv_bfloat16 vb = (xb >= 0 && xb < W) ? row[i + 2 + sh] : z;
+      if (p + 1 < P) {
+        *reinterpret_cast<__nv_bfloat162*>(orow + p) = __halves2bfloat162(va, vb);
+      } else {
+        orow[p] = va;
+      }
     }
   }
 }
@@ -794,16 +830,17 @@ extern "C" int64_t pty_ws_wgrad_tc_scratch(int32_t B, int32_t H, int32_t W, int3
 
 extern "C" int pty_ws_shift_transpose(int32_t B, int32_t H, int32_t W, int32_t C, int32_t S, const void* X,
                                       void* XS, void* stream) {
-  if (B < 1 || H < 1 || W < 2 || (W & 1) || C < 1 || C > 256 || !(S == 1 || S == 3) || !X || !XS)
+  if (B < 1 || H < 1 || W < 2 || (W & 1) || C < 1 || C > 128 || !(S == 1 || S == 3) || !X || !XS)
     return set_error(PTY_ERR_ARG, "pty_ws_shift_transpose: bad arguments");
   if ((reinterpret_cast<uintptr_t>(XS) & 3) != 0)
     return set_error(PTY_ERR_ARG, "pty_ws_shift_transpose: XS must be 4-byte aligned");
   const long long P = (long long)B * H * W;
   const long long blocks = (P + kTrPix - 1) / kTrPix;
   if (blocks >= (1ll << 31)) return set_error(PTY_ERR_UNSUPPORTED, "pty_ws_shift_transpose: too many pixels");
-  const size_t smem = (size_t)(kTrPix + 2) * (C + 2) * sizeof(__nv_bfloat16);
+  const size_t smem = (size_t)C * kTrPitch * sizeof(__nv_bfloat16);
+  const int vec = C % 8 == 0 && (reinterpret_cast<uintptr_t>(X) & 15) == 0;
   ws_shift_transpose_kernel<<<(unsigned)blocks, 256, smem, (cudaStream_t)stream>>>(
-      P, W, C, S, static_cast<const __nv_bfloat16*>(X), static_cast<__nv_bfloat16*>(XS));
+      P, W, C, S, vec, static_cast<const __nv_bfloat16*>(X), static_cast<__nv_bfloat16*>(XS));
   return check_launch("ws_shift_transpose_kernel");
 }
 

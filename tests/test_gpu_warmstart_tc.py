@@ -168,9 +168,11 @@ def shift_ref(x, S):
     return out.reshape(S, C, B * H * W)
 
 
-@pytest.mark.parametrize("S,C", [(3, 64), (1, 2), (3, 32), (1, 128)])
-def test_shift_transpose_matches_numpy(S, C):
-    B, H, W = 2, 8, 32
+@pytest.mark.parametrize("S,C", [(3, 64), (1, 2), (3, 32), (1, 128), (3, 128)])
+@pytest.mark.parametrize("B,H,W", [(2, 8, 32), (1, 3, 34)])
+def test_shift_transpose_matches_numpy(S, C, B, H, W):
+    """Exact (a copy): whole 128-pixel tiles, and a ragged last tile with
+    rows that straddle tiles (34 x 3 pixels)."""
     rng = np.random.default_rng(S * 100 + C)
     x = bf16(rng.standard_normal((B, H, W, C)))
     xs = torch.empty((S, C, B * H * W), dtype=torch.bfloat16, device=dev())
