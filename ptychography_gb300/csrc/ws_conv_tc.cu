@@ -46,9 +46,12 @@ constexpr int kStages = 4;
 constexpr int kThreads = 192;
 constexpr int kMaxCout = 128;
 constexpr int kAccCols = 256;         // TMEM columns: two accumulators of up to 128
-// at least this much dynamic shared memory per CTA, so one CTA runs per SM and
-// its tensor-memory allocation never waits for another CTA's
-constexpr size_t kMinSmem = 116 * 1024;
+// at least this much dynamic shared memory per CTA, so that at most two CTAs
+// share an SM and their tensor-memory allocations (kAccCols each, 512 columns
+// per SM) never wait for another CTA's; a layer whose stage ring fits in
+// kTwoPerSm bytes runs two CTAs per SM (twice the TMA bytes in flight)
+constexpr size_t kMinSmem = 77 * 1024;
+constexpr size_t kTwoPerSm = 112 * 1024;
 constexpr unsigned kSpinLimit = 1u << 26;
 
 struct ConvParams {
@@ -776,7 +779,8 @@ static int conv_tc(int32_t B, int32_t H, int32_t W, int32_t Cin, int32_t Cout, c
                                     (int)conv_tc_smem(64, kMaxCout));
   });
   if (attr_err != cudaSuccess) return set_cuda_error(attr_err, "pty_ws_conv3x3_tc: smem attribute");
-  const int grid = p.tiles < sm_count() ? p.tiles : sm_count();
+  const int slots = (smem <= kTwoPerSm ? 2 : 1) * sm_count();
+  const int grid = p.tiles < slots ? p.tiles : slots;
   ws_conv_tc_kernel<<<grid, kThreads, smem, (cudaStream_t)stream>>>(tmX, tmW, p);
   return check_launch("ws_conv_tc_kernel");
 }
@@ -789,6 +793,12 @@ namespace {
 struct WgradShape {
   int kchunk, npad, tpt, mtiles, nchunks, cps, splits, kpad;
 };
+
+size_t wgrad_smem(const WgradShape& w) {
+  const size_t stage = (((size_t)kTileM * w.kchunk * 2 + (size_t)w.npad * w.kchunk * 2 + 1023) / 1024) * 1024;
+  const size_t need = kStages * stage + sizeof(SmemCtl) + 1024;
+  return need > kMinSmem ? need : kMinSmem;
+}
 
 int wgrad_shape(int B, int H, int W, int Cin, int Cout, WgradShape& w) {
   if (B < 1 || H < 1 || W < 1) return set_error(PTY_ERR_ARG, "pty_ws_wgrad_tc: empty input");
@@ -804,8 +814,9 @@ int wgrad_shape(int B, int H, int W, int Cin, int Cout, WgradShape& w) {
   w.tpt = kTileM / Cin;
   w.mtiles = (9 + w.tpt - 1) / w.tpt;
   w.nchunks = (int)(P / w.kchunk);
-  // at most two items per SM, every split non-empty
-  const int want = 2 * sm_count() / w.mtiles > 0 ? 2 * sm_count() / w.mtiles : 1;
+  // at most two items per CTA slot, every split non-empty
+  const int slots = (wgrad_smem(w) <= kTwoPerSm ? 2 : 1) * sm_count();
+  const int want = 2 * slots / w.mtiles > 0 ? 2 * slots / w.mtiles : 1;
   int splits = want < w.nchunks ? want : w.nchunks;
   w.cps = (w.nchunks + splits - 1) / splits;
   w.splits = (w.nchunks + w.cps - 1) / w.cps;
@@ -813,11 +824,6 @@ int wgrad_shape(int B, int H, int W, int Cin, int Cout, WgradShape& w) {
   return PTY_OK;
 }
 
-size_t wgrad_smem(const WgradShape& w) {
-  const size_t stage = (((size_t)kTileM * w.kchunk * 2 + (size_t)w.npad * w.kchunk * 2 + 1023) / 1024) * 1024;
-  const size_t need = kStages * stage + sizeof(SmemCtl) + 1024;
-  return need > kMinSmem ? need : kMinSmem;
-}
 
 }  // namespace
 }  // namespace pty
@@ -905,7 +911,8 @@ extern "C" int pty_ws_wgrad_tc(int32_t B, int32_t H, int32_t W, int32_t Cin, int
                                     (int)wgrad_smem(big));
   });
   if (attr_err != cudaSuccess) return set_cuda_error(attr_err, "pty_ws_wgrad_tc: smem attribute");
-  const int grid = p.items < sm_count() ? p.items : sm_count();
+  const int slots = (smem <= kTwoPerSm ? 2 : 1) * sm_count();
+  const int grid = p.items < slots ? p.items : slots;
   ws_wgrad_tc_kernel<<<grid, kThreads, smem, (cudaStream_t)stream>>>(tmX, tmD, p);
   PTY_TRY(check_launch("ws_wgrad_tc_kernel"));
   const long long n = (long long)Cout * 9 * Cin;
