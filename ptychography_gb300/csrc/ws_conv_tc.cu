@@ -19,7 +19,7 @@
 // reads (64-byte swizzle when C_in = 32).  No im2col buffer is written.
 //
 // Roles (one CTA per SM, persistent over tiles, 192 threads):
-//   warp 4, one lane: TMA producer over a ring of kStages stages;
+//   warp 4, one lane: TMA producer over a ring of 4-8 stages;
 //   warp 5, one lane: MMA issuer; accumulators double-buffered in TMEM so the
 //     epilogue of one tile overlaps the MMAs of the next;
 //   warps 0-3: epilogue, warp w reading TMEM lanes 32w..32w+31 (its 32 pixels).
@@ -42,7 +42,11 @@ namespace {
 
 constexpr int kTileM = 128;
 constexpr int kChunk = 64;            // input channels per stage
-constexpr int kStages = 4;
+constexpr int kStages = 4;            // ring depth of a layer running one CTA per SM
+constexpr int kMaxStages = 8;
+#ifndef PTY_WS_RING_MAX
+#define PTY_WS_RING_MAX kMaxStages   // deepest ring ring_depth() picks (a tuning bound, 4..8)
+#endif
 constexpr int kThreads = 192;
 constexpr int kMaxCout = 128;
 constexpr int kAccCols = 256;         // TMEM columns: two accumulators of up to 128
@@ -61,6 +65,7 @@ struct ConvParams {
   int tiles;               // B * (H / rows) * xtiles
   int chunks;              // ceil(Cin / 64)
   int chunk_ch;            // channels per chunk (64, or Cin when Cin < 64)
+  int stages;              // TMA ring depth (<= kMaxStages)
   int relu;
   const float* bias;       // [Cout]
   const __nv_bfloat16* skip;   // [P][Cout] or nullptr
@@ -194,8 +199,8 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
 }
 
 struct __align__(8) SmemCtl {
-  uint64_t full[kStages];
-  uint64_t empty[kStages];
+  uint64_t full[kMaxStages];
+  uint64_t empty[kMaxStages];
   uint64_t acc_full[2];
   uint64_t acc_empty[2];
   uint64_t drain;
@@ -221,16 +226,17 @@ __global__ void __launch_bounds__(kThreads, 1)
   // stage buffers at a 1024-byte boundary (the 128-byte swizzle's atom)
   const uint32_t raw = smem_u32(smem_raw);
   unsigned char* base = smem_raw + ((1024 - (raw & 1023)) & 1023);
+  const int nst = p.stages;
   const int a_bytes = kTileM * p.chunk_ch * 2;            // 16 KB (8 KB when C_in = 32)
   const int b_bytes = p.Cout * p.chunk_ch * 2;
   const int stage_bytes = ((a_bytes + b_bytes + 1023) / 1024) * 1024;
-  SmemCtl* ctl = reinterpret_cast<SmemCtl*>(base + kStages * stage_bytes);
+  SmemCtl* ctl = reinterpret_cast<SmemCtl*>(base + nst * stage_bytes);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int swz = p.chunk_ch * 2;                         // 128 or 64 bytes per row
 
   for (int i = threadIdx.x; i < p.Cout; i += kThreads) ctl->bias[i] = p.bias ? p.bias[i] : 0.f;
   if (threadIdx.x == 0) {
-    for (int s = 0; s < kStages; ++s) {
+    for (int s = 0; s < nst; ++s) {
       mbar_init(&ctl->full[s], 1);
       mbar_init(&ctl->empty[s], 1);
     }
@@ -262,13 +268,13 @@ __global__ void __launch_bounds__(kThreads, 1)
   if (warp == 4) {
     // ------------------------------------------------ TMA producer
     if (lane == 0) {
-      int q = 0;
+      int q = 0, rs = 0, rph = 0;   // ring position: q = stages used, rs = q mod nst, rph = its phase
       bool ok = true;
       for (int t = blockIdx.x; t < p.tiles && ok; t += gridDim.x) {
         int b, y0, x0;
         tile_origin(p, t, b, y0, x0);
-        for (int st = 0; st < nstage_per_tile && ok; ++st, ++q) {
-          const int s = q % kStages, ph = (q / kStages) & 1;
+        for (int st = 0; st < nstage_per_tile && ok; ++st, ++q, rs = (rs + 1 == nst) ? 0 : rs + 1, rph ^= (rs == 0)) {
+          const int s = rs, ph = rph;
           if (!mbar_wait(&ctl->empty[s], ph ^ 1, abort, p.err)) { ok = false; break; }
           const int tap = st / p.chunks, ch = st % p.chunks;
           const int ky = tap / 3, kx = tap % 3;
@@ -281,10 +287,10 @@ __global__ void __launch_bounds__(kThreads, 1)
       }
       // copies issued but never consumed (after an abort) finish before exit
       if (!ok) {
-        for (int k = 0; k < kStages; ++k) {
+        for (int k = 0; k < nst; ++k) {
           const int qq = q - 1 - k;
           if (qq < 0) break;
-          const int s = qq % kStages, ph = (qq / kStages) & 1;
+          const int s = qq % nst, ph = (qq / nst) & 1;
           for (unsigned i = 0; i < kSpinLimit && !mbar_try_wait(&ctl->full[s], ph); ++i) {
           }
         }
@@ -293,15 +299,15 @@ __global__ void __launch_bounds__(kThreads, 1)
   } else if (warp == 5) {
     // ------------------------------------------------ MMA issuer
     if (lane == 0) {
-      int q = 0, local = 0;
+      int q = 0, rs = 0, rph = 0, local = 0;
       bool ok = true;
       for (int t = blockIdx.x; t < p.tiles && ok; t += gridDim.x, ++local) {
         const int buf = local & 1, use = local >> 1;
         if (!mbar_wait(&ctl->acc_empty[buf], (use & 1) ^ 1, abort, p.err)) { ok = false; break; }
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         const uint32_t d = tmem + buf * acc_stride;
-        for (int st = 0; st < nstage_per_tile; ++st, ++q) {
-          const int s = q % kStages, ph = (q / kStages) & 1;
+        for (int st = 0; st < nstage_per_tile; ++st, ++q, rs = (rs + 1 == nst) ? 0 : rs + 1, rph ^= (rs == 0)) {
+          const int s = rs, ph = rph;
           if (!mbar_wait(&ctl->full[s], ph, abort, p.err)) { ok = false; break; }
           asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
           const uint32_t sa = smem_u32(base + s * stage_bytes);
@@ -419,6 +425,7 @@ struct WgradParams {
   int nchunks, cps, splits;      // pixel chunks, chunks per split, splits
   int items;                     // mtiles * splits
   int kpad;                      // mtiles * 128
+  int stages;                    // TMA ring depth (<= kMaxStages)
   float* partial;                // [splits][kpad][Cout]
   int* err;
 };
@@ -439,15 +446,16 @@ __global__ void __launch_bounds__(kThreads, 1)
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   const uint32_t raw = smem_u32(smem_raw);
   unsigned char* base = smem_raw + ((1024 - (raw & 1023)) & 1023);
+  const int nst = p.stages;
   const int row_bytes = p.kchunk * 2;                     // 128 or 64: the swizzle span
   const int a_bytes = kTileM * row_bytes;
   const int b_bytes = p.npad * row_bytes;
   const int stage_bytes = ((a_bytes + b_bytes + 1023) / 1024) * 1024;
-  SmemCtl* ctl = reinterpret_cast<SmemCtl*>(base + kStages * stage_bytes);
+  SmemCtl* ctl = reinterpret_cast<SmemCtl*>(base + nst * stage_bytes);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
   if (threadIdx.x == 0) {
-    for (int s = 0; s < kStages; ++s) {
+    for (int s = 0; s < nst; ++s) {
       mbar_init(&ctl->full[s], 1);
       mbar_init(&ctl->empty[s], 1);
     }
@@ -478,15 +486,15 @@ __global__ void __launch_bounds__(kThreads, 1)
   if (warp == 4) {
     // ------------------------------------------------ TMA producer
     if (lane == 0) {
-      int q = 0;
+      int q = 0, rs = 0, rph = 0;
       bool ok = true;
       for (int t = blockIdx.x; t < p.items && ok; t += gridDim.x) {
         const int mt = t % p.mtiles, sp = t / p.mtiles;
         const int c0 = sp * p.cps, c1 = min(c0 + p.cps, p.nchunks);
         const int tap0 = mt * p.tpt, ntap = min(p.tpt, 9 - tap0);
         const unsigned tx = (unsigned)(ntap * p.Cin * row_bytes + b_bytes);
-        for (int c = c0; c < c1 && ok; ++c, ++q) {
-          const int s = q % kStages, ph = (q / kStages) & 1;
+        for (int c = c0; c < c1 && ok; ++c, ++q, rs = (rs + 1 == nst) ? 0 : rs + 1, rph ^= (rs == 0)) {
+          const int s = rs, ph = rph;
           if (!mbar_wait(&ctl->empty[s], ph ^ 1, abort, p.err)) { ok = false; break; }
           const int xt = c % p.xtiles, row = c / p.xtiles;
           const int y = row % p.H, b = row / p.H, x0 = xt * p.kchunk;
@@ -501,10 +509,10 @@ __global__ void __launch_bounds__(kThreads, 1)
         }
       }
       if (!ok) {
-        for (int k = 0; k < kStages; ++k) {
+        for (int k = 0; k < nst; ++k) {
           const int qq = q - 1 - k;
           if (qq < 0) break;
-          const int s = qq % kStages, ph = (qq / kStages) & 1;
+          const int s = qq % nst, ph = (qq / nst) & 1;
           for (unsigned i = 0; i < kSpinLimit && !mbar_try_wait(&ctl->full[s], ph); ++i) {
           }
         }
@@ -513,7 +521,7 @@ __global__ void __launch_bounds__(kThreads, 1)
   } else if (warp == 5) {
     // ------------------------------------------------ MMA issuer
     if (lane == 0) {
-      int q = 0, local = 0;
+      int q = 0, rs = 0, rph = 0, local = 0;
       bool ok = true;
       for (int t = blockIdx.x; t < p.items && ok; t += gridDim.x, ++local) {
         const int sp = t / p.mtiles;
@@ -522,8 +530,8 @@ __global__ void __launch_bounds__(kThreads, 1)
         if (!mbar_wait(&ctl->acc_empty[buf], (use & 1) ^ 1, abort, p.err)) { ok = false; break; }
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         const uint32_t d = tmem + buf * acc_stride;
-        for (int c = c0; c < c1; ++c, ++q) {
-          const int s = q % kStages, ph = (q / kStages) & 1;
+        for (int c = c0; c < c1; ++c, ++q, rs = (rs + 1 == nst) ? 0 : rs + 1, rph ^= (rs == 0)) {
+          const int s = rs, ph = rph;
           if (!mbar_wait(&ctl->full[s], ph, abort, p.err)) { ok = false; break; }
           asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
           const uint32_t sa = smem_u32(base + s * stage_bytes);
@@ -681,12 +689,29 @@ int sm_count() {
 
 }  // namespace
 
-// dynamic shared memory of one CTA for a layer (stage ring + control block + alignment slack)
-static size_t conv_tc_smem(int Cin, int Cout) {
+// The ring of a CTA with stage_bytes per stage: the deepest ring (up to
+// kMaxStages) whose CTA still fits two per SM, or kStages stages at one per
+// SM; returns the depth and the dynamic shared memory (stage ring + control
+// block + alignment slack).
+static int ring_depth(size_t stage_bytes, size_t* smem) {
+  const size_t fixed = sizeof(SmemCtl) + 1024;
+  int n = PTY_WS_RING_MAX;
+  while (n > kStages && n * stage_bytes + fixed > kTwoPerSm) --n;
+  const size_t need = n * stage_bytes + fixed;
+  *smem = need > kMinSmem ? need : kMinSmem;
+  return n;
+}
+
+// the largest ring_depth() shared memory of any layer whose stages are at
+// most stage_bytes: a deep ring within kTwoPerSm, or kStages stages
+static size_t max_ring_smem(size_t stage_bytes) {
+  const size_t one = kStages * stage_bytes + sizeof(SmemCtl) + 1024;
+  return one > kTwoPerSm ? one : kTwoPerSm;
+}
+
+static size_t conv_tc_stage_bytes(int Cin, int Cout) {
   const int chunk = Cin < kChunk ? Cin : kChunk;
-  const size_t stage = (((size_t)kTileM * chunk * 2 + (size_t)Cout * chunk * 2 + 1023) / 1024) * 1024;
-  const size_t need = kStages * stage + sizeof(SmemCtl) + 1024;
-  return need > kMinSmem ? need : kMinSmem;
+  return (((size_t)kTileM * chunk * 2 + (size_t)Cout * chunk * 2 + 1023) / 1024) * 1024;
 }
 
 }  // namespace pty
@@ -771,12 +796,13 @@ static int conv_tc(int32_t B, int32_t H, int32_t W, int32_t Cin, int32_t Cout, c
                         CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) return set_error(PTY_ERR_CUDA, "pty_ws_conv3x3_tc: weight tensor map");
   }
-  const size_t smem = conv_tc_smem(Cin, Cout);
+  size_t smem = 0;
+  p.stages = ring_depth(conv_tc_stage_bytes(Cin, Cout), &smem);
   static std::once_flag attr_once;
   static cudaError_t attr_err = cudaSuccess;
   std::call_once(attr_once, [] {
     attr_err = cudaFuncSetAttribute(ws_conv_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    (int)conv_tc_smem(64, kMaxCout));
+                                    (int)max_ring_smem(conv_tc_stage_bytes(64, kMaxCout)));
   });
   if (attr_err != cudaSuccess) return set_cuda_error(attr_err, "pty_ws_conv3x3_tc: smem attribute");
   const int slots = (smem <= kTwoPerSm ? 2 : 1) * sm_count();
@@ -794,10 +820,8 @@ struct WgradShape {
   int kchunk, npad, tpt, mtiles, nchunks, cps, splits, kpad;
 };
 
-size_t wgrad_smem(const WgradShape& w) {
-  const size_t stage = (((size_t)kTileM * w.kchunk * 2 + (size_t)w.npad * w.kchunk * 2 + 1023) / 1024) * 1024;
-  const size_t need = kStages * stage + sizeof(SmemCtl) + 1024;
-  return need > kMinSmem ? need : kMinSmem;
+size_t wgrad_stage_bytes(const WgradShape& w) {
+  return (((size_t)kTileM * w.kchunk * 2 + (size_t)w.npad * w.kchunk * 2 + 1023) / 1024) * 1024;
 }
 
 int wgrad_shape(int B, int H, int W, int Cin, int Cout, WgradShape& w) {
@@ -815,7 +839,9 @@ int wgrad_shape(int B, int H, int W, int Cin, int Cout, WgradShape& w) {
   w.mtiles = (9 + w.tpt - 1) / w.tpt;
   w.nchunks = (int)(P / w.kchunk);
   // at most two items per CTA slot, every split non-empty
-  const int slots = (wgrad_smem(w) <= kTwoPerSm ? 2 : 1) * sm_count();
+  size_t smem = 0;
+  ring_depth(wgrad_stage_bytes(w), &smem);
+  const int slots = (smem <= kTwoPerSm ? 2 : 1) * sm_count();
   const int want = 2 * slots / w.mtiles > 0 ? 2 * slots / w.mtiles : 1;
   int splits = want < w.nchunks ? want : w.nchunks;
   w.cps = (w.nchunks + splits - 1) / splits;
@@ -902,13 +928,14 @@ extern "C" int pty_ws_wgrad_tc(int32_t B, int32_t H, int32_t W, int32_t Cin, int
   p.kpad = w.kpad;
   p.partial = scratch;
   p.err = err;
-  const size_t smem = wgrad_smem(w);
+  size_t smem = 0;
+  p.stages = ring_depth(wgrad_stage_bytes(w), &smem);
   static std::once_flag attr_once;
   static cudaError_t attr_err = cudaSuccess;
   std::call_once(attr_once, [] {
     WgradShape big{64, kMaxCout, 1, 9, 1, 1, 1, 9 * kTileM};
     attr_err = cudaFuncSetAttribute(ws_wgrad_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    (int)wgrad_smem(big));
+                                    (int)max_ring_smem(wgrad_stage_bytes(big)));
   });
   if (attr_err != cudaSuccess) return set_cuda_error(attr_err, "pty_ws_wgrad_tc: smem attribute");
   const int slots = (smem <= kTwoPerSm ? 2 : 1) * sm_count();
