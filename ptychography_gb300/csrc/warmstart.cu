@@ -830,8 +830,8 @@ struct BfVec<2> {
   }
 };
 
-template <int COUT, int VEC, int PX>
-__global__ void __launch_bounds__(kDirThreads) ws_conv_direct_kernel(int Bt, int H, int W, int Cin,
+template <int COUT, int VEC, int PX, int CIN>
+__global__ void __launch_bounds__(kDirThreads) ws_conv_direct_kernel(int Bt, int H, int W, int Cin_rt,
                                                                      const __nv_bfloat16* __restrict__ X,
                                                                      const __nv_bfloat16* __restrict__ Wt,
                                                                      const float* __restrict__ bias, int relu,
@@ -840,8 +840,11 @@ __global__ void __launch_bounds__(kDirThreads) ws_conv_direct_kernel(int Bt, int
                                                                      float* __restrict__ out32) {
   // a thread owns PX pixels of a row, 32 apart (W a multiple of 32 PX when
   // PX > 1), so that every weight read from shared memory feeds PX
-  // multiply-adds while the lanes of a warp still read neighbouring pixels
-  extern __shared__ float wsm[];                 // [9 Cin][COUT]
+  // multiply-adds while the lanes of a warp still read neighbouring pixels.
+  // CIN > 0 fixes C_in at compile time (the network's 2- and 32-channel
+  // inputs): the channel loop unrolls and a tap's loads issue together.
+  const int Cin = CIN > 0 ? CIN : Cin_rt;
+  extern __shared__ __align__(16) float wsm[];   // [9 Cin][COUT]
   const int K = 9 * Cin;
   for (int i = threadIdx.x; i < K * COUT; i += blockDim.x) {
     const int co = i / K, k = i - co * K;
@@ -858,7 +861,7 @@ __global__ void __launch_bounds__(kDirThreads) ws_conv_direct_kernel(int Bt, int
     for (int u = 0; u < PX; ++u)
 #pragma unroll
       for (int c = 0; c < COUT; ++c) acc[u][c] = 0.f;
-#pragma unroll 1
+#pragma unroll (CIN > 0 && CIN <= 8 ? 9 : 1)
     for (int tap = 0; tap < 9; ++tap) {
       const int yy = y + tap / 3 - 1;
       if (yy < 0 || yy >= H) continue;
@@ -965,13 +968,125 @@ __global__ void ws_upsample_kernel(int Uh, int Vh, const float2* __restrict__ Oh
   }
 }
 
-template <int COUT, int VEC, int PX>
+
+// The network's last layer, 32 -> 2 channels with an FP32 output, on the CUDA
+// cores.  Four lanes share a pixel, each summing 8 of its 32 input channels:
+// a warp load then covers 8 pixels' 64 contiguous bytes (4 cache lines), where
+// one lane per pixel reading 16 of them touches 16 lines per load and the L1
+// wavefronts bound the kernel.  A lane owns 4 pixels 8 apart (a warp: 32
+// consecutive pixels of a row) and accumulates channel pairs in packed FP32x2
+// FMAs (even and odd channels in the two halves); the halves and then the four
+// lanes' sums are added at the end.
+constexpr int kC2Threads = 256;
+
+PTY_DEV unsigned long long fma2(unsigned long long a, unsigned long long b, unsigned long long c) {
+  unsigned long long d;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+  return d;
+}
+PTY_DEV unsigned long long pack2(float lo, float hi) {
+  unsigned long long r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+  return r;
+}
+PTY_DEV float2 unpack2(unsigned long long r) {
+  float2 a;
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(a.x), "=f"(a.y) : "l"(r));
+  return a;
+}
+
+__global__ void __launch_bounds__(kC2Threads) ws_conv_c32o2_kernel(int Bt, int H, int W,
+                                                                  const __nv_bfloat16* __restrict__ X,
+                                                                  const __nv_bfloat16* __restrict__ Wt,
+                                                                  const float* __restrict__ bias, int relu,
+                                                                  float* __restrict__ out32) {
+  __shared__ __align__(16) float wsm[9][2][32];             // [tap][co][ci]
+  for (int i = threadIdx.x; i < 2 * 9 * 32; i += blockDim.x) {
+    const int co = i / 288, k = i % 288;                    // Wt[co][tap 32 + ci]
+    wsm[k / 32][co][k % 32] = __bfloat162float(Wt[i]);
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31, q = lane & 3, pc = lane >> 2;
+  const int wpb = blockDim.x >> 5;
+  const long long xblocks = W / 32, units = (long long)Bt * H * xblocks;
+  const float b0 = bias[0], b1 = bias[1];
+  for (long long u0 = (long long)blockIdx.x * wpb + (threadIdx.x >> 5); u0 < units;
+       u0 += (long long)gridDim.x * wpb) {
+    const int xb = (int)(u0 % xblocks) * 32;
+    const long long t = u0 / xblocks;
+    const int y = (int)(t % H), b = (int)(t / H);
+    unsigned long long acc[4][2];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) acc[u][0] = acc[u][1] = 0ull;
+#pragma unroll
+    for (int tap = 0; tap < 9; ++tap) {
+      const int yy = y + tap / 3 - 1, dx = tap % 3 - 1;
+      if (yy < 0 || yy >= H) continue;                      // the same for the whole warp
+      const float4* wp = reinterpret_cast<const float4*>(&wsm[tap][0][8 * q]);
+      const float4 w00 = wp[0], w01 = wp[1];                // co 0, channels 8q .. 8q + 7
+      const float4 w10 = wp[8], w11 = wp[9];                // co 1 (32 floats further)
+      const unsigned long long wc0[4] = {pack2(w00.x, w00.y), pack2(w00.z, w00.w), pack2(w01.x, w01.y),
+                                         pack2(w01.z, w01.w)};
+      const unsigned long long wc1[4] = {pack2(w10.x, w10.y), pack2(w10.z, w10.w), pack2(w11.x, w11.y),
+                                         pack2(w11.z, w11.w)};
+      const __nv_bfloat16* xrow = X + ((size_t)(b * H + yy) * W) * 32 + 8 * q;
+      uint4 v[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int x = xb + pc + 8 * u + dx;
+        v[u] = (x >= 0 && x < W) ? __ldg(reinterpret_cast<const uint4*>(xrow + (size_t)x * 32))
+                                 : make_uint4(0u, 0u, 0u, 0u);
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const unsigned int wd[4] = {v[u].x, v[u].y, v[u].z, v[u].w};
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+          // a bf16 pair (channels 2e, 2e + 1 of the chunk) as two floats
+          const unsigned long long xe = pack2(__uint_as_float(wd[e] << 16), __uint_as_float(wd[e] & 0xffff0000u));
+          acc[u][0] = fma2(xe, wc0[e], acc[u][0]);
+          acc[u][1] = fma2(xe, wc1[e], acc[u][1]);
+        }
+      }
+    }
+    float r[4][2];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+#pragma unroll
+      for (int c = 0; c < 2; ++c) {
+        const float2 h = unpack2(acc[u][c]);
+        float sum = h.x + h.y;
+        sum += __shfl_xor_sync(0xffffffffu, sum, 1);
+        sum += __shfl_xor_sync(0xffffffffu, sum, 2);
+        r[u][c] = sum;
+      }
+    }
+    // lane q writes pixel u = q of its column: a warp stores 32 consecutive pixels
+    float o0 = r[0][0], o1 = r[0][1];
+#pragma unroll
+    for (int u = 1; u < 4; ++u)
+      if (q == u) {
+        o0 = r[u][0];
+        o1 = r[u][1];
+      }
+    o0 += b0;
+    o1 += b1;
+    if (relu) {
+      o0 = fmaxf(o0, 0.f);
+      o1 = fmaxf(o1, 0.f);
+    }
+    const int x = xb + pc + 8 * q;
+    *reinterpret_cast<float2*>(out32 + ((size_t)(b * H + y) * W + x) * 2) = make_float2(o0, o1);
+  }
+}
+
+template <int COUT, int VEC, int PX, int CIN>
 void direct_grid(int B, int H, int W, int Cin, const void* X, const void* Wt, const float* bias, int relu,
                  const void* skip, void* out, float* out32, size_t smem, cudaStream_t st) {
   const long long Q = (long long)B * H * (W / PX);
   long long g = (Q + kDirThreads - 1) / kDirThreads;
   if (g > 32 * 152) g = 32 * 152;
-  ws_conv_direct_kernel<COUT, VEC, PX><<<(unsigned)g, kDirThreads, smem, st>>>(
+  ws_conv_direct_kernel<COUT, VEC, PX, CIN><<<(unsigned)g, kDirThreads, smem, st>>>(
       B, H, W, Cin, (const __nv_bfloat16*)X, (const __nv_bfloat16*)Wt, bias, relu, (const __nv_bfloat16*)skip,
       (__nv_bfloat16*)out, out32);
 }
@@ -984,11 +1099,18 @@ int launch_direct(int B, int H, int W, int Cin, const void* X, const void* Wt, c
   // pixels per thread: more for narrow outputs (fewer accumulators)
   constexpr int PXW = COUT <= 4 ? 4 : 2;
   if (W % (32 * PXW) == 0) {
-    if (v8) direct_grid<COUT, 8, PXW>(B, H, W, Cin, X, Wt, bias, relu, skip, out, out32, smem, st);
-    else direct_grid<COUT, 2, PXW>(B, H, W, Cin, X, Wt, bias, relu, skip, out, out32, smem, st);
+    // the network's shapes with C_in fixed at compile time: 2 -> 32 and 32 -> 2
+    if (COUT == 32 && Cin == 2)
+      direct_grid<COUT, 2, PXW, 2>(B, H, W, Cin, X, Wt, bias, relu, skip, out, out32, smem, st);
+    else if (COUT == 2 && Cin == 32 && v8)
+      direct_grid<COUT, 8, PXW, 32>(B, H, W, Cin, X, Wt, bias, relu, skip, out, out32, smem, st);
+    else if (v8)
+      direct_grid<COUT, 8, PXW, 0>(B, H, W, Cin, X, Wt, bias, relu, skip, out, out32, smem, st);
+    else
+      direct_grid<COUT, 2, PXW, 0>(B, H, W, Cin, X, Wt, bias, relu, skip, out, out32, smem, st);
   } else {
-    if (v8) direct_grid<COUT, 8, 1>(B, H, W, Cin, X, Wt, bias, relu, skip, out, out32, smem, st);
-    else direct_grid<COUT, 2, 1>(B, H, W, Cin, X, Wt, bias, relu, skip, out, out32, smem, st);
+    if (v8) direct_grid<COUT, 8, 1, 0>(B, H, W, Cin, X, Wt, bias, relu, skip, out, out32, smem, st);
+    else direct_grid<COUT, 2, 1, 0>(B, H, W, Cin, X, Wt, bias, relu, skip, out, out32, smem, st);
   }
   return check_launch("ws_conv_direct_kernel");
 }
@@ -1007,6 +1129,15 @@ extern "C" int pty_ws_conv3x3_direct(int32_t B, int32_t H, int32_t W, int32_t Ci
     return set_error(PTY_ERR_ARG, "pty_ws_conv3x3_direct: X and skip must be 4-byte, out and out32 16-byte aligned");
   if ((long long)B * H * W >= (1ll << 31)) return set_error(PTY_ERR_ARG, "pty_ws_conv3x3_direct: too many pixels");
   cudaStream_t st = (cudaStream_t)stream;
+  if (Cin == 32 && Cout == 2 && !out && !skip && W % 32 == 0 && ((uintptr_t)X & 15) == 0) {
+    const long long units = (long long)B * H * (W / 32);
+    const long long wpb = kC2Threads / 32;
+    long long g = (units + wpb - 1) / wpb;
+    if (g > 16 * 152) g = 16 * 152;
+    ws_conv_c32o2_kernel<<<(unsigned)g, kC2Threads, 0, st>>>(B, H, W, (const __nv_bfloat16*)X,
+                                                            (const __nv_bfloat16*)Wt, bias, relu, out32);
+    return check_launch("ws_conv_c32o2_kernel");
+  }
   switch (Cout) {
     case 2: return launch_direct<2>(B, H, W, Cin, X, Wt, bias, relu, skip, out, out32, st);
     case 4: return launch_direct<4>(B, H, W, Cin, X, Wt, bias, relu, skip, out, out32, st);

@@ -309,6 +309,41 @@ def test_conv_direct_matches_fp64(case):
     assert np.linalg.norm(got - ref) / np.linalg.norm(ref) < 3e-3
 
 
+@pytest.mark.parametrize("case", [(2, 128, 128, False), (1, 5, 64, True), (1, 6, 40, False)],
+                         ids=lambda c: "x".join(map(str, c[:3])))
+def test_conv_direct_last_layer_matches_fp64(case):
+    """The network's last layer (32 -> 2 channels, FP32 output only): the
+    four-lanes-per-pixel kernel with packed FP32x2 FMAs when W is a multiple
+    of 32 (the 40-wide case takes the general kernel), against float64 of the
+    same BF16 operands: FP32 accumulation in another order, within 1e-5."""
+    B, H, W, relu = case
+    cin, cout = 32, 2
+    lib = _native.load()
+    rng = np.random.default_rng(H + W)
+    xd = bf16(rng.standard_normal((B, H, W, cin)))
+    wd = bf16(rng.standard_normal((cout, 9 * cin)) * np.sqrt(2.0 / (9 * cin)))
+    b = (0.1 * rng.standard_normal(cout)).astype(np.float32)
+    bd = torch.from_numpy(b).to(dev())
+    out32 = torch.full((B, H, W, cout), float("nan"), dtype=torch.float32, device=dev())
+    _native.check(lib.pty_ws_conv3x3_direct(B, H, W, cin, cout, p(xd), p(wd), p(bd), int(relu), None, None,
+                                            p(out32), stream()))
+    xr = xd.float().cpu().numpy().astype(np.float64)
+    wr = wd.float().cpu().numpy().astype(np.float64)
+    xp = np.zeros((B, H + 2, W + 2, cin))
+    xp[:, 1:-1, 1:-1] = xr
+    z = np.zeros((B, H, W, cout))
+    wk = wr.reshape(cout, 3, 3, cin)
+    for ky in range(3):
+        for kx in range(3):
+            z += np.einsum("bhwc,oc->bhwo", xp[:, ky:ky + H, kx:kx + W], wk[:, ky, kx])
+    z += b
+    if relu:
+        z = np.maximum(z, 0)
+    got = out32.cpu().numpy().astype(np.float64)
+    assert np.all(np.isfinite(got))
+    assert np.linalg.norm(got - z) / np.linalg.norm(z) < 1e-5
+
+
 def test_conv_direct_rejects_unsupported_shapes():
     lib = _native.load()
     t = torch.zeros(1 << 16, dtype=torch.bfloat16, device=dev())
