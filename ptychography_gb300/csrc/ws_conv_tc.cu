@@ -18,7 +18,8 @@
 // C_out x 64 slice, both in the 128-byte-swizzled K-major layout the MMA
 // reads (64-byte swizzle when C_in = 32).  No im2col buffer is written.
 //
-// Roles (one CTA per SM, persistent over tiles, 192 threads):
+// Roles (persistent CTAs of 192 threads, one or two per SM by the size of the
+// layer's stage ring):
 //   warp 4, one lane: TMA producer over a ring of 4-8 stages;
 //   warp 5, one lane: MMA issuer; accumulators double-buffered in TMEM so the
 //     epilogue of one tile overlaps the MMAs of the next;
