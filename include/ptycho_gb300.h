@@ -292,6 +292,16 @@ int pty_ws_crop_center(int32_t nf, int32_t N0, int32_t N1, int32_t M0, int32_t M
                        const int32_t* frames, float scale, float* out, void* stream);
 int pty_ws_upsample_object(int32_t Uh, int32_t Vh, const void* Oh, int32_t U, int32_t V, int32_t f,
                            void* O, void* stream);
+/* Per-frame phase alignment of predicted exit waves before they are stitched
+ * again (a frame's far-field data fix its object phase only up to a
+ * constant): for frame f with object window starting at win[f] = (a, b)
+ * (device int32 [nf][2], the negated scan offsets of a plan),
+ *   z_f = sum_r psi_f(r) conj(P(r) O(a + r0, b + r1)),  psi_f *= conj(z_f) / |z_f|;
+ * psi complex64 [nf][M0][M1] in place, P complex64 [M0][M1], O complex64
+ * [U][V] (the current stitched object).  A frame whose window is not inside
+ * the object is left unchanged. */
+int pty_ws_align_phase(int32_t nf, int32_t M0, int32_t M1, const int32_t* win, int32_t U, int32_t V,
+                       const void* O, const void* P, void* psi, void* stream);
 /* The network's forward 3 x 3 convolution (zero padding) on the tensor cores
  * (tcgen05, accumulators in tensor memory, operands staged by TMA), with the
  * bias, activation and skip of pty_ws_bias_act fused:

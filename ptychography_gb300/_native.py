@@ -105,6 +105,8 @@ SIGNATURES = {
     "pty_ws_crop_center": [c_int32, c_int32, c_int32, c_int32, c_int32, c_void_p, c_void_p, ctypes.c_float,
                            c_void_p, c_void_p],
     "pty_ws_upsample_object": [c_int32, c_int32, c_void_p, c_int32, c_int32, c_int32, c_void_p, c_void_p],
+    "pty_ws_align_phase": [c_int32, c_int32, c_int32, c_void_p, c_int32, c_int32, c_void_p, c_void_p, c_void_p,
+                           c_void_p],
     "pty_shape_supported": [c_int32, c_int32],
     "pty_frame_tile_candidates": [c_int32, c_int32, ctypes.POINTER(c_int32), c_int32,
                                   ctypes.POINTER(c_int32)],

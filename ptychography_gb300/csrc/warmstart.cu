@@ -1157,6 +1157,57 @@ extern "C" int pty_ws_crop_center(int32_t nf, int32_t N0, int32_t N1, int32_t M0
   return ws_launched("ws_crop_center_kernel");
 }
 
+namespace pty {
+namespace {
+
+// Per-frame phase alignment of predicted exit waves before they are stitched
+// again: a frame's far-field data fix its object phase only up to a constant,
+// so the network's frames disagree by per-frame offsets.  For frame f with
+// object window starting at (a_f, b_f):
+//   z_f = sum_r psi_f(r) conj(P(r) O(a_f + r0, b_f + r1)),  psi_f *= conj(z_f) / |z_f|
+// (one block per frame, a fixed-order block sum: deterministic).
+constexpr int kAlignThreads = 256;
+__global__ void __launch_bounds__(kAlignThreads) ws_align_phase_kernel(int M0, int M1, const int* __restrict__ win,
+                                                                       int U, int V, const float2* __restrict__ O,
+                                                                       const float2* __restrict__ P,
+                                                                       float2* __restrict__ psi) {
+  __shared__ float2 red[kAlignThreads];
+  const int f = blockIdx.x;
+  const int a = win[2 * f], b = win[2 * f + 1];
+  if (a < 0 || b < 0 || a > U - M0 || b > V - M1) return;   // a window outside the object: frame left as is
+  const int npix = M0 * M1;
+  float2* fr = psi + (size_t)f * npix;
+  float2 acc = make_float2(0.f, 0.f);
+  for (int pix = threadIdx.x; pix < npix; pix += blockDim.x) {
+    const int r0 = pix / M1, r1 = pix - r0 * M1;
+    const float2 po = cmul(P[pix], O[(size_t)(a + r0) * V + b + r1]);
+    acc = cadd(acc, cmulc(fr[pix], po));
+  }
+  red[threadIdx.x] = acc;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) red[threadIdx.x] = cadd(red[threadIdx.x], red[threadIdx.x + s]);
+    __syncthreads();
+  }
+  const float2 z = red[0];
+  const float m = sqrtf(z.x * z.x + z.y * z.y);
+  const float2 rot = m > 0.f ? make_float2(z.x / m, -z.y / m) : make_float2(1.f, 0.f);
+  for (int pix = threadIdx.x; pix < npix; pix += blockDim.x) fr[pix] = cmul(fr[pix], rot);
+}
+
+}  // namespace
+}  // namespace pty
+
+extern "C" int pty_ws_align_phase(int32_t nf, int32_t M0, int32_t M1, const int32_t* win, int32_t U, int32_t V,
+                                  const void* O, const void* P, void* psi, void* stream) {
+  if (nf < 1 || M0 < 1 || M1 < 1 || U < M0 || V < M1 || !win || !O || !P || !psi)
+    return set_error(PTY_ERR_ARG, "pty_ws_align_phase: bad arguments");
+  if ((long long)M0 * M1 >= (1ll << 31)) return set_error(PTY_ERR_ARG, "pty_ws_align_phase: frame too large");
+  ws_align_phase_kernel<<<(unsigned)nf, kAlignThreads, 0, (cudaStream_t)stream>>>(
+      M0, M1, win, U, V, (const float2*)O, (const float2*)P, (float2*)psi);
+  return ws_launched("ws_align_phase_kernel");
+}
+
 extern "C" int pty_ws_upsample_object(int32_t Uh, int32_t Vh, const void* Oh, int32_t U, int32_t V, int32_t f,
                                       void* O, void* stream) {
   if (Uh < 1 || Vh < 1 || U < 1 || V < 1 || f < 1 || !Oh || !O)

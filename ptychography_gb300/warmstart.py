@@ -450,10 +450,18 @@ class _FramePlan:
     def __init__(self, n, N, U, V, R):
         self.lib = _native.load()
         R64 = np.ascontiguousarray(np.asarray(R)[:, :2], dtype=np.int64)
+        self._win_host = np.ascontiguousarray(-R64, dtype=np.int32)   # object window of each frame
+        self._win = None
         self.h = ctypes.c_void_p()
         _native.check(self.lib.pty_plan_create(ctypes.byref(_native.Geometry(n, N, N, U, V)),
                                                R64.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)),
                                                ctypes.byref(self.h)))
+
+    def windows(self, device):
+        """Each frame's object window start (-R), int32 (n, 2) on the device."""
+        if self._win is None:
+            self._win = _torch().from_numpy(self._win_host).to(device)
+        return self._win
 
     def close(self):
         if self.h:
@@ -527,13 +535,18 @@ def train(net, data, steps, batch=32, lr=1e-3, seed=0, log_every=0):
     return hist.sum(dim=1, dtype=torch.float64).cpu().numpy().tolist()
 
 
-def warm_start_object(net, I_dev, P_dev, plan_h, U, V, alpha=1e-10, heat=None, phasors=None):
+def warm_start_object(net, I_dev, P_dev, plan_h, U, V, alpha=1e-10, heat=None, phasors=None, align=0, win=None):
     """The initial object for ERA: the network's exit waves for the centred
     intensities I_dev (n, N, N) float32, stitched by the overlap update
     (psup_O, era.py:336-369) with the probe P_dev on the plan's U x V grid.
     plan_h must be a plan of exactly these n frames of N x N (its kernels
-    read n frames of I_dev; a mismatch raises ValueError).  Returns a
-    complex64 (U, V) device tensor."""
+    read n frames of I_dev; a mismatch raises ValueError).  With align > 0
+    and win (the frames' object window starts, int32 (n, 2) on the device)
+    each frame's phase offset against the stitched object is removed
+    (pty_ws_align_phase) and the frames stitched again, align times: a
+    frame's far-field data fix its object phase only up to a constant, so
+    the network's frames disagree by per-frame offsets.  Returns a complex64
+    (U, V) device tensor."""
     torch = _torch()
     g = _native.plan_geometry(plan_h)
     if (g.U, g.V) != (U, V):
@@ -543,16 +556,23 @@ def warm_start_object(net, I_dev, P_dev, plan_h, U, V, alpha=1e-10, heat=None, p
     if heat is None:
         heat = torch.empty((U, V), dtype=torch.float64, device=net.dev)
     _native.check(net.lib.pty_psup_O(plan_h, _p(psi), _p(P_dev), _p(heat), 1, alpha, _p(O), net._sp()))
+    if align > 0 and win is None:
+        raise ValueError("align needs the frames' object windows (win)")
+    n, N0, N1 = psi.shape
+    for _ in range(align):
+        _native.check(net.lib.pty_ws_align_phase(n, N0, N1, _p(win), U, V, _p(O), _p(P_dev), _p(psi), net._sp()))
+        _native.check(net.lib.pty_psup_O(plan_h, _p(psi), _p(P_dev), _p(heat), 0, alpha, _p(O), net._sp()))
     return O
 
 
-def initial_object(net, I, R, P, O_shape=None, alpha=1e-10):
+def initial_object(net, I, R, P, O_shape=None, alpha=1e-10, align=2):
     """The warm start for ``ERA(I, R, P, O, ...)`` on host arrays: centred
     intensities I (n, N, N), scan offsets R (n, 2) and the probe P (N, N),
     as ERA takes them.  R is shifted as ERA's preamble shifts it
     (era.py:504-505, on a copy); the object has ERA's default shape
-    (era.py:480-486) unless O_shape is given.  Returns a complex64 host array
-    to pass as ERA's O."""
+    (era.py:480-486) unless O_shape is given; the frames' phase offsets are
+    aligned `align` times (warm_start_object).  Returns a complex64 host
+    array to pass as ERA's O."""
     torch = _torch()
     I = np.asarray(I)
     n, N0, N1 = I.shape
@@ -568,7 +588,7 @@ def initial_object(net, I, R, P, O_shape=None, alpha=1e-10):
     try:
         I_d = torch.from_numpy(np.ascontiguousarray(I, dtype=np.float32)).to(net.dev)
         P_d = torch.from_numpy(np.ascontiguousarray(P, dtype=np.complex64)).to(net.dev)
-        O = warm_start_object(net, I_d, P_d, plan.h, U, V, alpha)
+        O = warm_start_object(net, I_d, P_d, plan.h, U, V, alpha, align=align, win=plan.windows(net.dev))
         return O.cpu().numpy()
     finally:
         plan.close()
@@ -640,7 +660,9 @@ class DownsampledStart:
 
     With cover (the default) only the frames covering_frames picks go
     through the network: each object pixel needs one good view for a start,
-    and on a dense scan that is a third to a quarter of the frames.
+    and on a dense scan that is a third to a quarter of the frames.  The
+    coarse frames' phase offsets are aligned against the stitched object
+    `align` times (warm_start_object) before the final stitch.
 
     Set-up (host work, once per scan: the coarse probe, the frame subset, the
     coarse plan and buffers) happens here; run() is device work plus the
@@ -648,9 +670,10 @@ class DownsampledStart:
     (host array), R the plan's scan offsets (n, 2) with maximum 0.
     """
 
-    def __init__(self, net, n, N0, N1, P, R, cover=True, spacing=0.75, graph=True):
+    def __init__(self, net, n, N0, N1, P, R, cover=True, spacing=0.75, graph=True, align=2):
         torch = _torch()
         self.graph = bool(graph)
+        self.align = int(align)
         self._graph = self._gkey = self._out = None
         if N0 != N1 or net.H != net.W or N0 % net.H:
             raise ValueError("frames must be square, a multiple of the network's %d x %d" % (net.H, net.W))
@@ -712,7 +735,7 @@ class DownsampledStart:
         _native.check(net.lib.pty_ws_crop_center(k, self.N, self.N, self.M, self.M, _p(I_dev), _p(self.sel), 1.0,
                                                  _p(self.I_s), sp))
         O_c = warm_start_object(net, self.I_s, self.P_s, self.plan.h, self.Uc, self.Vc, heat=self.heat,
-                                phasors=self.phasors)
+                                phasors=self.phasors, align=self.align, win=self.plan.windows(net.dev))
         if (self.Uc, self.Vc) != (self.Us, self.Vs):
             # the subset's object window inside the full scan's coarse object
             # (outside it: ones, the default start)
