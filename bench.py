@@ -1079,7 +1079,7 @@ def main():
         # about 10 s of single-core work: every frame of the workload once
         shard = 1024 if method == 6 else 100
         r, wall = cpu_oracle_rate(method, shard, 1)
-        cpu = {"value": round(r, 2), "unit": "frame-iters/s", "cores": 1, "kind": "port",
+        cpu = {"value": round(r, 2), "unit": "frame-iters/s", "cores": 1, "host_cpus": os.cpu_count(), "kind": "port",
                "sample": ("ERA m6 + DM m6, one iteration each, on all %d frames "
                           "(oracle NumPy port, single process), %.1f s" % (shard, wall))
                if method == 6 else "ERA m1 one iteration on the 100 frames, %.1f s" % wall}
