@@ -87,8 +87,11 @@ class Preamble:
                         dtype=self.cdt)
         if P is None:
             P = np.random.random(I[0].shape) + 1J * np.random.random(I[0].shape)
-        self.P = np.asarray(P).astype(self.cdt)
-        self.O = np.asarray(O).astype(self.cdt)
+        # the reference's astype copies (era.py:492-493) only shield the
+        # caller's arrays from its in-place updates; these are read once, to
+        # upload, so a matching dtype is not copied
+        self.P = np.asarray(P, dtype=self.cdt)
+        self.O = np.asarray(O, dtype=self.cdt)
         if self.P.shape != (N0, N1):
             raise ValueError("P must have the frame shape %s" % ((N0, N1),))
         scalar_mask = np.ndim(mask) == 0
@@ -307,8 +310,8 @@ class _Job:
                 _native.check(lib.pty_amp_from_intensity(self.plan, _ptr(I_d),
                                                          int(Iin.dtype == np.float64), _ptr(amp), sp))
             del I_d
-            self.O_d = torch.from_numpy(np.ascontiguousarray(pre.O.astype(np.complex64))).to(dev)
-            self.P_d = torch.from_numpy(np.ascontiguousarray(pre.P.astype(np.complex64))).to(dev)
+            self.O_d = torch.from_numpy(np.ascontiguousarray(pre.O, dtype=np.complex64)).to(dev)
+            self.P_d = torch.from_numpy(np.ascontiguousarray(pre.P, dtype=np.complex64)).to(dev)
             psi = torch.empty((n, N0, N1), dtype=torch.complex64, device=dev)
             if pre.background is not None:
                 bg_d = torch.from_numpy(pre.background).to(dev)
@@ -365,7 +368,8 @@ class _Job:
             "I": self._intensities(rt),
             "eMod": [rt(x) for x in self.emod.cpu().numpy()[:iters]],
             "eCon": [rt(x) for x in self.econ.cpu().numpy()[:iters]],
-            "heatmap": (self.heat.cpu().numpy().astype(rt)
+            # rounded to rt on the device: half the bytes to copy, no host pass
+            "heatmap": ((self.heat.to(_torch().float32) if rt == np.float32 else self.heat).cpu().numpy()
                         if (self.heat_valid and upd != "P") else None),
         }
         if self.bmean is not None:
