@@ -17,6 +17,10 @@
 // fill is the convolution's zero padding) and one brings the weights' matching
 // C_out x 64 slice, both in the 128-byte-swizzled K-major layout the MMA
 // reads (64-byte swizzle when C_in = 32).  No im2col buffer is written.
+// A layer whose tiles are single image rows of 64 input channels (C_out up
+// to 64) stages instead the tile's three input rows with a one-pixel halo
+// and keeps the nine weight taps resident: the kx shift of a tap is a start
+// one or two swizzled rows into the staged row (halo staging, see the kernel).
 //
 // Roles (persistent CTAs of 192 threads, one or two per SM by the size of the
 // layer's stage ring):
@@ -57,6 +61,7 @@ constexpr int kAccCols = 256;         // TMEM columns: two accumulators of up to
 // kTwoPerSm bytes runs two CTAs per SM (twice the TMA bytes in flight)
 constexpr size_t kMinSmem = 77 * 1024;
 constexpr size_t kTwoPerSm = 112 * 1024;
+constexpr size_t kHaloSmem = 227 * 1024;   // the halo-staging ring fills one SM's shared memory
 constexpr unsigned kSpinLimit = 1u << 26;
 
 struct ConvParams {
@@ -67,6 +72,7 @@ struct ConvParams {
   int chunks;              // ceil(Cin / 64)
   int chunk_ch;            // channels per chunk (64, or Cin when Cin < 64)
   int stages;              // TMA ring depth (<= kMaxStages)
+  int halo;                // one image row per tile, C_in = 64: halo-row staging (see the kernel)
   int relu;
   const float* bias;       // [Cout]
   const __nv_bfloat16* skip;   // [P][Cout] or nullptr
@@ -157,6 +163,12 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t addr, int swz_bytes) {
   const uint64_t mode = swz_bytes == 128 ? 2ull : 4ull;
   return (uint64_t)((addr >> 4) & 0x3FFF) | (1ull << 16) | (sbo << 32) | (1ull << 46) | (mode << 61);
 }
+// The same for a 128-byte-swizzled K-major matrix whose first row is not at
+// the start of a 1024-byte swizzle pattern.  The MMA forms the swizzle from
+// the absolute shared-memory address (as the TMA that wrote the rows did):
+// a start one or two rows in needs no base offset, just as the K steps'
+// starts 32-96 bytes into a row need none.
+__device__ __forceinline__ uint64_t smem_desc_row(uint32_t addr) { return smem_desc(addr, 128); }
 
 // Instruction descriptor, kind::f16: D f32 (bits 4-5 = 1), A and B bf16 (bits
 // 7-9 = 1, 10-12 = 1), both K-major (bits 15, 16 = 0), N >> 3 in bits 17-22,
@@ -199,7 +211,10 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
   for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
 }
 
+constexpr int kHaloPix = kTileM + 2;   // a halo row: the tile's 128 pixels and one on each side
+
 struct __align__(8) SmemCtl {
+  uint64_t wfull;                      // halo staging: the resident weights have landed
   uint64_t full[kMaxStages];
   uint64_t empty[kMaxStages];
   uint64_t acc_full[2];
@@ -222,7 +237,7 @@ __device__ __forceinline__ void tile_origin(const ConvParams& p, int t, int& b, 
 
 __global__ void __launch_bounds__(kThreads, 1)
     ws_conv_tc_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constant__ CUtensorMap tmW,
-                      const ConvParams p) {
+                      const __grid_constant__ CUtensorMap tmH, const ConvParams p) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   // stage buffers at a 1024-byte boundary (the 128-byte swizzle's atom)
   const uint32_t raw = smem_u32(smem_raw);
@@ -230,8 +245,18 @@ __global__ void __launch_bounds__(kThreads, 1)
   const int nst = p.stages;
   const int a_bytes = kTileM * p.chunk_ch * 2;            // 16 KB (8 KB when C_in = 32)
   const int b_bytes = p.Cout * p.chunk_ch * 2;
-  const int stage_bytes = ((a_bytes + b_bytes + 1023) / 1024) * 1024;
-  SmemCtl* ctl = reinterpret_cast<SmemCtl*>(base + nst * stage_bytes);
+  // Halo staging (a tile of one image row, C_in = 64): the nine taps' weights
+  // stay resident (wtap bytes each), and a stage holds the three input rows
+  // y0 - 1 .. y0 + 1 of the tile, 130 pixels each (hrow bytes); tap (ky, kx)
+  // reads row ky from pixel kx on, a start one or two 128-byte rows into the
+  // swizzle pattern (smem_desc_row).  Three 17 KB loads per tile instead of
+  // nine 16 KB loads plus the weights.
+  const int wtap = ((p.Cout * 128 + 1023) / 1024) * 1024;
+  const int hrow = ((kHaloPix * 128 + 1023) / 1024) * 1024;
+  unsigned char* wres = base;
+  unsigned char* ring = p.halo ? base + 9 * wtap : base;
+  const int stage_bytes = p.halo ? 3 * hrow : ((a_bytes + b_bytes + 1023) / 1024) * 1024;
+  SmemCtl* ctl = reinterpret_cast<SmemCtl*>(ring + nst * stage_bytes);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int swz = p.chunk_ch * 2;                         // 128 or 64 bytes per row
 
@@ -246,6 +271,7 @@ __global__ void __launch_bounds__(kThreads, 1)
       mbar_init(&ctl->acc_empty[i], 4);
     }
     mbar_init(&ctl->drain, 1);
+    mbar_init(&ctl->wfull, 1);
     ctl->abort = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
@@ -262,7 +288,7 @@ __global__ void __launch_bounds__(kThreads, 1)
   const uint32_t tmem = ctl->tmem_base;
   volatile int* abort = &ctl->abort;
   const int ksteps = p.chunk_ch / 16;
-  const int nstage_per_tile = 9 * p.chunks;
+  const int nstage_per_tile = p.halo ? 1 : 9 * p.chunks;
   const uint32_t idesc = instr_desc(kTileM, p.Cout);
   const uint32_t acc_stride = 128u;                        // column offset of the second accumulator
 
@@ -271,15 +297,26 @@ __global__ void __launch_bounds__(kThreads, 1)
     if (lane == 0) {
       int q = 0, rs = 0, rph = 0;   // ring position: q = stages used, rs = q mod nst, rph = its phase
       bool ok = true;
+      if (p.halo) {
+        // the nine taps' weights, once per CTA
+        mbar_expect_tx(&ctl->wfull, (unsigned)(9 * p.Cout * 128));
+        for (int tap = 0; tap < 9; ++tap) tma_load_2d(wres + tap * wtap, &tmW, &ctl->wfull, tap * p.Cin, 0);
+      }
       for (int t = blockIdx.x; t < p.tiles && ok; t += gridDim.x) {
         int b, y0, x0;
         tile_origin(p, t, b, y0, x0);
         for (int st = 0; st < nstage_per_tile && ok; ++st, ++q, rs = (rs + 1 == nst) ? 0 : rs + 1, rph ^= (rs == 0)) {
           const int s = rs, ph = rph;
           if (!mbar_wait(&ctl->empty[s], ph ^ 1, abort, p.err)) { ok = false; break; }
+          unsigned char* sa = ring + s * stage_bytes;
+          if (p.halo) {
+            mbar_expect_tx(&ctl->full[s], (unsigned)(3 * kHaloPix * 128));
+            for (int ky = 0; ky < 3; ++ky)
+              tma_load_4d(sa + ky * hrow, &tmH, &ctl->full[s], 0, x0 - 1, y0 + ky - 1, b);
+            continue;
+          }
           const int tap = st / p.chunks, ch = st % p.chunks;
           const int ky = tap / 3, kx = tap % 3;
-          unsigned char* sa = base + s * stage_bytes;
           unsigned char* sb = sa + a_bytes;
           mbar_expect_tx(&ctl->full[s], (unsigned)(a_bytes + b_bytes));
           tma_load_4d(sa, &tmX, &ctl->full[s], ch * p.chunk_ch, x0 + kx - 1, y0 + ky - 1, b);
@@ -295,6 +332,9 @@ __global__ void __launch_bounds__(kThreads, 1)
           for (unsigned i = 0; i < kSpinLimit && !mbar_try_wait(&ctl->full[s], ph); ++i) {
           }
         }
+        if (p.halo)
+          for (unsigned i = 0; i < kSpinLimit && !mbar_try_wait(&ctl->wfull, 0); ++i) {
+          }
       }
     }
   } else if (warp == 5) {
@@ -302,6 +342,8 @@ __global__ void __launch_bounds__(kThreads, 1)
     if (lane == 0) {
       int q = 0, rs = 0, rph = 0, local = 0;
       bool ok = true;
+      if (p.halo && !mbar_wait(&ctl->wfull, 0, abort, p.err)) ok = false;
+      if (p.halo) asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
       for (int t = blockIdx.x; t < p.tiles && ok; t += gridDim.x, ++local) {
         const int buf = local & 1, use = local >> 1;
         if (!mbar_wait(&ctl->acc_empty[buf], (use & 1) ^ 1, abort, p.err)) { ok = false; break; }
@@ -311,7 +353,19 @@ __global__ void __launch_bounds__(kThreads, 1)
           const int s = rs, ph = rph;
           if (!mbar_wait(&ctl->full[s], ph, abort, p.err)) { ok = false; break; }
           asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-          const uint32_t sa = smem_u32(base + s * stage_bytes);
+          const uint32_t sa = smem_u32(ring + s * stage_bytes);
+          if (p.halo) {
+            const uint32_t wb = smem_u32(wres);
+            for (int tap = 0; tap < 9; ++tap) {
+              const int ky = tap / 3, kx = tap % 3;
+              const uint32_t a0 = sa + ky * hrow + kx * 128, b0 = wb + tap * wtap;
+              for (int k = 0; k < 4; ++k)
+                mma_bf16(d, smem_desc_row(a0 + 32 * k), smem_desc(b0 + 32 * k, 128), idesc,
+                         (tap > 0 || k > 0) ? 1u : 0u);
+            }
+            mma_commit(&ctl->empty[s]);
+            continue;
+          }
           const uint32_t sb = sa + a_bytes;
           for (int k = 0; k < ksteps; ++k) {
             // K = 16 bf16 = 32 bytes along the swizzled row
@@ -333,13 +387,19 @@ __global__ void __launch_bounds__(kThreads, 1)
     int local = 0;
     for (int t = blockIdx.x; t < p.tiles; t += gridDim.x, ++local) {
       const int buf = local & 1, use = local >> 1;
-      if (!mbar_wait_warp(&ctl->acc_full[buf], use & 1, abort, p.err)) break;
-      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
       int b, y0, x0;
       tile_origin(p, t, b, y0, x0);
       const int r = warp * 32 + lane;                    // pixel row of the tile
       const int y = y0 + r / p.wbox, x = x0 + r % p.wbox;
       const size_t pix = ((size_t)b * p.H + y) * p.W + x;
+      // the first 32 skip channels are loaded while the tile's MMAs run
+      uint4 sk0[4];
+      if (p.skip && !p.out32) {
+#pragma unroll
+        for (int q4 = 0; q4 < 4; ++q4) sk0[q4] = *reinterpret_cast<const uint4*>(p.skip + pix * p.Cout + 8 * q4);
+      }
+      if (!mbar_wait_warp(&ctl->acc_full[buf], use & 1, abort, p.err)) break;
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
       const uint32_t tbase = tmem + buf * acc_stride + ((uint32_t)(warp * 32) << 16);
       for (int c0 = 0; c0 < p.Cout; c0 += 32) {
         float v[32];
@@ -363,7 +423,7 @@ __global__ void __launch_bounds__(kThreads, 1)
 #pragma unroll
         for (int q4 = 0; q4 < 4; ++q4) {
           uint4 skv = make_uint4(0u, 0u, 0u, 0u);
-          if (sk) skv = *reinterpret_cast<const uint4*>(sk + 8 * q4);
+          if (sk) skv = c0 == 0 ? sk0[q4] : *reinterpret_cast<const uint4*>(sk + 8 * q4);
           const __nv_bfloat162* s2 = reinterpret_cast<const __nv_bfloat162*>(&skv);
           uint4 ov, av;
           __nv_bfloat162* o2 = reinterpret_cast<__nv_bfloat162*>(&ov);
@@ -798,17 +858,40 @@ static int conv_tc(int32_t B, int32_t H, int32_t W, int32_t Cin, int32_t Cout, c
     if (r != CUDA_SUCCESS) return set_error(PTY_ERR_CUDA, "pty_ws_conv3x3_tc: weight tensor map");
   }
   size_t smem = 0;
-  p.stages = ring_depth(conv_tc_stage_bytes(Cin, Cout), &smem);
+  // halo staging for one-row tiles of 64 input channels whose nine weight
+  // taps fit beside a ring of at least two halo stages (C_out <= 64)
+  p.halo = (p.rows == 1 && Cin == kChunk && Cout <= 64) ? 1 : 0;
+  CUtensorMap tmH;
+  if (p.halo) {
+    // activations: dims (C, W, H, B), box (64, 130, 1, 1): a tile's input row with one pixel each side
+    const cuuint64_t dims[4] = {(cuuint64_t)Cin, (cuuint64_t)W, (cuuint64_t)H, (cuuint64_t)B};
+    const cuuint64_t strides[3] = {(cuuint64_t)Cin * 2, (cuuint64_t)W * Cin * 2, (cuuint64_t)H * W * Cin * 2};
+    const cuuint32_t box[4] = {(cuuint32_t)kChunk, (cuuint32_t)kHaloPix, 1, 1};
+    const cuuint32_t estr[4] = {1, 1, 1, 1};
+    CUresult r = encode(&tmH, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<void*>(X), dims, strides, box,
+                        estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                        CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return set_error(PTY_ERR_CUDA, "pty_ws_conv3x3_tc: halo tensor map");
+    const size_t wtap = (((size_t)Cout * 128 + 1023) / 1024) * 1024;
+    const size_t hrow = (((size_t)kHaloPix * 128 + 1023) / 1024) * 1024;
+    const size_t fixed = 9 * wtap + sizeof(SmemCtl) + 1024;
+    int n = kMaxStages;
+    while (n > 2 && n * 3 * hrow + fixed > kHaloSmem) --n;
+    p.stages = n;
+    smem = n * 3 * hrow + fixed;
+  } else {
+    p.stages = ring_depth(conv_tc_stage_bytes(Cin, Cout), &smem);
+  }
   static std::once_flag attr_once;
   static cudaError_t attr_err = cudaSuccess;
   std::call_once(attr_once, [] {
     attr_err = cudaFuncSetAttribute(ws_conv_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    (int)max_ring_smem(conv_tc_stage_bytes(64, kMaxCout)));
+                                    (int)kHaloSmem);
   });
   if (attr_err != cudaSuccess) return set_cuda_error(attr_err, "pty_ws_conv3x3_tc: smem attribute");
   const int slots = (smem <= kTwoPerSm ? 2 : 1) * sm_count();
   const int grid = p.tiles < slots ? p.tiles : slots;
-  ws_conv_tc_kernel<<<grid, kThreads, smem, (cudaStream_t)stream>>>(tmX, tmW, p);
+  ws_conv_tc_kernel<<<grid, kThreads, smem, (cudaStream_t)stream>>>(tmX, tmW, p.halo ? tmH : tmX, p);
   return check_launch("ws_conv_tc_kernel");
 }
 

@@ -59,10 +59,14 @@ def status_ok():
 
 
 # (B, H, W, C_in, C_out, relu, skip): the network's layers 1-4 at 128^2 frames,
-# plus a 256-wide image (two tiles per row) and a 32-channel-in layer with skip
+# plus a 256-wide image (two tiles per row) and a 32-channel-in layer with
+# skip; one-row tiles of 64 input channels and C_out <= 64 take the halo
+# staging (layer 4, the 256-wide 64 -> 64 case with halos across tiles, and a
+# 3-row image whose every tile meets the top or bottom edge)
 CASES = [(2, 64, 64, 32, 64, True, False), (2, 32, 32, 64, 128, True, False),
          (2, 64, 64, 128, 64, True, True), (2, 128, 128, 64, 32, True, True),
-         (1, 8, 256, 64, 96, False, False), (3, 16, 16, 32, 32, True, True)]
+         (1, 8, 256, 64, 96, False, False), (3, 16, 16, 32, 32, True, True),
+         (1, 4, 256, 64, 64, True, True), (2, 3, 128, 64, 32, False, False)]
 
 
 @pytest.mark.parametrize("case", CASES, ids=lambda c: "x".join(map(str, c[:5])))
