@@ -653,16 +653,17 @@ __global__ void __launch_bounds__(kThreads, 1)
   }
 }
 
-// dW[co][k] = sum over s < splits of partial[s][k][co], in split order
+// dW[co][k] = sum over s < splits of partial[s][k][co], in split order;
+// consecutive threads take consecutive co, so the partials are read coalesced
 __global__ void ws_wgrad_reduce_kernel(int splits, int kpad, int K9, int Cout, const float* __restrict__ part,
                                        float* __restrict__ dW) {
   const long long n = (long long)Cout * K9;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
        i += (long long)gridDim.x * blockDim.x) {
-    const int co = (int)(i / K9), k = (int)(i % K9);
+    const int k = (int)(i / Cout), co = (int)(i % Cout);
     float s = 0.f;
     for (int sp = 0; sp < splits; ++sp) s += part[((size_t)sp * kpad + k) * Cout + co];
-    dW[i] = s;
+    dW[(size_t)co * K9 + k] = s;
   }
 }
 
