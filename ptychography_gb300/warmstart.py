@@ -292,7 +292,7 @@ class WarmStartNet:
                                           _p(self.gw[i]), K, 1, splits, _p(part), sp))
         if not need_dx:
             return None
-        if getattr(self, "_fwd_inputs", None) is not None:
+        if tc:
             # input gradient as a convolution of dZ with the flipped weights:
             # the tensor-core kernel for layers 1-4, the direct one for the
             # 2-channel layer 5; no dcol buffer, no col2im
