@@ -117,6 +117,27 @@ def test_preamble_matches_oracle_rng_and_R_shift():
     np.testing.assert_allclose(pre.Pamp, st["Pamp"], rtol=1e-6)
 
 
+def test_preamble_leaves_the_callers_arrays_alone():
+    """The reference copies P and O (era.py:492-493) and shifts R in place
+    (era.py:504-505).  The preamble shifts R in place as well, converts P and
+    O only when their dtype differs (a matching array is used as it is: it
+    is only read, to upload), and writes to none of the caller's arrays."""
+    rng = np.random.default_rng(1)
+    I = (rng.random((4, 32, 32)) * 10).astype(np.float32)
+    R = -rng.integers(0, 6, (4, 2)) + 2
+    P = (rng.random((32, 32)) + 1j * rng.random((32, 32))).astype(np.complex64)
+    O = (rng.random((40, 40)) + 1j * rng.random((40, 40))).astype(np.complex64)
+    I0, P0, O0, R0 = I.copy(), P.copy(), O.copy(), R.copy()
+    pre = _engine.Preamble(I, R, P, O, 1, 1, None, 3, "single")
+    assert pre.P is P and pre.O is O                     # complex64 already: not copied
+    assert np.array_equal(R, R0 - R0.max(axis=0))        # shifted in place, as the reference does
+    assert np.array_equal(I, I0) and np.array_equal(P, P0) and np.array_equal(O, O0)
+    pre64 = _engine.Preamble(I, R.copy(), P, O, 1, 1, None, 3, "double")
+    assert pre64.P.dtype == np.complex128 and pre64.P is not P
+    assert np.array_equal(pre64.P, P0.astype(np.complex128))
+    assert np.array_equal(P, P0) and np.array_equal(O, O0)
+
+
 def test_engine_fails_loudly_without_gpu():
     import torch
     if torch.cuda.is_available():
