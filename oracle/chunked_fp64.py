@@ -18,8 +18,8 @@ as era.py:355-360 and 386-390 do, so results agree with the NumPy oracle to
 float64 rounding of the transforms (tests/test_chunked_oracle_cpu.py pins
 that on small problems).
 
-Supported: methods 1, 3, 4 and 6 (object, or object and probe, without or
-with a known background), OP_iters = 1, with or without probe centring
+Supported: methods 1-6 (object, probe, or object and probe, without or with
+a known background), OP_iters = 1, with or without probe centring
 (era.py:172-186, dm.py:65-82 / 115-127) and the far-field probe constraint
 Pmod_P (era.py:597-610) for the first Pmod_probe iterations.  Anything else
 raises NotImplementedError.
@@ -194,9 +194,12 @@ def _pmod_count(Pmod_probe, iters):
     return iters if x == float("inf") else max(0, min(iters, int(np.ceil(x))))
 
 
+_UPDATE = {1: "O", 2: "P", 3: "OP", 4: "O", 5: "P", 6: "OP"}   # era.py:451-456
+
+
 def _check(method):
-    if method not in (1, 3, 4, 6):
-        raise NotImplementedError("the chunked oracle restates methods 1, 3, 4 and 6")
+    if method not in _UPDATE:
+        raise NotImplementedError("the chunked oracle restates methods 1-6")
 
 
 def _econ(bak, cur):
@@ -208,7 +211,11 @@ def _econ(bak, cur):
 
 def _snap(update, O, P):
     torch = _torch()
-    return O.reshape(-1).clone() if update == "O" else torch.cat((O.reshape(-1), P.reshape(-1)))
+    if update == "O":
+        return O.reshape(-1).clone()
+    if update == "P":
+        return P.reshape(-1).clone()
+    return torch.cat((O.reshape(-1), P.reshape(-1)))
 
 
 def _mean_frames(pb, bg):
@@ -221,8 +228,13 @@ def _mean_frames(pb, bg):
 
 
 def _op_projection(pb, exits, O, P, update, P_heat, alpha):
-    """One consistency projection, update 'O' (cached heatmap) or 'OP' with
-    OP_iters = 1 (era.py:163-189, dm.py:56-85)."""
+    """One consistency projection, update 'O' (cached heatmap), 'P' (the
+    object's heatmap, which cannot change, recomputed: the same values as the
+    reference's cached one) or 'OP' with OP_iters = 1 (era.py:163-189,
+    dm.py:56-85)."""
+    if update == "P":
+        numP, Oheat = pb.psup_P(exits, O)
+        return O, numP / (Oheat + alpha), None, P_heat
     num, heat = pb.psup_O(exits, P)
     if P_heat is None:
         P_heat = heat
@@ -236,15 +248,15 @@ def _op_projection(pb, exits, O, P, update, P_heat, alpha):
 
 
 def ERA(pb, iters, method, alpha=1e-10, probe_centering=False, Pmod_probe=False):
-    """Error reduction (era.py:13-332) for methods 1, 3, 4, 6.  Returns
-    (O, P, info) with info keys eMod, eCon, heatmap and, for methods 4 and 6,
-    background (fftshift(b)^2 of the frames' common background)."""
+    """Error reduction (era.py:13-332) for methods 1-6.  Returns (O, P, info)
+    with info keys eMod, eCon, heatmap and, for methods 4-6, background
+    (fftshift(b)^2 of the frames' common background)."""
     torch = _torch()
     _check(method)
-    update = "O" if method in (1, 4) else "OP"
+    update = _UPDATE[method]
     use_bg = method >= 4
     if use_bg and pb.bg2d is None:
-        raise NotImplementedError("methods 4 and 6 need the known background here")
+        raise NotImplementedError("methods 4-6 need the known background here")
     O, P = pb.O0.clone(), pb.P0.clone()
     exits = torch.empty((pb.n, pb.N0, pb.N1), dtype=torch.complex128, device=pb.dev)
     for s, e in pb.chunks():
@@ -282,15 +294,15 @@ def ERA(pb, iters, method, alpha=1e-10, probe_centering=False, Pmod_probe=False)
 
 
 def DM(pb, iters, method, alpha=1e-10, probe_centering=False, Pmod_probe=False):
-    """Difference map (dm.py:13-333) for methods 1, 3, 4, 6.  Returns
-    (O, P, info) like ERA; info's background is the frames' mean of the last
-    metric projection (dm.py:308-318)."""
+    """Difference map (dm.py:13-333) for methods 1-6.  Returns (O, P, info)
+    like ERA; info's background is the frames' mean of the last metric
+    projection (dm.py:308-318)."""
     torch = _torch()
     _check(method)
-    update = "O" if method in (1, 4) else "OP"
+    update = _UPDATE[method]
     use_bg = method >= 4
     if use_bg and pb.bg2d is None:
-        raise NotImplementedError("methods 4 and 6 need the known background here")
+        raise NotImplementedError("methods 4-6 need the known background here")
     O, P = pb.O0.clone(), pb.P0.clone()
     exits = torch.empty((pb.n, pb.N0, pb.N1), dtype=torch.complex128, device=pb.dev)
     for s, e in pb.chunks():

@@ -3,10 +3,11 @@ oracle, which the golden fixtures pin to the reference itself.
 
 A small seeded problem (24 frames of 32 x 32 on a jittered raster, a random
 object and probe, a beamstop mask and a smooth background) runs three ERA and
-three DM iterations of each supported method through both; every output must
+three DM iterations of each method (1-6) through both; every output must
 agree to 1e-11 relative (float64 rounding of the transforms: the NumPy
-oracle uses pocketfft, torch its own FFT).  Frame chunks of 5 make every
-chunk loop run ragged.
+oracle uses pocketfft, torch its own FFT), with the two exceptions the test
+states (a settled eCon, DM method 5's background).  Frame chunks of 5 make
+every chunk loop run ragged.
 """
 import numpy as np
 import pytest
@@ -44,7 +45,7 @@ def _problem(seed=3):
 
 
 @pytest.mark.parametrize("algo", ["ERA", "DM"])
-@pytest.mark.parametrize("method", [1, 3, 4, 6])
+@pytest.mark.parametrize("method", [1, 2, 3, 4, 5, 6])
 def test_chunked_matches_numpy_oracle(algo, method):
     I, R, P0, O0, M, B = _problem()
     bg = B if method >= 4 else None
@@ -55,23 +56,33 @@ def test_chunked_matches_numpy_oracle(algo, method):
     if method in (1, 4):
         O_o, info_o = out
         P_o = P0
+    elif method in (2, 5):
+        P_o, info_o = out
+        O_o = O0
     else:
         O_o, P_o, info_o = out
     assert _rel(O_c.numpy(), O_o) < 1e-11
     assert _rel(P_c.numpy(), P_o) < 1e-11
     np.testing.assert_allclose(info_c["eMod"], info_o["eMod"], rtol=1e-11)
-    np.testing.assert_allclose(info_c["eCon"], info_o["eCon"], rtol=1e-9)
+    # eCon relative to the first iteration's: a probe-only ERA run settles in
+    # one step (eCon ~1e-11 after it), where only the absolute error means anything
+    np.testing.assert_allclose(info_c["eCon"], info_o["eCon"], rtol=1e-9, atol=1e-12 * info_o["eCon"][0])
     if method >= 4:
-        assert _rel(info_c["background"].numpy(), info_o["background"]) < 1e-11
+        # DM method 5's background recursion amplifies the two FFT libraries'
+        # last-bit differences: 1e-14, 3e-13, 9e-9 after 1, 2, 3 iterations
+        tol = 1e-7 if (algo, method) == ("DM", 5) else 1e-11
+        assert _rel(info_c["background"].numpy(), info_o["background"]) < tol
 
 
 def test_unsupported_options_raise():
     I, R, P0, O0, M, B = _problem()
     pb = ck.Problem(I, R, P0, O0, M, None, torch.device("cpu"), chunk=5)
     with pytest.raises(NotImplementedError):
-        ck.DM(pb, 1, 2)
+        ck.DM(pb, 1, 7)
     with pytest.raises(NotImplementedError):
-        ck.ERA(pb, 1, 4)
+        ck.ERA(pb, 1, 4)                        # a background method without the known background
+    with pytest.raises(NotImplementedError):
+        ck.DM(pb, 1, 5)
 
 
 @pytest.mark.parametrize("algo", ["ERA", "DM"])
