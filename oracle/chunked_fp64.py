@@ -19,10 +19,12 @@ float64 rounding of the transforms (tests/test_chunked_oracle_cpu.py pins
 that on small problems).
 
 Supported: methods 1-6 (object, probe, or object and probe, without or with
-a known background), OP_iters = 1, with or without probe centring
-(era.py:172-186, dm.py:65-82 / 115-127) and the far-field probe constraint
-Pmod_P (era.py:597-610) for the first Pmod_probe iterations.  Anything else
-raises NotImplementedError.
+a known background), OP_iters = k or (k, m) (k object / probe rounds every
+m-th iteration, the object alone in between, with the reference's cached
+heatmaps: era.py:163-189, dm.py:56-85 / 104-134), with or without probe
+centring (era.py:172-186, dm.py:65-82 / 115-127) and the far-field probe
+constraint Pmod_P (era.py:597-610) for the first Pmod_probe iterations.
+Anything else raises NotImplementedError.
 """
 import numpy as np
 
@@ -227,27 +229,42 @@ def _mean_frames(pb, bg):
     return acc / pb.n
 
 
-def _op_projection(pb, exits, O, P, update, P_heat, alpha):
-    """One consistency projection, update 'O' (cached heatmap), 'P' (the
-    object's heatmap, which cannot change, recomputed: the same values as the
-    reference's cached one) or 'OP' with OP_iters = 1 (era.py:163-189,
-    dm.py:56-85)."""
-    if update == "P":
-        numP, Oheat = pb.psup_P(exits, O)
-        return O, numP / (Oheat + alpha), None, P_heat
+def _op_iters(OP_iters):
+    """(rounds, every) from an int k or a pair (era.py:458-463)."""
+    if isinstance(OP_iters, (int, np.integer)):
+        return int(OP_iters), 1
+    k, m = (int(x) for x in OP_iters)
+    if k < 1 or m < 1:
+        raise NotImplementedError("OP_iters must be positive")
+    return k, m
+
+
+def _psup_O(pb, exits, P, P_heat, alpha):
+    """psup_O with the reference's heatmap cache: a given P_heat is used as
+    it is, even when P has changed since (era.py:336-369)."""
     num, heat = pb.psup_O(exits, P)
-    if P_heat is None:
-        P_heat = heat
-    O = num / (P_heat + alpha)
-    if update == "OP":
-        numP, Oheat = pb.psup_P(exits, O)
-        P = numP / (Oheat + alpha)
-        P_heat_out = None                         # recomputed every OP round
-        return O, P, heat, P_heat_out
-    return O, P, P_heat, P_heat
+    P_heat = heat if P_heat is None else P_heat
+    return num / (P_heat + alpha), P_heat
 
 
-def ERA(pb, iters, method, alpha=1e-10, probe_centering=False, Pmod_probe=False):
+def _psup_P(pb, exits, O, O_heat, alpha):
+    """psup_P with the reference's heatmap cache (era.py:371-400)."""
+    num, heat = pb.psup_P(exits, O)
+    O_heat = heat if O_heat is None else O_heat
+    return num / (O_heat + alpha), O_heat
+
+
+def _op_round(pb, exits, O, P, rounds, alpha):
+    """`rounds` alternating object and probe projections, heatmaps recomputed
+    each time; returns the last round's heatmaps (the object's from the probe
+    before its update), as era.py:166-171 leaves them."""
+    for _ in range(rounds):
+        O, Ph = _psup_O(pb, exits, P, None, alpha)
+        P, Oh = _psup_P(pb, exits, O, None, alpha)
+    return O, P, Ph, Oh
+
+
+def ERA(pb, iters, method, alpha=1e-10, probe_centering=False, Pmod_probe=False, OP_iters=1):
     """Error reduction (era.py:13-332) for methods 1-6.  Returns (O, P, info)
     with info keys eMod, eCon, heatmap and, for methods 4-6, background
     (fftshift(b)^2 of the frames' common background)."""
@@ -257,12 +274,13 @@ def ERA(pb, iters, method, alpha=1e-10, probe_centering=False, Pmod_probe=False)
     use_bg = method >= 4
     if use_bg and pb.bg2d is None:
         raise NotImplementedError("methods 4-6 need the known background here")
+    rounds, every = _op_iters(OP_iters)
     O, P = pb.O0.clone(), pb.P0.clone()
     exits = torch.empty((pb.n, pb.N0, pb.N1), dtype=torch.complex128, device=pb.dev)
     for s, e in pb.chunks():
         exits[s:e] = pb.make_exits(O, P, s, e)                  # era.py:536
     bg = pb.bg2d.expand(pb.n, pb.N0, pb.N1).clone() if use_bg else None
-    P_heat = heat_out = None
+    P_heat = O_heat = None
     npm = _pmod_count(Pmod_probe, iters)
     eMods, eCons = [], []
     for i in range(iters):
@@ -274,11 +292,18 @@ def ERA(pb, iters, method, alpha=1e-10, probe_centering=False, Pmod_probe=False)
             else:
                 exits[s:e], em = _pmod_1(pb, exits[s:e], pb.amp(s, e), alpha)
             emod += em
-        O, P, heat_out, P_heat = _op_projection(pb, exits, O, P, update, P_heat, alpha)
-        if update == "OP" and probe_centering:                  # era.py:172-186
-            cm = _probe_shift(P)
-            P, O = _roll2(P, (-cm[0], -cm[1])), _roll2(O, (-cm[0], -cm[1]))
-            heat_out = None
+        if update == "O":                                       # era.py:163 / 233
+            O, P_heat = _psup_O(pb, exits, P, P_heat, alpha)
+        elif update == "P":                                     # era.py:164 / 234
+            P, O_heat = _psup_P(pb, exits, O, O_heat, alpha)
+        elif i % every == 0:                                    # era.py:166-186
+            O, P, P_heat, O_heat = _op_round(pb, exits, O, P, rounds, alpha)
+            if probe_centering:
+                cm = _probe_shift(P)
+                P, O = _roll2(P, (-cm[0], -cm[1])), _roll2(O, (-cm[0], -cm[1]))
+                P_heat = O_heat = None
+        else:                                                   # era.py:188-189
+            O, P_heat = _psup_O(pb, exits, P, P_heat, alpha)
         if i < npm:                                             # era.py:193-194
             P = _pmod_P(pb, P, alpha)
         if use_bg:                                              # era.py:265-270
@@ -287,13 +312,13 @@ def ERA(pb, iters, method, alpha=1e-10, probe_centering=False, Pmod_probe=False)
             exits[s:e] = pb.make_exits(O, P, s, e)
         eCons.append(_econ(bak, _snap(update, O, P)))
         eMods.append(float(np.sqrt(emod / pb.I_norm)))
-    info = {"eMod": eMods, "eCon": eCons, "heatmap": heat_out}
+    info = {"eMod": eMods, "eCon": eCons, "heatmap": P_heat}
     if use_bg:
         info["background"] = torch.fft.fftshift(bg[0]) ** 2
     return O, P, info
 
 
-def DM(pb, iters, method, alpha=1e-10, probe_centering=False, Pmod_probe=False):
+def DM(pb, iters, method, alpha=1e-10, probe_centering=False, Pmod_probe=False, OP_iters=1):
     """Difference map (dm.py:13-333) for methods 1-6.  Returns (O, P, info)
     like ERA; info's background is the frames' mean of the last metric
     projection (dm.py:308-318)."""
@@ -303,12 +328,13 @@ def DM(pb, iters, method, alpha=1e-10, probe_centering=False, Pmod_probe=False):
     use_bg = method >= 4
     if use_bg and pb.bg2d is None:
         raise NotImplementedError("methods 4-6 need the known background here")
+    rounds, every = _op_iters(OP_iters)
     O, P = pb.O0.clone(), pb.P0.clone()
     exits = torch.empty((pb.n, pb.N0, pb.N1), dtype=torch.complex128, device=pb.dev)
     for s, e in pb.chunks():
         exits[s:e] = pb.make_exits(O, P, s, e)                  # era.py:536
     bg = pb.bg2d.expand(pb.n, pb.N0, pb.N1).clone() if use_bg else None
-    P_heat = heat_out = None
+    P_heat = O_heat = None
     b0 = None
     npm = _pmod_count(Pmod_probe, iters)
     eMods, eCons = [], []
@@ -318,13 +344,20 @@ def DM(pb, iters, method, alpha=1e-10, probe_centering=False, Pmod_probe=False):
             for s, e in pb.chunks():
                 exits[s:e], bg[s:e], _ = _pmod_7(pb, exits[s:e], bg[s:e], pb.amp(s, e), alpha)
         # main consistency projection (dm.py:56-85 / 174-202)
-        O, P, heat_out, P_heat = _op_projection(pb, exits, O, P, update, P_heat, alpha)
-        if update == "OP" and probe_centering:                  # dm.py:65-82 / 183-200
-            cm = _probe_shift(P)
-            P, O = _roll2(P, (-cm[0], -cm[1])), _roll2(O, (-cm[0], -cm[1]))
-            heat_out = None
-            for s, e in pb.chunks():
-                exits[s:e] = _roll2(exits[s:e], (-cm[0], -cm[1]))
+        if update == "O":
+            O, P_heat = _psup_O(pb, exits, P, P_heat, alpha)
+        elif update == "P":
+            P, O_heat = _psup_P(pb, exits, O, O_heat, alpha)
+        elif i % every == 0:
+            O, P, P_heat, O_heat = _op_round(pb, exits, O, P, rounds, alpha)
+            if probe_centering:                                 # dm.py:65-82 / 183-200
+                cm = _probe_shift(P)
+                P, O = _roll2(P, (-cm[0], -cm[1])), _roll2(O, (-cm[0], -cm[1]))
+                P_heat = O_heat = None
+                for s, e in pb.chunks():
+                    exits[s:e] = _roll2(exits[s:e], (-cm[0], -cm[1]))
+        else:
+            O, P_heat = _psup_O(pb, exits, P, P_heat, alpha)
         if i < npm:                                             # dm.py:88-89
             P = _pmod_P(pb, P, alpha)
         # difference-map update (dm.py:91-97 / 203-224), frame chunk by chunk:
@@ -346,11 +379,21 @@ def DM(pb, iters, method, alpha=1e-10, probe_centering=False, Pmod_probe=False):
             else:
                 ex0, _ = _pmod_1(pb, ex0, pb.amp(s, e), alpha)
                 exits[s:e] = ps + ex0
-        # metric projection (dm.py:104-137 / 231-271)
-        Os, Ps, _, P_heat = _op_projection(pb, exits, O.clone(), P.clone(), update, P_heat, alpha)
-        if update == "OP" and probe_centering:                  # dm.py:115-127 / 242-254
-            cm = _probe_shift(Ps)
-            Ps, Os = _roll2(Ps, (-cm[0], -cm[1])), _roll2(Os, (-cm[0], -cm[1]))
+        # metric projection (dm.py:104-137 / 231-271): from copies of O, P;
+        # an object-only step projects with P itself and shares the main
+        # branch's heatmap cache, an OP round keeps its heatmaps to itself
+        Os, Ps = O.clone(), P.clone()
+        if update == "O":
+            Os, P_heat = _psup_O(pb, exits, Ps, P_heat, alpha)
+        elif update == "P":
+            Ps, O_heat = _psup_P(pb, exits, Os, O_heat, alpha)
+        elif i % every == 0:
+            Os, Ps, _, _ = _op_round(pb, exits, Os, Ps, rounds, alpha)
+            if probe_centering:                                 # dm.py:115-127 / 242-254
+                cm = _probe_shift(Ps)
+                Ps, Os = _roll2(Ps, (-cm[0], -cm[1])), _roll2(Os, (-cm[0], -cm[1]))
+        else:
+            Os, P_heat = _psup_O(pb, exits, P, P_heat, alpha)
         if i < npm:                                             # dm.py:136-137
             Ps = _pmod_P(pb, Ps, alpha)
         if use_bg:
@@ -363,7 +406,7 @@ def DM(pb, iters, method, alpha=1e-10, probe_centering=False, Pmod_probe=False):
         eCons.append(_econ(bak, cur))                           # dm.py:142-149
         eMods.append(float(np.sqrt(emod / pb.I_norm)))
         bak = cur                                               # dm.py:158-160
-    info = {"eMod": eMods, "eCon": eCons, "heatmap": heat_out}
+    info = {"eMod": eMods, "eCon": eCons, "heatmap": P_heat}
     if use_bg:
         info["background"] = torch.fft.fftshift(b0) ** 2
     return O, P, info

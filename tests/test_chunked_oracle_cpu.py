@@ -122,3 +122,23 @@ def test_chunked_centring_and_probe_modulus(algo, method):
     a = np.abs(P_c.numpy()) ** 2
     com = (np.arange(32) @ a.sum(axis=1) / a.sum(), np.arange(32) @ a.sum(axis=0) / a.sum())
     assert abs(com[0] - 16) <= 1.0 and abs(com[1] - 16) <= 1.0
+
+
+@pytest.mark.parametrize("algo", ["ERA", "DM"])
+@pytest.mark.parametrize("method", [3, 6])
+@pytest.mark.parametrize("OP_iters", [(2, 1), (1, 3), (2, 3)])
+def test_chunked_op_iters(algo, method, OP_iters):
+    """OP_iters = (k, m): k object / probe rounds every m-th iteration and the
+    object alone (with the cached, possibly stale heatmap) in between, five
+    iterations so that both kinds run, against the NumPy oracle."""
+    I, R, P0, O0, M, B = _problem()
+    bg = B if method >= 4 else None
+    fn = getattr(orc, algo)
+    O_o, P_o, info_o = fn(I, R.copy(), P0.copy(), O0.copy(), 5, OP_iters=OP_iters, mask=M, background=bg,
+                          method=method, dtype="double")
+    pb = ck.Problem(I, R, P0, O0, M, bg, torch.device("cpu"), chunk=5)
+    O_c, P_c, info_c = getattr(ck, algo)(pb, 5, method, OP_iters=OP_iters)
+    assert _rel(O_c.numpy(), O_o) < 1e-11
+    assert _rel(P_c.numpy(), P_o) < 1e-11
+    np.testing.assert_allclose(info_c["eMod"], info_o["eMod"], rtol=1e-11)
+    np.testing.assert_allclose(info_c["eCon"], info_o["eCon"], rtol=1e-9, atol=1e-12 * info_o["eCon"][0])
