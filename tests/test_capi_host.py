@@ -19,6 +19,22 @@ def header_functions():
     return sorted(set(re.findall(r"^\s*(?:const\s+)?\w+\**\s+\**(pty_\w+)\s*\(", src, flags=re.M)))
 
 
+def test_header_is_plain_c(tmp_path):
+    """The boundary header needs no C++ and no CUDA headers: a C99 translation
+    unit that includes it compiles with warnings as errors (what a cgo or
+    JNI binding would compile)."""
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    src = tmp_path / "use_header.c"
+    src.write_text('#include "ptycho_gb300.h"\nint main(void) { return pty_version() == 0; }\n')
+    r = subprocess.run([cc, "-std=c99", "-Wall", "-Wextra", "-Werror", "-I", os.path.dirname(HEADER), "-c",
+                        str(src), "-o", str(tmp_path / "use_header.o")], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+
+
 def test_header_declares_entry_points():
     names = header_functions()
     for must in ("pty_plan_create", "pty_era", "pty_dm", "pty_pmod_1", "pty_psup_O", "pty_psup_P"):
